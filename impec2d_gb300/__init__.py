@@ -1,0 +1,283 @@
+"""GB300-native Impec2D IMPES engine: Python binding of the C ABI (include/impec2d.h).
+
+The numerical work runs in hand-written CUDA kernels for sm_103a inside
+``libimpec2d.so``; this module only loads that library with ctypes and passes device
+pointers (torch CUDA tensors) and plain scalars across.  There is no CPU fallback:
+if the library is missing or no GPU is present, calls raise.
+
+Device layout (no ghost cells): cell fields ``(N1, N2)``, x-face field ``u``
+``(N1+1, N2)``, y-face field ``v`` ``(N1, N2+1)``, all float64, row-major.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libimpec2d.so")
+
+MEANCONC, HARMONIC = 0, 1
+EXPLICIT, CRANKNICOLSON = 0, 1
+ALTERNATING, X_FIRST, Y_FIRST, STRANG, SYMMETRIC_PARALLEL = 0, 1, 2, 3, 4
+UPWINDSPLIT, MUSCL = 0, 4
+PARALLEL, DIAGONAL, HORIZONTAL = 0, 1, 2
+BC_NEUMANN, BC_PERIODIC = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOT_CONVERGED", 4: "ERR_NAN", 5: "ERR_NO_DEVICE",
+          6: "ERR_CONFIG"}
+
+
+class ImpecError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {STATUS.get(status, status)}: {last_error()}")
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("N1", C.c_int), ("N2", C.c_int),
+        ("x_lb", C.c_double), ("x_ub", C.c_double), ("y_lb", C.c_double), ("y_ub", C.c_double),
+        ("mu_res", C.c_double), ("mu_inj", C.c_double),
+        ("avgproc", C.c_int), ("nu", C.c_double),
+        ("porosity", C.c_double), ("cfl", C.c_double), ("inj_fluid_conc", C.c_double), ("I", C.c_double),
+        ("diffusion", C.c_int), ("alpha_l", C.c_double), ("alpha_t", C.c_double), ("Dm", C.c_double),
+        ("ptype", C.c_int), ("dt_diff_limit", C.c_double),
+        ("dim_splitting", C.c_int), ("hmtype", C.c_int), ("stype", C.c_int),
+        ("is_test", C.c_int), ("testno", C.c_int), ("bc", C.c_int),
+        ("eps", C.c_double), ("para_eps", C.c_double),
+        ("peaceman_guard", C.c_int), ("cfl_porosity", C.c_int), ("precision", C.c_int),
+        ("max_cycles", C.c_int), ("warm_start", C.c_int),
+    ]
+
+
+class StepInfo(C.Structure):
+    _fields_ = [
+        ("t", C.c_double), ("dt", C.c_double), ("total_outflux", C.c_double), ("relres", C.c_double),
+        ("mass_err", C.c_double),
+        ("counter", C.c_int), ("its", C.c_int), ("para_its", C.c_int), ("prev_first_sweep", C.c_int),
+        ("clipped", C.c_int),
+    ]
+
+
+_lib = None
+_VP = C.c_void_p
+_PI = C.POINTER(C.c_int)
+_PD = C.POINTER(C.c_double)
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "impec_last_error": (C.c_char_p, []),
+    "impec_default_params": (None, [C.POINTER(Params), C.c_int, C.c_int]),
+    "impec_ctx_create": (C.c_int, [C.POINTER(Params), _VP, C.POINTER(_VP)]),
+    "impec_ctx_destroy": (C.c_int, [_VP]),
+    "impec_ctx_params": (C.c_int, [_VP, C.POINTER(Params)]),
+    "impec_set_permeability": (C.c_int, [_VP, _VP, _VP]),
+    "impec_set_source": (C.c_int, [_VP, _VP]),
+    "impec_pressure_solve": (C.c_int, [_VP, _VP, _VP, C.c_double, _PI, _PD]),
+    "impec_face_mobility": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "impec_pressure_apply": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "impec_velocity": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "impec_max_stable_dt": (C.c_int, [_VP, _VP, _VP, _PD]),
+    "impec_tr_integrate": (C.c_int, [_VP, _VP, C.c_double, _PD]),
+    "impec_advect_x": (C.c_int, [_VP, _VP, _VP, C.c_double]),
+    "impec_advect_y": (C.c_int, [_VP, _VP, _VP, C.c_double]),
+    "impec_advect_split": (C.c_int, [_VP, _VP, _VP, _VP, C.c_double, _PI]),
+    "impec_dispersion_cn": (C.c_int, [_VP, _VP, _VP, _VP, C.c_double, C.c_double, _PI, _PD]),
+    "impec_hyperbolic_solve": (C.c_int, [_VP, _VP, _VP, _VP, C.c_double, _PI, _PD]),
+    "impec_diagnostics": (C.c_int, [_VP, _VP, _VP, _VP, _PD]),
+    "impec_state": (C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP)]),
+    "impec_step": (C.c_int, [_VP, C.c_double, C.POINTER(StepInfo)]),
+    "impec_run_steps": (C.c_int, [_VP, C.c_int, C.POINTER(StepInfo)]),
+    "impec_state_upload": (C.c_int, [_VP, _PD, _PD, C.c_int]),
+    "impec_state_download": (C.c_int, [_VP, _PD, _PD, _PD, C.c_int]),
+    "impec_set_time": (C.c_int, [_VP, C.c_double]),
+    "impec_velocity_upload": (C.c_int, [_VP, _PD, C.c_int]),
+    "impec_pressure_upload": (C.c_int, [_VP, _PD, C.c_int]),
+    "impec_set_pin_kappa": (C.c_int, [_VP, C.c_double]),
+    "impec_cfg_load": (C.c_int, [C.c_char_p, C.POINTER(Params), _PD, _PD]),
+    "impec_cfg_source": (C.c_int, [C.c_char_p, _PD]),
+    "impec_run_cfg": (C.c_int, [C.c_char_p, C.c_int]),
+}
+
+
+def load_cfg(path: str):
+    """Parse a reference .cfg file: returns (Params, tstart, tfinal)."""
+    P = Params()
+    t0, t1 = C.c_double(), C.c_double()
+    _chk(lib().impec_cfg_load(path.encode(), C.byref(P), C.byref(t0), C.byref(t1)), f"cfg_load({path})")
+    return P, t0.value, t1.value
+
+
+def cfg_source(path: str, N1: int, N2: int):
+    """Source term q (numpy, N1*N2) of a .cfg's wells."""
+    import numpy as np
+    q = np.zeros(N1 * N2)
+    _chk(lib().impec_cfg_source(path.encode(), q.ctypes.data_as(_PD)), f"cfg_source({path})")
+    return q
+
+
+def lib():
+    """Load libimpec2d.so (built by ``impec2d_gb300.build.build()``); raise if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run impec2d_gb300.build.build() first "
+                               "(the engine has no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    try:
+        return lib().impec_last_error().decode()
+    except Exception:  # noqa: BLE001 - error path of an error path
+        return ""
+
+
+def _chk(status: int, what: str):
+    if status != 0:
+        raise ImpecError(status, what)
+
+
+def default_params(N1: int, N2: int, **kw) -> Params:
+    P = Params()
+    lib().impec_default_params(C.byref(P), N1, N2)
+    for k, v in kw.items():
+        if not hasattr(P, k):
+            raise AttributeError(k)
+        setattr(P, k, v)
+    return P
+
+
+def _p(t):
+    if t is None:
+        return None
+    import torch
+    assert t.is_cuda and t.dtype == torch.float64 and t.is_contiguous(), "float64 contiguous CUDA tensor expected"
+    return C.c_void_p(t.data_ptr())
+
+
+class Context:
+    """One grid's device workspaces (C handle ``impec_ctx``)."""
+
+    def __init__(self, P: Params, stream: int | None = None):
+        self.P = P
+        h = C.c_void_p()
+        _chk(lib().impec_ctx_create(C.byref(P), C.c_void_p(stream) if stream else None, C.byref(h)), "ctx_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().impec_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    def set_source(self, q):
+        _chk(lib().impec_set_source(self.h, _p(q)), "set_source")
+
+    def set_permeability(self, K11, K22=None):
+        _chk(lib().impec_set_permeability(self.h, _p(K11), _p(K22)), "set_permeability")
+
+    def pressure_solve(self, c, p, tol=None, check=True):
+        cyc, rr = C.c_int(), C.c_double()
+        s = lib().impec_pressure_solve(self.h, _p(c), _p(p), self.P.eps if tol is None else tol, C.byref(cyc),
+                                       C.byref(rr))
+        if check:
+            _chk(s, "pressure_solve")
+        return cyc.value, rr.value, s
+
+    def face_mobility(self, c, lamx, lamy):
+        _chk(lib().impec_face_mobility(self.h, _p(c), _p(lamx), _p(lamy)), "face_mobility")
+
+    def pressure_apply(self, c, x, y):
+        _chk(lib().impec_pressure_apply(self.h, _p(c), _p(x), _p(y)), "pressure_apply")
+
+    def velocity(self, p, c, u, v):
+        _chk(lib().impec_velocity(self.h, _p(p), _p(c), _p(u), _p(v)), "velocity")
+
+    def max_stable_dt(self, u, v) -> float:
+        dt = C.c_double()
+        _chk(lib().impec_max_stable_dt(self.h, _p(u), _p(v), C.byref(dt)), "max_stable_dt")
+        return dt.value
+
+    def tr_integrate(self, c, dt) -> float:
+        tmo = C.c_double()
+        _chk(lib().impec_tr_integrate(self.h, _p(c), dt, C.byref(tmo)), "tr_integrate")
+        return tmo.value
+
+    def advect_x(self, c, u, dt):
+        _chk(lib().impec_advect_x(self.h, _p(c), _p(u), dt), "advect_x")
+
+    def advect_y(self, c, v, dt):
+        _chk(lib().impec_advect_y(self.h, _p(c), _p(v), dt), "advect_y")
+
+    def advect_split(self, c, u, v, dt, prev_first_sweep=1) -> int:
+        pfs = C.c_int(prev_first_sweep)
+        _chk(lib().impec_advect_split(self.h, _p(c), _p(u), _p(v), dt, C.byref(pfs)), "advect_split")
+        return pfs.value
+
+    def dispersion_cn(self, c, u, v, dt, tol=None):
+        its, rr = C.c_int(), C.c_double()
+        _chk(lib().impec_dispersion_cn(self.h, _p(c), _p(u), _p(v), dt, self.P.para_eps if tol is None else tol,
+                                       C.byref(its), C.byref(rr)), "dispersion_cn")
+        return its.value, rr.value
+
+    def hyperbolic_solve(self, c, u, v, dt, prev_first_sweep=1, outflux=0.0):
+        pfs, of = C.c_int(prev_first_sweep), C.c_double(outflux)
+        _chk(lib().impec_hyperbolic_solve(self.h, _p(c), _p(u), _p(v), dt, C.byref(pfs), C.byref(of)),
+             "hyperbolic_solve")
+        return pfs.value, of.value
+
+    def diagnostics(self, c, u, v):
+        out = (C.c_double * 5)()
+        _chk(lib().impec_diagnostics(self.h, _p(c), _p(u), _p(v), out), "diagnostics")
+        return list(out)
+
+    def state_ptrs(self):
+        ps = [C.c_void_p() for _ in range(5)]
+        _chk(lib().impec_state(self.h, *[C.byref(x) for x in ps]), "state")
+        return [x.value for x in ps]
+
+    def set_time(self, t0: float):
+        _chk(lib().impec_set_time(self.h, t0), "set_time")
+
+    def step(self, t_clip=-1.0) -> StepInfo:
+        info = StepInfo()
+        _chk(lib().impec_step(self.h, t_clip, C.byref(info)), "step")
+        return info
+
+    def run_steps(self, n: int) -> StepInfo:
+        info = StepInfo()
+        _chk(lib().impec_run_steps(self.h, n, C.byref(info)), "run_steps")
+        return info
+
+    def upload(self, c_host=None, q_host=None, ghost=2):
+        import numpy as np
+
+        def ptr(a):
+            if a is None:
+                return None
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+            return a.ctypes.data_as(_PD)
+        _chk(lib().impec_state_upload(self.h, ptr(c_host), ptr(q_host), ghost), "state_upload")
+
+    def download(self, c_host=None, p_host=None, v_host=None, ghost=2):
+        import numpy as np
+
+        def ptr(a):
+            if a is None:
+                return None
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+            return a.ctypes.data_as(_PD)
+        _chk(lib().impec_state_download(self.h, ptr(c_host), ptr(p_host), ptr(v_host), ghost), "state_download")

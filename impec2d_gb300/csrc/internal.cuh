@@ -1,0 +1,146 @@
+// Internal declarations of the GB300 Impec2D engine (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/impec2d.h"
+
+namespace impec {
+
+// ---------------------------------------------------------------- error handling
+void set_error(const std::string& msg);
+#define IMPEC_CUDA_TRY(expr)                                                                   \
+    do {                                                                                       \
+        cudaError_t _e = (expr);                                                               \
+        if (_e != cudaSuccess) {                                                               \
+            ::impec::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e) + " at " +   \
+                               __FILE__ + ":" + std::to_string(__LINE__));                     \
+            return IMPEC_ERR_CUDA;                                                             \
+        }                                                                                      \
+    } while (0)
+#define IMPEC_LAUNCH_CHECK() IMPEC_CUDA_TRY(cudaGetLastError())
+#define IMPEC_TRY(expr)                          \
+    do {                                         \
+        impec_status _s = (expr);                \
+        if (_s != IMPEC_OK) return _s;           \
+    } while (0)
+
+// ---------------------------------------------------------------- grid constants
+// Trigonometric constants of the rotated (diagonal) stencil, src/EllipticSolver.cpp:59-100.
+struct Geo {
+    double dx, dy, dA, dxi, deta, secamt2, cosa2, sina2, costsina, cosasint, cost2, sint2, cosa,
+        sint, cost, sina, mob1over4;
+};
+Geo make_geo(const impec_params& P);
+
+// Reflection of cell and face indices that reproduces the reference ghost fills
+// (src/Util.cpp:215-438): scalars are mirrored about the boundary face (even), the normal
+// velocity component is mirrored with a sign change about the boundary face (odd).
+__host__ __device__ inline int refl_cell(int i, int n) { return i < 0 ? -1 - i : (i >= n ? 2 * n - 1 - i : i); }
+__host__ __device__ inline int wrap_cell(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+// Face index f in [0, n]; returns index in range and sets sign to -1 where reflected.
+__host__ __device__ inline int refl_face(int f, int n, double& sign) {
+    if (f < 0) { sign = -sign; return -f; }
+    if (f > n) { sign = -sign; return 2 * n - f; }
+    return f;
+}
+__host__ __device__ inline int wrap_face(int f, int n) { return f < 0 ? f + n : (f > n ? f - n : f); }
+
+// ---------------------------------------------------------------- multigrid level
+enum LevelKind { FACE5 = 5, EXP9 = 9 };
+struct Level {
+    int n1 = 0, n2 = 0, kind = FACE5;
+    __host__ __device__ size_t n() const { return (size_t)n1 * n2; }
+    // FP64 operator (integrated, positive-definite sign convention)
+    double* tx = nullptr;    // FACE5: (n1+1)*n2 x-face transmissibilities (boundary faces 0)
+    double* ty = nullptr;    // FACE5: n1*(n2+1)
+    double* a9 = nullptr;    // EXP9: 9 planes of n1*n2, folded (no coupling outside the grid)
+    double* idiag = nullptr; // 1 / diagonal
+    double *x = nullptr, *b = nullptr;
+    // FP32 copies for the mixed-precision cycle
+    float *tx32 = nullptr, *ty32 = nullptr, *a932 = nullptr, *idiag32 = nullptr;
+    float *x32 = nullptr, *b32 = nullptr;
+};
+
+// Device-resident scalars of a step (so a step needs no host round trip).
+struct DevScalars {
+    double dt, t, maxvel, tmo_pre, tmo_post, total_outflux;
+    double fsum, fnorm2, rnorm2, pin_value;  // fsum,fnorm2 adjacent: written as a pair
+    double red[8];
+    int cycles, flags;
+};
+
+}  // namespace impec
+
+struct impec_ctx {
+    impec_params P;
+    impec::Geo G;
+    cudaStream_t stream = nullptr;
+    int device = 0, num_sms = 148;
+    // resident state
+    double *c = nullptr, *p = nullptr, *u = nullptr, *v = nullptr, *q = nullptr;
+    double *K11 = nullptr, *K22 = nullptr;  // owned copies, or nullptr (K = 1)
+    // pressure operator
+    double *muK11 = nullptr, *muK22 = nullptr;    // per-cell mu/K
+    double *lamx = nullptr, *lamy = nullptr;      // face mobilities (reference KoverMu)
+    double *cm11 = nullptr, *cm22 = nullptr, *cm12 = nullptr;  // corner tensors (nu < 1)
+    double *f = nullptr, *r = nullptr;            // integrated rhs, FP64 residual
+    std::vector<impec::Level> L;
+    double* dense_inv = nullptr;                  // coarsest-level inverse (n x n)
+    int dense_n = 0;
+    int pin_i = 1, pin_j = 1;
+    double pin_kappa = 1.0;
+    // transport scratch
+    double *t1 = nullptr, *t2 = nullptr, *t3 = nullptr;
+    // wells (TR integrator)
+    int nwells = 0;
+    int* well_idx = nullptr;
+    double* well_q = nullptr;
+    // dispersion
+    double *dfx = nullptr, *dfy = nullptr;        // Peaceman tensors at x-faces (d11,d12) and y-faces (d22,d21)
+    double *cn_a9 = nullptr, *cn_b = nullptr, *cn_idiag = nullptr;
+    // reductions
+    double* partials = nullptr;                   // [8][max_blocks]
+    unsigned* counter = nullptr;
+    int max_blocks = 0;
+    impec::DevScalars* dscal = nullptr;
+    impec::DevScalars* hscal = nullptr;           // pinned host mirror
+    // run state
+    double t = 0, t0 = 0, total_outflux = 0;
+    int counter_steps = 0, prev_first_sweep = 1, last_its = 0, last_para_its = 0;
+    double last_relres = 0;
+    bool have_source = false;
+};
+
+namespace impec {
+// pressure.cu
+impec_status pressure_setup(impec_ctx* ctx, const double* c);
+impec_status pressure_solve(impec_ctx* ctx, const double* c, double* p, double tol, int* cycles, double* relres);
+impec_status pressure_alloc(impec_ctx* ctx);
+void pressure_free(impec_ctx* ctx);
+impec_status face_mobility(impec_ctx* ctx, const double* c);
+impec_status pressure_apply_ref(impec_ctx* ctx, const double* x, double* y);
+// elliptic velocity
+impec_status velocity(impec_ctx* ctx, const double* p, const double* c, double* u, double* v);
+impec_status max_stable_dt_dev(impec_ctx* ctx, const double* u, const double* v);
+// transport.cu
+impec_status tr_integrate_dev(impec_ctx* ctx, double* c, double dt_scale, const double* dt_dev, int slot);
+impec_status advect_x_dev(impec_ctx* ctx, const double* cin, double* cout, const double* u, double dt_scale,
+                          const double* dt_dev, const double* cghost = nullptr);
+impec_status advect_y_dev(impec_ctx* ctx, const double* cin, double* cout, const double* v, double dt_scale, const double* dt_dev);
+impec_status advect_split_dev(impec_ctx* ctx, double* c, const double* u, const double* v, const double* dt_dev, int* pfs);
+impec_status average_dev(impec_ctx* ctx, double* c, const double* a, const double* b);
+// dispersion.cu
+impec_status dispersion_cn_dev(impec_ctx* ctx, double* c, const double* u, const double* v, double dt_scale,
+                               const double* dt_dev, double tol, int* its, double* relres);
+// step.cu
+impec_status hyperbolic_solve_dev(impec_ctx* ctx, double* c, const double* u, const double* v, const double* dt_dev,
+                                  int* pfs);
+// reductions (common.cu)
+impec_status reduce_launch_sum(impec_ctx* ctx, const double* x, size_t n, double* out_dev);
+impec_status sync_scalars(impec_ctx* ctx);
+}  // namespace impec

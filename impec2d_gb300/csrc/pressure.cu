@@ -1,0 +1,838 @@
+// Pressure equation: mobility, operator assembly, multigrid solve, Darcy velocities.
+//
+// The reference assembles the nu-weighted 9-point (nu < 1) or 5-point (nu = 1) operator with
+// Neumann folding and one Dirichlet pin at cell (1,1) (src/MGSolver.cpp:268-570) and solves
+// it with HYPRE PCG + SMG (:594-629).  Here the same pinned system is solved as follows:
+// every non-pinned row has zero row sum, so with b~ = b except b~(pin) = -sum_{k != pin} b(k)
+// the singular Neumann system A_N x = b~ is consistent; any solution shifted by
+// (p_pin - x_pin) satisfies all rows of the pinned system.  The consistent singular system is
+// solved by geometric multigrid (cell-centred, Galerkin coarse operators from 2x2
+// aggregation scaled by 1/2, red-black / four-colour Gauss-Seidel, summed restriction,
+// bilinear prolongation, dense coarsest solve with one unknown fixed).
+//
+// Internally the operator is stored in integrated form with positive diagonal:
+// A_int = -dA * A_ref, f = dA * q, so that ||f - A_int x|| / ||f|| equals the reference's
+// relative residual ||b - A x|| / ||b||.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "internal.cuh"
+#include "reduce.cuh"
+
+namespace impec {
+
+constexpr int BX = 32, BY = 8;
+static inline dim3 grid2(int n1, int n2) { return dim3((n2 + BX - 1) / BX, (n1 + BY - 1) / BY); }
+#define IX(i, j, n2) ((size_t)(i) * (n2) + (j))
+
+// ---------------------------------------------------------------- mobility
+// Cell value w = mu/K (harmonic averaging) or K/mu (arithmetic averaging), where
+// mu(c) = 1/(x^4) * mu_res, x = 1 - c + M^(1/4) c   (src/EllipticSolver.cpp:692-695).
+__global__ void k_cell_w(int n1, int n2, const double* __restrict__ c, const double* __restrict__ K1,
+                         const double* __restrict__ K2, double m14, double mu_res, int harmonic,
+                         double* __restrict__ w1, double* __restrict__ w2) {
+    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    if (i >= n1 || j >= n2) return;
+    size_t k = IX(i, j, n2);
+    double cc = c[k];
+    double x = __dadd_rn(1. - cc, __dmul_rn(m14, cc));  // no FMA: same rounding as the reference
+    double mu = 1. / (x * x * x * x) * mu_res;
+    double a = K1 ? K1[k] : 1.0;
+    w1[k] = harmonic ? (K1 ? mu / a : mu) : (K1 ? a / mu : 1.0 / mu);
+    if (w2) {
+        double b = K2[k];
+        w2[k] = harmonic ? mu / b : b / mu;
+    }
+}
+
+// Face mobilities KoverMu_11_im12j / KoverMu_22_ijm12 (src/EllipticSolver.cpp:478-524),
+// neighbours outside the grid mirrored (FillGhostCellsNeumannScalar).
+__global__ void k_face_lam(int n1, int n2, const double* __restrict__ w1, const double* __restrict__ w2,
+                           int harmonic, double* __restrict__ lamx, double* __restrict__ lamy) {
+    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    if (i <= n1 && j < n2) {  // x-face between cells (i-1,j) and (i,j)
+        double a = w1[IX(refl_cell(i - 1, n1), j, n2)], b = w1[IX(refl_cell(i, n1), j, n2)];
+        lamx[IX(i, j, n2)] = harmonic ? 2. / (a + b) : 1. / 2 * (a + b);
+    }
+    if (i < n1 && j <= n2) {  // y-face between cells (i,j-1) and (i,j)
+        double a = w2[IX(i, refl_cell(j - 1, n2), n2)], b = w2[IX(i, refl_cell(j, n2), n2)];
+        lamy[IX(i, j, n2 + 1)] = harmonic ? 2. / (a + b) : 1. / 2 * (a + b);
+    }
+}
+
+// Corner tensors of the rotated stencil.  Corner (ci,cj), ci in [0,n1], cj in [0,n2], sits at
+// (ci-1/2, cj-1/2); its four cells are (ci-1..ci, cj-1..cj), mirrored at the boundary.
+// KoverMu_*_ip12jp12 (src/EllipticSolver.cpp:697-754), GetTransformedMobilityTensor
+// (src/MGSolver.cpp:807-841) and M_im12j (src/EllipticSolver.cpp:554-562).
+__global__ void k_corner(int n1, int n2, const double* __restrict__ w1, const double* __restrict__ w2,
+                         int harmonic, Geo G, double* __restrict__ m11, double* __restrict__ m22,
+                         double* __restrict__ m12) {
+    int cj = blockIdx.x * BX + threadIdx.x, ci = blockIdx.y * BY + threadIdx.y;
+    if (ci > n1 || cj > n2) return;
+    const int i = ci - 1, j = cj - 1;  // reference corner (i+1/2, j+1/2)
+    const int a0 = refl_cell(i, n1), a1 = refl_cell(i + 1, n1), b0 = refl_cell(j, n2), b1 = refl_cell(j + 1, n2);
+    // order of the reference sum: (ip1j + ij) + ijp1 + ip1jp1
+    double s1 = w1[IX(a1, b0, n2)] + w1[IX(a0, b0, n2)] + w1[IX(a0, b1, n2)] + w1[IX(a1, b1, n2)];
+    double s2 = w2[IX(a1, b0, n2)] + w2[IX(a0, b0, n2)] + w2[IX(a0, b1, n2)] + w2[IX(a1, b1, n2)];
+    double K11 = harmonic ? 4. / s1 : 1. / 4 * s1;
+    double K22 = harmonic ? 4. / s2 : 1. / 4 * s2;
+    size_t k = IX(ci, cj, n2 + 1);
+    m11[k] = G.secamt2 * (K11 * G.cosa2 + K22 * G.sina2);
+    m22[k] = G.secamt2 * (K22 * G.cost2 + K11 * G.sint2);
+    m12[k] = G.secamt2 * (K22 * G.costsina - K11 * G.cosasint);
+}
+
+// ---------------------------------------------------------------- fine operators
+// nu = 1: face transmissibilities dA/dx^2 * lambda with zero flux through the boundary.
+__global__ void k_face5_fine(int n1, int n2, const double* __restrict__ lamx, const double* __restrict__ lamy,
+                             double sx, double sy, double* __restrict__ tx, double* __restrict__ ty) {
+    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    if (i <= n1 && j < n2) tx[IX(i, j, n2)] = (i == 0 || i == n1) ? 0.0 : lamx[IX(i, j, n2)] * sx;
+    if (i < n1 && j <= n2) ty[IX(i, j, n2 + 1)] = (j == 0 || j == n2) ? 0.0 : lamy[IX(i, j, n2 + 1)] * sy;
+}
+
+// Reference row (C,W,SW,S,SE,E,NE,N,NW) of GetWeightedMatrixCoefficientsForCell
+// (src/MGSolver.cpp:710-804) with the Neumann folding of :304-515.
+__device__ void ref_row(int i, int j, int n1, int n2, const double* __restrict__ lamx,
+                        const double* __restrict__ lamy, const double* __restrict__ m11,
+                        const double* __restrict__ m22, const double* __restrict__ m12, double nu, const Geo& G,
+                        double* o) {
+    const double dx = G.dx, dy = G.dy, dxi = G.dxi, deta = G.deta;
+    // parallel (five-point) part
+    double K11_im = lamx[IX(i, j, n2)], K11_ip = lamx[IX(i + 1, j, n2)];
+    double K22_jm = lamy[IX(i, j, n2 + 1)], K22_jp = lamy[IX(i, j + 1, n2 + 1)];
+    double Wp = 1. / (dx * dx) * K11_im, Ep = 1. / (dx * dx) * K11_ip;
+    double Sp = 1. / (dy * dy) * K22_jm, Np = 1. / (dy * dy) * K22_jp;
+    double Cp = -1. / (dy * dy) * (K22_jm + K22_jp) - 1. / (dx * dx) * (K11_im + K11_ip);
+    // diagonal (rotated nine-point) part; corners (i+1/2,j+1/2) -> (i+1,j+1) etc.
+    const int w = n2 + 1;
+    double M11_ip12j = m11[IX(i + 1, j + 1, w)], M11_im12j = m11[IX(i, j, w)];
+    double M22_ijp12 = m22[IX(i, j + 1, w)], M22_ijm12 = m22[IX(i + 1, j, w)];
+    double M12_ip12j = m12[IX(i + 1, j + 1, w)], M21_ijp12 = m12[IX(i, j + 1, w)];
+    double M12_im12j = m12[IX(i, j, w)], M21_ijm12 = m12[IX(i + 1, j, w)];
+    double NEd = M11_ip12j / (dxi * dxi), SWd = M11_im12j / (dxi * dxi);
+    double NWd = M22_ijp12 / (deta * deta), SEd = M22_ijm12 / (deta * deta);
+    double Cd = -1. / (dxi * dxi) * (M11_ip12j + M11_im12j) - 1. / (deta * deta) * (M22_ijp12 + M22_ijm12);
+    double Nd = 1. / (deta * dxi) * (M12_ip12j + M21_ijp12);
+    double Wd = -1. / (deta * dxi) * (M21_ijp12 + M12_im12j);
+    double Ed = -1. / (deta * dxi) * (M12_ip12j + M21_ijm12);
+    double Sd = 1. / (deta * dxi) * (M12_im12j + M21_ijm12);
+    double C = nu * Cp + (1 - nu) * Cd, W = nu * Wp + (1 - nu) * Wd, SW = nu * 0.0 + (1 - nu) * SWd;
+    double S = nu * Sp + (1 - nu) * Sd, SE = nu * 0.0 + (1 - nu) * SEd, E = nu * Ep + (1 - nu) * Ed;
+    double NE = nu * 0.0 + (1 - nu) * NEd, N = nu * Np + (1 - nu) * Nd, NW = nu * 0.0 + (1 - nu) * NWd;
+    double s[9] = {C, W, SW, S, SE, E, NE, N, NW};
+    for (int e = 0; e < 9; ++e) o[e] = s[e];
+    const int k = i, l = j;
+    auto set = [&](double a0, double a1, double a2, double a3, double a4, double a5, double a6, double a7, double a8) {
+        o[0] = a0; o[1] = a1; o[2] = a2; o[3] = a3; o[4] = a4; o[5] = a5; o[6] = a6; o[7] = a7; o[8] = a8;
+    };
+    if (l == 0) set(C + S, W + SW, 0, 0, 0, E + SE, NE, N, NW);
+    if (l == n2 - 1) set(C + N, W + NW, SW, S, SE, E + NE, 0, 0, 0);
+    if (k == 0) set(C + W, 0, 0, S + SW, SE, E, NE, N + NW, 0);
+    if (k == n1 - 1) set(C + E, W, SW, S + SE, 0, 0, 0, N + NE, NW);
+    if (k == 0 && l == 0) set(C + W + S + SW, 0, 0, 0, 0, E + SE, NE, N + NW, 0);
+    if (k == 0 && l == n2 - 1) set(C + W + N + NW, 0, 0, S + SW, SE, E + NE, 0, 0, 0);
+    if (k == n1 - 1 && l == n2 - 1) set(C + N + NE + E, W + NW, SW, S + SE, 0, 0, 0, 0, 0);
+    if (k == n1 - 1 && l == 0) set(C + S + E + SE, W + SW, 0, 0, 0, 0, 0, N + NE, NW);
+}
+
+__global__ void k_exp9_fine(int n1, int n2, const double* __restrict__ lamx, const double* __restrict__ lamy,
+                            const double* __restrict__ m11, const double* __restrict__ m22,
+                            const double* __restrict__ m12, double nu, Geo G, double* __restrict__ a9) {
+    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    if (i >= n1 || j >= n2) return;
+    double o[9];
+    ref_row(i, j, n1, n2, lamx, lamy, m11, m22, m12, nu, G, o);
+    const size_t n = (size_t)n1 * n2, k = IX(i, j, n2);
+    for (int e = 0; e < 9; ++e) a9[e * n + k] = -G.dA * o[e];
+}
+
+// Stencil offsets in HYPRE entry order (src/MGSolver.cpp:164-166).
+__constant__ int c_off[9][2] = {{0, 0}, {-1, 0}, {-1, -1}, {0, -1}, {1, -1}, {1, 0}, {1, 1}, {0, 1}, {-1, 1}};
+
+// ---------------------------------------------------------------- coarse operators
+__global__ void k_face5_coarsen(int n1f, int n2f, const double* __restrict__ txf, const double* __restrict__ tyf,
+                                int n1c, int n2c, double* __restrict__ txc, double* __restrict__ tyc) {
+    int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
+    if (I <= n1c && J < n2c) {
+        int fi = 2 * I;
+        double s = 0.0;
+        if (fi <= n1f) {
+            s = txf[IX(fi, 2 * J, n2f)];
+            if (2 * J + 1 < n2f) s += txf[IX(fi, 2 * J + 1, n2f)];
+        }
+        txc[IX(I, J, n2c)] = 0.5 * s;
+    }
+    if (I < n1c && J <= n2c) {
+        int fj = 2 * J;
+        double s = 0.0;
+        if (fj <= n2f) {
+            s = tyf[IX(2 * I, fj, n2f + 1)];
+            if (2 * I + 1 < n1f) s += tyf[IX(2 * I + 1, fj, n2f + 1)];
+        }
+        tyc[IX(I, J, n2c + 1)] = 0.5 * s;
+    }
+}
+
+__global__ void k_exp9_coarsen(int n1f, int n2f, const double* __restrict__ af, int n1c, int n2c,
+                               double* __restrict__ ac) {
+    int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
+    if (I >= n1c || J >= n2c) return;
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const size_t nf = (size_t)n1f * n2f;
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) {
+            int i = 2 * I + a, j = 2 * J + b;
+            if (i >= n1f || j >= n2f) continue;
+            for (int e = 0; e < 9; ++e) {
+                int ii = i + c_off[e][0], jj = j + c_off[e][1];
+                if (ii < 0 || ii >= n1f || jj < 0 || jj >= n2f) continue;
+                double val = af[e * nf + IX(i, j, n2f)];
+                int dI = (ii >> 1) - I, dJ = (jj >> 1) - J;
+                int ec = 0;
+                for (int q = 0; q < 9; ++q)
+                    if (c_off[q][0] == dI && c_off[q][1] == dJ) ec = q;
+                acc[ec] += val;
+            }
+        }
+    const size_t nc = (size_t)n1c * n2c;
+    for (int e = 0; e < 9; ++e) ac[e * nc + IX(I, J, n2c)] = 0.5 * acc[e];
+}
+
+__global__ void k_idiag(int n1, int n2, int kind, const double* __restrict__ tx, const double* __restrict__ ty,
+                        const double* __restrict__ a9, double* __restrict__ idiag) {
+    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    if (i >= n1 || j >= n2) return;
+    double d;
+    if (kind == FACE5)
+        d = tx[IX(i, j, n2)] + tx[IX(i + 1, j, n2)] + ty[IX(i, j, n2 + 1)] + ty[IX(i, j + 1, n2 + 1)];
+    else
+        d = a9[IX(i, j, n2)];
+    idiag[IX(i, j, n2)] = d != 0.0 ? 1.0 / d : 0.0;
+}
+
+__global__ void k_to_float(size_t n, const double* __restrict__ a, float* __restrict__ b) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        b[k] = (float)a[k];
+}
+
+// ---------------------------------------------------------------- operator application
+template <class T>
+__device__ __forceinline__ T apply_face5(int i, int j, int n1, int n2, const T* __restrict__ tx,
+                                         const T* __restrict__ ty, const T* __restrict__ x, T& diag, T& offsum) {
+    T tw = tx[IX(i, j, n2)], te = tx[IX(i + 1, j, n2)], ts = ty[IX(i, j, n2 + 1)], tn = ty[IX(i, j + 1, n2 + 1)];
+    T s = 0;
+    if (i > 0) s += tw * x[IX(i - 1, j, n2)];
+    if (i < n1 - 1) s += te * x[IX(i + 1, j, n2)];
+    if (j > 0) s += ts * x[IX(i, j - 1, n2)];
+    if (j < n2 - 1) s += tn * x[IX(i, j + 1, n2)];
+    diag = tw + te + ts + tn;
+    offsum = s;
+    return diag * x[IX(i, j, n2)] - s;
+}
+
+template <class T>
+__device__ __forceinline__ T offsum_exp9(int i, int j, int n1, int n2, const T* __restrict__ a9,
+                                         const T* __restrict__ x) {
+    const size_t n = (size_t)n1 * n2, k = IX(i, j, n2);
+    T s = 0;
+#pragma unroll
+    for (int e = 1; e < 9; ++e) {
+        int ii = i + c_off[e][0], jj = j + c_off[e][1];
+        if (ii < 0 || ii >= n1 || jj < 0 || jj >= n2) continue;
+        s += a9[e * n + k] * x[IX(ii, jj, n2)];
+    }
+    return s;
+}
+
+// ---------------------------------------------------------------- smoothers
+template <class T>
+__global__ void k_rb_face5(int n1, int n2, const T* __restrict__ tx, const T* __restrict__ ty,
+                           const T* __restrict__ idiag, const T* __restrict__ b, T* __restrict__ x, int color) {
+    int jj = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    int j = 2 * jj + ((i + color) & 1);
+    if (i >= n1 || j >= n2) return;
+    T s = b[IX(i, j, n2)];
+    if (i > 0) s += tx[IX(i, j, n2)] * x[IX(i - 1, j, n2)];
+    if (i < n1 - 1) s += tx[IX(i + 1, j, n2)] * x[IX(i + 1, j, n2)];
+    if (j > 0) s += ty[IX(i, j, n2 + 1)] * x[IX(i, j - 1, n2)];
+    if (j < n2 - 1) s += ty[IX(i, j + 1, n2 + 1)] * x[IX(i, j + 1, n2)];
+    x[IX(i, j, n2)] = s * idiag[IX(i, j, n2)];
+}
+
+template <class T>
+__global__ void k_gs4_exp9(int n1, int n2, const T* __restrict__ a9, const T* __restrict__ idiag,
+                           const T* __restrict__ b, T* __restrict__ x, int ci, int cj) {
+    int j = 2 * (blockIdx.x * BX + threadIdx.x) + cj, i = 2 * (blockIdx.y * BY + threadIdx.y) + ci;
+    if (i >= n1 || j >= n2) return;
+    T s = b[IX(i, j, n2)] - offsum_exp9<T>(i, j, n1, n2, a9, x);
+    x[IX(i, j, n2)] = s * idiag[IX(i, j, n2)];
+}
+
+// ---------------------------------------------------------------- transfers
+template <class T>
+__device__ __forceinline__ T resid(const Level& Lv, int i, int j, const T* tx, const T* ty, const T* a9,
+                                   const T* b, const T* x) {
+    if (Lv.kind == FACE5) {
+        T d, o;
+        return b[IX(i, j, Lv.n2)] - apply_face5<T>(i, j, Lv.n1, Lv.n2, tx, ty, x, d, o);
+    }
+    return b[IX(i, j, Lv.n2)] - (a9[IX(i, j, Lv.n2)] * x[IX(i, j, Lv.n2)] + offsum_exp9<T>(i, j, Lv.n1, Lv.n2, a9, x));
+}
+
+// Residual of the fine level summed over each 2x2 aggregate -> coarse rhs; coarse x := 0.
+template <class T>
+__global__ void k_restrict(Level F, const T* __restrict__ tx, const T* __restrict__ ty, const T* __restrict__ a9,
+                           const T* __restrict__ b, const T* __restrict__ x, int n1c, int n2c, T* __restrict__ bc,
+                           T* __restrict__ xc) {
+    int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
+    if (I >= n1c || J >= n2c) return;
+    T s = 0;
+    for (int a = 0; a < 2; ++a)
+        for (int bb = 0; bb < 2; ++bb) {
+            int i = 2 * I + a, j = 2 * J + bb;
+            if (i < F.n1 && j < F.n2) s += resid<T>(F, i, j, tx, ty, a9, b, x);
+        }
+    bc[IX(I, J, n2c)] = s;
+    xc[IX(I, J, n2c)] = 0;
+}
+
+// Bilinear cell-centred prolongation (weights 9/16, 3/16, 3/16, 1/16; the outside
+// neighbour is replaced by the cell itself), added to the fine iterate.
+template <class T>
+__global__ void k_prolong(int n1, int n2, T* __restrict__ x, int n1c, int n2c, const T* __restrict__ xc) {
+    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    if (i >= n1 || j >= n2) return;
+    int I = i >> 1, J = j >> 1;
+    int I2 = (i & 1) ? I + 1 : I - 1, J2 = (j & 1) ? J + 1 : J - 1;
+    if (I2 < 0 || I2 >= n1c) I2 = I;
+    if (J2 < 0 || J2 >= n2c) J2 = J;
+    T e = T(0.5625) * xc[IX(I, J, n2c)] + T(0.1875) * xc[IX(I2, J, n2c)] + T(0.1875) * xc[IX(I, J2, n2c)] +
+          T(0.0625) * xc[IX(I2, J2, n2c)];
+    x[IX(i, j, n2)] += e;
+}
+
+// ---------------------------------------------------------------- coarsest level (dense)
+__global__ void k_dense_build(Level C, const double* __restrict__ tx, const double* __restrict__ ty,
+                              const double* __restrict__ a9, int singular, double* __restrict__ D) {
+    const int n1 = C.n1, n2 = C.n2, n = n1 * n2;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        for (int cc = 0; cc < n; ++cc) D[(size_t)r * n + cc] = 0.0;
+        int i = r / n2, j = r % n2;
+        if (C.kind == FACE5) {
+            double tw = tx[IX(i, j, n2)], te = tx[IX(i + 1, j, n2)], ts = ty[IX(i, j, n2 + 1)], tn = ty[IX(i, j + 1, n2 + 1)];
+            D[(size_t)r * n + r] = tw + te + ts + tn;
+            if (i > 0) D[(size_t)r * n + IX(i - 1, j, n2)] = -tw;
+            if (i < n1 - 1) D[(size_t)r * n + IX(i + 1, j, n2)] = -te;
+            if (j > 0) D[(size_t)r * n + IX(i, j - 1, n2)] = -ts;
+            if (j < n2 - 1) D[(size_t)r * n + IX(i, j + 1, n2)] = -tn;
+        } else {
+            for (int e = 0; e < 9; ++e) {
+                int ii = i + c_off[e][0], jj = j + c_off[e][1];
+                if (ii < 0 || ii >= n1 || jj < 0 || jj >= n2) continue;
+                D[(size_t)r * n + IX(ii, jj, n2)] = a9[(size_t)e * n + r];
+            }
+        }
+    }
+    __syncthreads();
+    if (singular && threadIdx.x == 0) {  // fix the constant mode: row 0 := e_0
+        for (int cc = 0; cc < n; ++cc) D[cc] = 0.0;
+        D[0] = 1.0;
+    }
+}
+
+// Gauss-Jordan inversion of an n x n (n <= 64) diagonally dominant matrix in shared memory.
+__global__ void k_dense_invert(int n, const double* __restrict__ D, double* __restrict__ Dinv) {
+    extern __shared__ double sm[];
+    double* A = sm;          // n x n
+    double* B = sm + n * n;  // n x n
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+        A[k] = D[k];
+        B[k] = (k / n == k % n) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    for (int piv = 0; piv < n; ++piv) {
+        double inv = 1.0 / A[piv * n + piv];
+        __syncthreads();
+        for (int cc = threadIdx.x; cc < n; cc += blockDim.x) {
+            A[piv * n + cc] *= inv;
+            B[piv * n + cc] *= inv;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+            int r = k / n, cc = k % n;
+            if (r == piv) continue;
+            double f = A[r * n + piv];
+            if (cc != piv) A[r * n + cc] -= f * A[piv * n + cc];
+            B[r * n + cc] -= f * B[piv * n + cc];
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < n; r += blockDim.x)
+            if (r != piv) A[r * n + piv] = 0.0;
+        __syncthreads();
+    }
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) Dinv[k] = B[k];
+}
+
+// x = Dinv * b (FP64 arithmetic), b(0) := 0 and mean removal for the singular system.
+template <class T>
+__global__ void k_dense_solve(int n, const double* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x,
+                              int singular) {
+    __shared__ double sb[64];
+    __shared__ double sx[64];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) sb[k] = (singular && k == 0) ? 0.0 : (double)b[k];
+    __syncthreads();
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        double s = 0;
+        for (int cc = 0; cc < n; ++cc) s += Dinv[(size_t)r * n + cc] * sb[cc];
+        sx[r] = s;
+    }
+    __syncthreads();
+    if (singular) {
+        __shared__ double mean;
+        if (threadIdx.x == 0) {
+            double m = 0;
+            for (int k = 0; k < n; ++k) m += sx[k];
+            mean = m / n;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = (T)(sx[k] - mean);
+    } else {
+        for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = (T)sx[k];
+    }
+}
+
+// ---------------------------------------------------------------- fine residual, norms, rhs
+// r = f - A x on the fine level (FP64); accumulates ||r||^2 over all cells except the pinned
+// one; optionally stores r as FP32 for the mixed-precision correction cycle.
+__global__ void __launch_bounds__(RED_THREADS) k_fine_resid(Level F, const double* __restrict__ f,
+                                                            const double* __restrict__ x, int pin,
+                                                            float* __restrict__ r32, double* partials, int mb,
+                                                            unsigned* counter, double* out) {
+    double acc[1] = {0.0};
+    const size_t n = F.n();
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        int i = (int)(k / F.n2), j = (int)(k % F.n2);
+        double r = resid<double>(F, i, j, F.tx, F.ty, F.a9, f, x);
+        if (r32) r32[k] = (float)r;  // consistent rhs of the singular correction equation
+        if ((int)k == pin) r = 0.0;  // the pinned row of the reference system has zero residual
+        acc[0] += r * r;
+    }
+    grid_reduce<1>(acc, 0u, partials, mb, counter, out);
+}
+
+// f = dA*q with sum and sum of squares.
+__global__ void __launch_bounds__(RED_THREADS) k_rhs(size_t n, const double* __restrict__ q, double dA,
+                                                     double* __restrict__ f, double* partials, int mb,
+                                                     unsigned* counter, double* out) {
+    double acc[2] = {0.0, 0.0};
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        double v = dA * q[k];
+        f[k] = v;
+        acc[0] += v;
+        acc[1] += v * v;
+    }
+    grid_reduce<2>(acc, 0u, partials, mb, counter, out);
+}
+
+// Consistent right-hand side and pinned value: f(pin) := -(sum f - f(pin));
+// p_pin = -q_pin dA / kappa  (pinned row kappa/dA p = -q, src/MGSolver.cpp:553-565).
+__global__ void k_fix_pin(double* f, const double* q, int pin, double dA, double kappa, DevScalars* S) {
+    double fp = f[pin];
+    S->pin_value = -q[pin] * dA / kappa;
+    f[pin] = -(S->fsum - fp);
+}
+
+__global__ void k_add_f32(size_t n, double* __restrict__ x, const float* __restrict__ e) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        x[k] += (double)e[k];
+}
+
+__global__ void k_shift(size_t n, double* __restrict__ x, int pin, const DevScalars* S) {
+    double s = S->pin_value - x[pin];
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        x[k] += s;
+}
+
+// y = A_ref x (reference pinned matrix) from the device operator.
+__global__ void k_apply_ref(Level F, const double* __restrict__ x, int pin, double dA, double kappa,
+                            double* __restrict__ y) {
+    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    if (i >= F.n1 || j >= F.n2) return;
+    size_t k = IX(i, j, F.n2);
+    if ((int)k == pin) { y[k] = kappa / dA * x[k]; return; }
+    double v;
+    if (F.kind == FACE5) {
+        double d, o;
+        v = apply_face5<double>(i, j, F.n1, F.n2, F.tx, F.ty, x, d, o);
+    } else {
+        v = F.a9[k] * x[k] + offsum_exp9<double>(i, j, F.n1, F.n2, F.a9, x);
+    }
+    y[k] = -v / dA;
+}
+
+// ---------------------------------------------------------------- host orchestration
+static int red_blocks(impec_ctx* ctx) { return ctx->num_sms * 2 < ctx->max_blocks ? ctx->num_sms * 2 : ctx->max_blocks; }
+
+impec_status pressure_alloc(impec_ctx* ctx) {
+    const impec_params& P = ctx->P;
+    int n1 = P.N1, n2 = P.N2;
+    const bool nine = P.nu < 1.0;
+    const size_t nc = (size_t)(n1 + 1) * (n2 + 1);
+    if (nine) {
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->cm11, nc * 8));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->cm22, nc * 8));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->cm12, nc * 8));
+    }
+    ctx->L.clear();
+    for (int l = 0;; ++l) {
+        Level Lv;
+        Lv.n1 = n1;
+        Lv.n2 = n2;
+        Lv.kind = nine ? EXP9 : FACE5;
+        const size_t n = Lv.n();
+        if (Lv.kind == FACE5) {
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.tx, (size_t)(n1 + 1) * n2 * 8));
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.ty, (size_t)n1 * (n2 + 1) * 8));
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.tx32, (size_t)(n1 + 1) * n2 * 4));
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.ty32, (size_t)n1 * (n2 + 1) * 4));
+        } else {
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.a9, n * 9 * 8));
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.a932, n * 9 * 4));
+        }
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.idiag, n * 8));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.idiag32, n * 4));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.x, n * 8));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.b, n * 8));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.x32, n * 4));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.b32, n * 4));
+        ctx->L.push_back(Lv);
+        if (n1 <= 8 && n2 <= 8) break;
+        n1 = (n1 + 1) / 2;
+        n2 = (n2 + 1) / 2;
+    }
+    ctx->dense_n = ctx->L.back().n1 * ctx->L.back().n2;
+    IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dense_inv, (size_t)ctx->dense_n * ctx->dense_n * 8 * 2));
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_dense_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 64 * 8));
+    return IMPEC_OK;
+}
+
+void pressure_free(impec_ctx* ctx) {
+    for (Level& Lv : ctx->L) {
+        void* ps[] = {Lv.tx, Lv.ty, Lv.a9, Lv.idiag, Lv.x, Lv.b, Lv.tx32, Lv.ty32, Lv.a932, Lv.idiag32, Lv.x32, Lv.b32};
+        for (void* p : ps)
+            if (p) cudaFree(p);
+    }
+    ctx->L.clear();
+    void* ps[] = {ctx->cm11, ctx->cm22, ctx->cm12, ctx->dense_inv};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+}
+
+impec_status face_mobility(impec_ctx* ctx, const double* c) {
+    const impec_params& P = ctx->P;
+    const int n1 = P.N1, n2 = P.N2;
+    const int harm = P.avgproc == IMPEC_HARMONIC;
+    double* w2 = ctx->K22 ? ctx->muK22 : nullptr;
+    k_cell_w<<<grid2(n1, n2), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, c, ctx->K11, ctx->K22, ctx->G.mob1over4,
+                                                               P.mu_res, harm, ctx->muK11, w2);
+    IMPEC_LAUNCH_CHECK();
+    const double* W2 = w2 ? w2 : ctx->muK11;
+    k_face_lam<<<grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, ctx->muK11, W2, harm, ctx->lamx,
+                                                                          ctx->lamy);
+    IMPEC_LAUNCH_CHECK();
+    if (P.nu < 1.0) {
+        k_corner<<<grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, ctx->muK11, W2, harm, ctx->G,
+                                                                            ctx->cm11, ctx->cm22, ctx->cm12);
+        IMPEC_LAUNCH_CHECK();
+    }
+    return IMPEC_OK;
+}
+
+impec_status pressure_setup(impec_ctx* ctx, const double* c) {
+    const impec_params& P = ctx->P;
+    IMPEC_TRY(face_mobility(ctx, c));
+    Level& F = ctx->L[0];
+    const Geo& G = ctx->G;
+    if (F.kind == FACE5) {
+        double sx = G.dA * (1. / (G.dx * G.dx)), sy = G.dA * (1. / (G.dy * G.dy));
+        k_face5_fine<<<grid2(F.n1 + 1, F.n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, ctx->lamx, ctx->lamy,
+                                                                                  sx, sy, F.tx, F.ty);
+    } else {
+        k_exp9_fine<<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, ctx->lamx, ctx->lamy, ctx->cm11,
+                                                                         ctx->cm22, ctx->cm12, P.nu, G, F.a9);
+    }
+    IMPEC_LAUNCH_CHECK();
+    for (size_t l = 0; l + 1 < ctx->L.size(); ++l) {
+        Level &A = ctx->L[l], &B = ctx->L[l + 1];
+        if (A.kind == FACE5)
+            k_face5_coarsen<<<grid2(B.n1 + 1, B.n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(A.n1, A.n2, A.tx, A.ty, B.n1,
+                                                                                        B.n2, B.tx, B.ty);
+        else
+            k_exp9_coarsen<<<grid2(B.n1, B.n2), dim3(BX, BY), 0, ctx->stream>>>(A.n1, A.n2, A.a9, B.n1, B.n2, B.a9);
+        IMPEC_LAUNCH_CHECK();
+    }
+    const bool mixed = P.precision == IMPEC_PREC_MIXED;
+    for (Level& Lv : ctx->L) {
+        k_idiag<<<grid2(Lv.n1, Lv.n2), dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, Lv.kind, Lv.tx, Lv.ty, Lv.a9,
+                                                                        Lv.idiag);
+        IMPEC_LAUNCH_CHECK();
+        if (mixed) {
+            const size_t n = Lv.n();
+            int nb = ctx->num_sms * 4;
+            k_to_float<<<nb, 256, 0, ctx->stream>>>(n, Lv.idiag, Lv.idiag32);
+            if (Lv.kind == FACE5) {
+                k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)(Lv.n1 + 1) * Lv.n2, Lv.tx, Lv.tx32);
+                k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)Lv.n1 * (Lv.n2 + 1), Lv.ty, Lv.ty32);
+            } else {
+                k_to_float<<<nb, 256, 0, ctx->stream>>>(n * 9, Lv.a9, Lv.a932);
+            }
+            IMPEC_LAUNCH_CHECK();
+        }
+    }
+    Level& C = ctx->L.back();
+    k_dense_build<<<1, 256, 0, ctx->stream>>>(C, C.tx, C.ty, C.a9, 1, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n);
+    IMPEC_LAUNCH_CHECK();
+    k_dense_invert<<<1, 256, 2 * ctx->dense_n * ctx->dense_n * 8, ctx->stream>>>(
+        ctx->dense_n, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n, ctx->dense_inv);
+    IMPEC_LAUNCH_CHECK();
+    return IMPEC_OK;
+}
+
+template <class T>
+static void level_ptrs(Level& Lv, const T*& tx, const T*& ty, const T*& a9, const T*& id, T*& x, T*& b);
+template <>
+void level_ptrs<double>(Level& Lv, const double*& tx, const double*& ty, const double*& a9, const double*& id,
+                        double*& x, double*& b) {
+    tx = Lv.tx; ty = Lv.ty; a9 = Lv.a9; id = Lv.idiag; x = Lv.x; b = Lv.b;
+}
+template <>
+void level_ptrs<float>(Level& Lv, const float*& tx, const float*& ty, const float*& a9, const float*& id,
+                       float*& x, float*& b) {
+    tx = Lv.tx32; ty = Lv.ty32; a9 = Lv.a932; id = Lv.idiag32; x = Lv.x32; b = Lv.b32;
+}
+
+template <class T>
+static void smooth(impec_ctx* ctx, Level& Lv, int sweeps, bool reverse) {
+    const T *tx, *ty, *a9, *id;
+    T *x, *b;
+    level_ptrs<T>(Lv, tx, ty, a9, id, x, b);
+    for (int s = 0; s < sweeps; ++s) {
+        if (Lv.kind == FACE5) {
+            dim3 g((Lv.n2 / 2 + 1 + BX - 1) / BX, (Lv.n1 + BY - 1) / BY);
+            for (int cc = 0; cc < 2; ++cc)
+                k_rb_face5<T><<<g, dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, tx, ty, id, b, x, reverse ? 1 - cc : cc);
+        } else {
+            dim3 g(((Lv.n2 + 1) / 2 + BX - 1) / BX, ((Lv.n1 + 1) / 2 + BY - 1) / BY);
+            for (int cc = 0; cc < 4; ++cc) {
+                int col = reverse ? 3 - cc : cc;
+                k_gs4_exp9<T><<<g, dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, a9, id, b, x, col >> 1, col & 1);
+            }
+        }
+    }
+}
+
+template <class T>
+static void vcycle(impec_ctx* ctx, size_t l) {
+    Level& F = ctx->L[l];
+    const T *tx, *ty, *a9, *id;
+    T *x, *b;
+    level_ptrs<T>(F, tx, ty, a9, id, x, b);
+    if (l + 1 == ctx->L.size()) {
+        k_dense_solve<T><<<1, 64, 0, ctx->stream>>>(ctx->dense_n, ctx->dense_inv, b, x, 1);
+        return;
+    }
+    smooth<T>(ctx, F, 2, false);
+    Level& C = ctx->L[l + 1];
+    const T *ctx_, *cty, *ca9, *cid;
+    T *cx, *cb;
+    level_ptrs<T>(C, ctx_, cty, ca9, cid, cx, cb);
+    k_restrict<T><<<grid2(C.n1, C.n2), dim3(BX, BY), 0, ctx->stream>>>(F, tx, ty, a9, b, x, C.n1, C.n2, cb, cx);
+    vcycle<T>(ctx, l + 1);
+    k_prolong<T><<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, x, C.n1, C.n2, cx);
+    smooth<T>(ctx, F, 2, true);
+}
+
+impec_status pressure_solve(impec_ctx* ctx, const double* c, double* p, double tol, int* cycles, double* relres) {
+    const impec_params& P = ctx->P;
+    IMPEC_TRY(pressure_setup(ctx, c));
+    Level& F = ctx->L[0];
+    const size_t n = F.n();
+    const int pin = (int)IX(ctx->pin_i, ctx->pin_j, F.n2);
+    const int rb = red_blocks(ctx);
+    DevScalars* S = ctx->dscal;
+    k_rhs<<<rb, RED_THREADS, 0, ctx->stream>>>(n, ctx->q, ctx->G.dA, ctx->f, ctx->partials, ctx->max_blocks,
+                                                ctx->counter, &S->fsum);
+    k_fix_pin<<<1, 1, 0, ctx->stream>>>(ctx->f, ctx->q, pin, ctx->G.dA, ctx->pin_kappa, S);
+    IMPEC_LAUNCH_CHECK();
+    double* x = F.x;
+    if (P.warm_start)
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(x, p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    else
+        IMPEC_CUDA_TRY(cudaMemsetAsync(x, 0, n * 8, ctx->stream));
+    const bool mixed = P.precision == IMPEC_PREC_MIXED;
+    // F.b aliases the consistent rhs for the FP64 cycle
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(F.b, ctx->f, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    int k = 0;
+    double rr = 0;
+    impec_status st = IMPEC_OK;
+    for (;;) {
+        k_fine_resid<<<rb, RED_THREADS, 0, ctx->stream>>>(F, ctx->f, x, pin, mixed ? F.b32 : nullptr, ctx->partials,
+                                                           ctx->max_blocks, ctx->counter, &S->rnorm2);
+        IMPEC_LAUNCH_CHECK();
+        IMPEC_TRY(sync_scalars(ctx));
+        double fn = ctx->hscal->fnorm2;
+        rr = fn > 0 ? sqrt(ctx->hscal->rnorm2 / fn) : sqrt(ctx->hscal->rnorm2);
+        if (!std::isfinite(rr)) { st = IMPEC_ERR_NAN; break; }
+        if (rr <= tol) break;
+        if (k >= P.max_cycles) { st = IMPEC_ERR_NOT_CONVERGED; break; }
+        if (mixed) {
+            IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
+            vcycle<float>(ctx, 0);
+            k_add_f32<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, x, F.x32);
+        } else {
+            vcycle<double>(ctx, 0);
+        }
+        IMPEC_LAUNCH_CHECK();
+        ++k;
+    }
+    k_shift<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, x, pin, S);
+    IMPEC_LAUNCH_CHECK();
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(p, x, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (cycles) *cycles = k;
+    if (relres) *relres = rr;
+    ctx->last_its = k;
+    ctx->last_relres = rr;
+    return st;
+}
+
+impec_status pressure_apply_ref(impec_ctx* ctx, const double* x, double* y) {
+    Level& F = ctx->L[0];
+    const int pin = (int)IX(ctx->pin_i, ctx->pin_j, F.n2);
+    k_apply_ref<<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F, x, pin, ctx->G.dA, ctx->pin_kappa, y);
+    IMPEC_LAUNCH_CHECK();
+    return IMPEC_OK;
+}
+
+// ---------------------------------------------------------------- Darcy velocities
+// CalcVelocities (src/EllipticSolver.cpp:541-683): u = nu * parallel + (1-nu) * diagonal.
+struct VelArgs {
+    int n1, n2;
+    double nu, inv_dx, inv_dy, inv_dxi, inv_deta, cost, sina, sint, cosa;
+};
+
+// (xi,eta) Darcy velocity at corner (ci,cj) = reference corner (ci-1/2, cj-1/2), rotated back
+// to (x,y): GetDiagonalW_im12j + XYFromXiEta.
+__device__ __forceinline__ void corner_vel(const VelArgs& A, const double* __restrict__ p,
+                                           const double* __restrict__ m11, const double* __restrict__ m22,
+                                           const double* __restrict__ m12, int ci, int cj, double& u1, double& u2) {
+    const int n1 = A.n1, n2 = A.n2;
+    int i0 = refl_cell(ci - 1, n1), i1 = refl_cell(ci, n1), j0 = refl_cell(cj - 1, n2), j1 = refl_cell(cj, n2);
+    double d1dp = A.inv_dxi * (p[IX(i1, j1, n2)] - p[IX(i0, j0, n2)]);
+    double d2dp = A.inv_deta * (p[IX(i0, j1, n2)] - p[IX(i1, j0, n2)]);
+    size_t k = IX(ci, cj, n2 + 1);
+    double M11 = m11[k], M12 = m12[k], M22 = m22[k];
+    double w1 = -d1dp * M11 - d2dp * M12;
+    double w2 = -d1dp * M12 - d2dp * M22;
+    u1 = A.cost * w1 - A.sina * w2;
+    u2 = A.sint * w1 + A.cosa * w2;
+}
+
+__global__ void k_velocity(VelArgs A, const double* __restrict__ p, const double* __restrict__ lamx,
+                           const double* __restrict__ lamy, const double* __restrict__ m11,
+                           const double* __restrict__ m22, const double* __restrict__ m12, double* __restrict__ u,
+                           double* __restrict__ v) {
+    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    const int n1 = A.n1, n2 = A.n2;
+    const bool diag = A.nu < 1.0;
+    if (i <= n1 && j < n2) {
+        double dp = p[IX(refl_cell(i, n1), j, n2)] - p[IX(refl_cell(i - 1, n1), j, n2)];
+        double par = (-lamx[IX(i, j, n2)] * dp) * A.inv_dx;
+        double val = par;
+        if (diag) {
+            double a1, a2, b1, b2;
+            corner_vel(A, p, m11, m22, m12, i, j, a1, a2);
+            corner_vel(A, p, m11, m22, m12, i, j + 1, b1, b2);
+            val = A.nu * par + (1. - A.nu) * (0.5 * (b1 + a1));
+        }
+        u[IX(i, j, n2)] = val;
+    }
+    if (i < n1 && j <= n2) {
+        double dp = p[IX(i, refl_cell(j, n2), n2)] - p[IX(i, refl_cell(j - 1, n2), n2)];
+        double par = (-lamy[IX(i, j, n2 + 1)] * dp) * A.inv_dy;
+        double val = par;
+        if (diag) {
+            double a1, a2, b1, b2;
+            corner_vel(A, p, m11, m22, m12, i, j, a1, a2);
+            corner_vel(A, p, m11, m22, m12, i + 1, j, b1, b2);
+            val = A.nu * par + (1. - A.nu) * (0.5 * (a2 + b2));
+        }
+        v[IX(i, j, n2 + 1)] = val;
+    }
+}
+
+impec_status velocity(impec_ctx* ctx, const double* p, const double* c, double* u, double* v) {
+    (void)c;  // mobilities were computed from c by the preceding pressure setup
+    const impec_params& P = ctx->P;
+    const Geo& G = ctx->G;
+    VelArgs A{P.N1, P.N2, P.nu, 1.0 / G.dx, 1.0 / G.dy, 1.0 / G.dxi, 1.0 / G.deta, G.cost, G.sina, G.sint, G.cosa};
+    k_velocity<<<grid2(P.N1 + 1, P.N2 + 1), dim3(BX, BY), 0, ctx->stream>>>(A, p, ctx->lamx, ctx->lamy, ctx->cm11,
+                                                                            ctx->cm22, ctx->cm12, u, v);
+    IMPEC_LAUNCH_CHECK();
+    return IMPEC_OK;
+}
+
+// MaxStableTimestepCombined (src/HyperbolicSolver.cpp:123-198); dt written to S->dt.
+__global__ void __launch_bounds__(RED_THREADS) k_maxvel(int n1, int n2, const double* __restrict__ u,
+                                                        const double* __restrict__ v, int diffusion, double al,
+                                                        double at, double dx, double* partials, int mb,
+                                                        unsigned* counter, double* out) {
+    double acc[2] = {0.0, -1.0e10};  // max velocity, max of -dt_diff
+    const size_t n = (size_t)n1 * n2;
+    const double tiny = 2.2250738585072014e-308;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        int i = (int)(k / n2), j = (int)(k % n2);
+        double uij = 0.5 * (u[IX(i, j, n2)] + u[IX(i + 1, j, n2)]);
+        double vij = 0.5 * (v[IX(i, j, n2 + 1)] + v[IX(i, j + 1, n2 + 1)]);
+        double uc = fabs(uij), vc = fabs(vij);
+        if (uc < tiny) uc = tiny;
+        if (vc < tiny) vc = tiny;
+        acc[0] = fmax(acc[0], fmax(uc, vc));
+        if (diffusion) {
+            double vij2 = vij * vij, uij2 = uij * uij;
+            double absu = sqrt(vij2 + uij2);
+            double d11 = dx / absu * (al * uij2 + at * vij2);
+            double d22 = dx / absu * (al * vij2 + at * uij2);
+            double dt = 1. / 2 * dx * dx / (d11 + d22);
+            acc[1] = fmax(acc[1], -dt);
+        }
+    }
+    grid_reduce<2>(acc, 3u, partials, mb, counter, out);
+}
+
+__global__ void k_finish_dt(DevScalars* S, double dx, double dy, double cfl, int use_diff, double limit) {
+    double mv = S->red[0];
+    S->maxvel = mv;
+    double dt = fmin(dx / mv, dy / mv) * cfl;
+    if (use_diff) {
+        double dd = fmin(-S->red[1], 1.e10) * limit;
+        dt = fmin(dd, dt);
+    }
+    S->dt = dt;
+}
+
+impec_status max_stable_dt_dev(impec_ctx* ctx, const double* u, const double* v) {
+    const impec_params& P = ctx->P;
+    const Geo& G = ctx->G;
+    const int rb = red_blocks(ctx);
+    k_maxvel<<<rb, RED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, u, v, P.diffusion, P.alpha_l, P.alpha_t, G.dx,
+                                                   ctx->partials, ctx->max_blocks, ctx->counter, ctx->dscal->red);
+    double cfl = P.cfl_porosity ? P.cfl * P.porosity : P.cfl;
+    const int use_diff = P.diffusion && P.ptype != IMPEC_CRANKNICOLSON;
+    k_finish_dt<<<1, 1, 0, ctx->stream>>>(ctx->dscal, G.dx, G.dy, cfl, use_diff, P.dt_diff_limit);
+    IMPEC_LAUNCH_CHECK();
+    return IMPEC_OK;
+}
+
+}  // namespace impec

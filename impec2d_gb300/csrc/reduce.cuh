@@ -1,0 +1,78 @@
+// Deterministic block reductions: every block writes its partial, the last block to
+// finish (ticket counter) folds the partials in a fixed order.  Reruns are bit-identical
+// because the grid size and the per-thread assignment are fixed.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace impec {
+
+constexpr int RED_THREADS = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Reduce K values across the block; result valid in thread 0.  maxmask bit k selects max.
+template <int K>
+__device__ __forceinline__ void block_reduce(double (&v)[K], unsigned maxmask) {
+    __shared__ double sh[K][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = ((maxmask >> k) & 1) ? warp_max(v[k]) : warp_sum(v[k]);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) sh[k][wid] = v[k];
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const bool mx = (maxmask >> k) & 1;
+            double t = lane < nw ? sh[k][lane] : (mx ? -INFINITY : 0.0);
+            v[k] = mx ? warp_max(t) : warp_sum(t);
+        }
+    }
+}
+
+// Grid-level reduction with last-block finalisation.  Requires blockDim.x == RED_THREADS,
+// 1-D grid with gridDim.x <= max_blocks.  out[k] receives the reduced values.
+template <int K>
+__device__ void grid_reduce(double (&v)[K], unsigned maxmask, double* partials, int max_blocks,
+                            unsigned* counter, double* out) {
+    __shared__ bool last;
+    block_reduce<K>(v, maxmask);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) partials[k * max_blocks + blockIdx.x] = v[k];
+        __threadfence();
+        unsigned ticket = atomicAdd(counter, 1u);
+        last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double w[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const bool mx = (maxmask >> k) & 1;
+        double a = mx ? -INFINITY : 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+            double p = ((volatile double*)partials)[k * max_blocks + b];
+            a = mx ? fmax(a, p) : a + p;
+        }
+        w[k] = a;
+    }
+    block_reduce<K>(w, maxmask);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[k] = w[k];
+        *counter = 0u;
+    }
+}
+
+}  // namespace impec

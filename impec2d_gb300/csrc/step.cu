@@ -1,0 +1,328 @@
+// IMPES step orchestration, diagnostics, host-layout transfers and the per-operation C ABI.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+#include "reduce.cuh"
+
+namespace impec {
+
+#define IX(i, j, n2) ((size_t)(i) * (n2) + (j))
+
+static impec_status set_dt(impec_ctx* ctx, double dt) {
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(&ctx->dscal->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    return IMPEC_OK;
+}
+
+// HyperbolicSplitSolver::Solve with SPLIT2ND (src/HyperbolicSplitSolver.cpp:162-198).
+impec_status hyperbolic_solve_dev(impec_ctx* ctx, double* c, const double* u, const double* v, const double* dt_dev,
+                                  int* pfs) {
+    const impec_params& P = ctx->P;
+    IMPEC_TRY(tr_integrate_dev(ctx, c, 0.5, dt_dev, 0));
+    if (P.diffusion) IMPEC_TRY(dispersion_cn_dev(ctx, c, u, v, 0.5, dt_dev, P.para_eps, nullptr, nullptr));
+    IMPEC_TRY(advect_split_dev(ctx, c, u, v, dt_dev, pfs));
+    IMPEC_TRY(tr_integrate_dev(ctx, c, 0.5, dt_dev, 1));
+    if (P.diffusion) IMPEC_TRY(dispersion_cn_dev(ctx, c, u, v, 0.5, dt_dev, P.para_eps, nullptr, nullptr));
+    return IMPEC_OK;
+}
+
+// GetTotalMass, CalculateDivergenceError, CalculateVelocityBoundaryError, max/min c
+// (src/Impec2DSolver.cpp:430-431, 542-620).
+__global__ void __launch_bounds__(RED_THREADS) k_diag(int n1, int n2, const double* __restrict__ c,
+                                                      const double* __restrict__ u, const double* __restrict__ v,
+                                                      const double* __restrict__ q, double inv_dx, double inv_dy,
+                                                      double* partials, int mb, unsigned* counter, double* out) {
+    double acc[5] = {0.0, 0.0, 0.0, -INFINITY, -INFINITY};
+    const size_t n = (size_t)n1 * n2;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        int i = (int)(k / n2), j = (int)(k % n2);
+        double cc = c[k];
+        acc[0] += cc;
+        double div = (v[IX(i, j + 1, n2 + 1)] - v[IX(i, j, n2 + 1)]) * inv_dy + (u[IX(i + 1, j, n2)] - u[IX(i, j, n2)]) * inv_dx;
+        acc[1] += fabs(div - (q ? q[k] : 0.0));
+        double be = 0;
+        if (j == 0) be += fabs(v[IX(i, 0, n2 + 1)]);
+        if (j == n2 - 1) be += fabs(v[IX(i, n2, n2 + 1)]);
+        if (i == 0) be += fabs(u[IX(0, j, n2)]);
+        if (i == n1 - 1) be += fabs(u[IX(n1, j, n2)]);
+        acc[2] += be;
+        acc[3] = fmax(acc[3], cc);
+        acc[4] = fmax(acc[4], -cc);
+    }
+    grid_reduce<5>(acc, (1u << 3) | (1u << 4), partials, mb, counter, out);
+}
+
+static impec_status diagnostics_dev(impec_ctx* ctx, const double* c, const double* u, const double* v) {
+    const impec_params& P = ctx->P;
+    k_diag<<<ctx->num_sms * 2, RED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, u, v, ctx->have_source ? ctx->q : nullptr,
+                                                              1.0 / ctx->G.dx, 1.0 / ctx->G.dy, ctx->partials,
+                                                              ctx->max_blocks, ctx->counter, ctx->dscal->red);
+    IMPEC_LAUNCH_CHECK();
+    return IMPEC_OK;
+}
+
+// CalculateMassError (src/Impec2DSolver.cpp:530-540)
+static double mass_error(const impec_ctx* ctx, double mass, double t) {
+    double influx = (t - ctx->t0) * ctx->P.I * (1. / (ctx->G.dx * ctx->G.dy));
+    if (ctx->P.stype == IMPEC_PARALLEL) influx *= 2.;
+    return fabs((mass + ctx->total_outflux - influx) / influx);
+}
+
+static impec_status one_step(impec_ctx* ctx, double t_clip, bool sync_dt, impec_step_info* info) {
+    const impec_params& P = ctx->P;
+    int cyc = 0;
+    double rr = 0;
+    IMPEC_TRY(pressure_solve(ctx, ctx->c, ctx->p, P.eps, &cyc, &rr));
+    IMPEC_TRY(velocity(ctx, ctx->p, ctx->c, ctx->u, ctx->v));
+    IMPEC_TRY(max_stable_dt_dev(ctx, ctx->u, ctx->v));
+    double dt = 0;
+    int clipped = 0;
+    if (sync_dt) {
+        IMPEC_TRY(sync_scalars(ctx));
+        dt = ctx->hscal->dt;
+        if (t_clip >= 0 && ctx->t + dt >= t_clip) {  // output-time matching, src/Impec2DSolver.cpp:375-378
+            dt = t_clip - ctx->t;
+            IMPEC_TRY(set_dt(ctx, dt));
+            clipped = 1;
+        }
+    }
+    IMPEC_TRY(hyperbolic_solve_dev(ctx, ctx->c, ctx->u, ctx->v, &ctx->dscal->dt, &ctx->prev_first_sweep));
+    ctx->counter_steps++;
+    if (sync_dt) ctx->t += dt;
+    if (info) {
+        IMPEC_TRY(sync_scalars(ctx));
+        if (!sync_dt) ctx->t += ctx->hscal->dt;
+        ctx->total_outflux = ctx->hscal->total_outflux;
+        info->t = ctx->t;
+        info->dt = ctx->hscal->dt;
+        info->total_outflux = ctx->total_outflux;
+        info->relres = rr;
+        info->counter = ctx->counter_steps;
+        info->its = cyc;
+        info->para_its = ctx->last_para_its;
+        info->prev_first_sweep = ctx->prev_first_sweep;
+        info->clipped = clipped;
+        IMPEC_TRY(diagnostics_dev(ctx, ctx->c, ctx->u, ctx->v));
+        IMPEC_TRY(sync_scalars(ctx));
+        info->mass_err = mass_error(ctx, ctx->hscal->red[0], ctx->t);
+    }
+    return IMPEC_OK;
+}
+
+}  // namespace impec
+
+using namespace impec;
+
+extern "C" {
+
+impec_status impec_pressure_solve(impec_ctx* ctx, const double* c, double* p, double tol, int* cycles, double* relres) {
+    if (!ctx || !c || !p) return IMPEC_ERR_ARG;
+    impec_status s = pressure_solve(ctx, c, p, tol, cycles, relres);
+    if (s == IMPEC_OK) IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+impec_status impec_face_mobility(impec_ctx* ctx, const double* c, double* lamx, double* lamy) {
+    if (!ctx || !c) return IMPEC_ERR_ARG;
+    IMPEC_TRY(face_mobility(ctx, c));
+    const size_t nu = (size_t)(ctx->P.N1 + 1) * ctx->P.N2, nv = (size_t)ctx->P.N1 * (ctx->P.N2 + 1);
+    if (lamx) IMPEC_CUDA_TRY(cudaMemcpyAsync(lamx, ctx->lamx, nu * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (lamy) IMPEC_CUDA_TRY(cudaMemcpyAsync(lamy, ctx->lamy, nv * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_pressure_apply(impec_ctx* ctx, const double* c, const double* x, double* y) {
+    if (!ctx || !c || !x || !y) return IMPEC_ERR_ARG;
+    IMPEC_TRY(pressure_setup(ctx, c));
+    IMPEC_TRY(pressure_apply_ref(ctx, x, y));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_velocity(impec_ctx* ctx, const double* p, const double* c, double* u, double* v) {
+    if (!ctx || !p || !c || !u || !v) return IMPEC_ERR_ARG;
+    IMPEC_TRY(face_mobility(ctx, c));
+    IMPEC_TRY(velocity(ctx, p, c, u, v));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_max_stable_dt(impec_ctx* ctx, const double* u, const double* v, double* dt) {
+    if (!ctx || !u || !v || !dt) return IMPEC_ERR_ARG;
+    IMPEC_TRY(max_stable_dt_dev(ctx, u, v));
+    IMPEC_TRY(sync_scalars(ctx));
+    *dt = ctx->hscal->dt;
+    return IMPEC_OK;
+}
+
+impec_status impec_tr_integrate(impec_ctx* ctx, double* c, double dt, double* tmo) {
+    if (!ctx || !c) return IMPEC_ERR_ARG;
+    IMPEC_TRY(set_dt(ctx, dt));
+    IMPEC_CUDA_TRY(cudaMemsetAsync(&ctx->dscal->tmo_pre, 0, sizeof(double), ctx->stream));
+    IMPEC_TRY(tr_integrate_dev(ctx, c, 1.0, &ctx->dscal->dt, 0));
+    IMPEC_TRY(sync_scalars(ctx));
+    if (tmo) *tmo = ctx->hscal->tmo_pre;
+    return IMPEC_OK;
+}
+
+impec_status impec_advect_x(impec_ctx* ctx, double* c, const double* u, double dt) {
+    if (!ctx || !c || !u) return IMPEC_ERR_ARG;
+    IMPEC_TRY(set_dt(ctx, dt));
+    IMPEC_TRY(advect_x_dev(ctx, c, ctx->t1, u, 1.0, &ctx->dscal->dt));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(c, ctx->t1, (size_t)ctx->P.N1 * ctx->P.N2 * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_advect_y(impec_ctx* ctx, double* c, const double* v, double dt) {
+    if (!ctx || !c || !v) return IMPEC_ERR_ARG;
+    IMPEC_TRY(set_dt(ctx, dt));
+    IMPEC_TRY(advect_y_dev(ctx, c, ctx->t1, v, 1.0, &ctx->dscal->dt));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(c, ctx->t1, (size_t)ctx->P.N1 * ctx->P.N2 * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_advect_split(impec_ctx* ctx, double* c, const double* u, const double* v, double dt, int* pfs) {
+    if (!ctx || !c || !u || !v || !pfs) return IMPEC_ERR_ARG;
+    IMPEC_TRY(set_dt(ctx, dt));
+    IMPEC_TRY(advect_split_dev(ctx, c, u, v, &ctx->dscal->dt, pfs));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_dispersion_cn(impec_ctx* ctx, double* c, const double* u, const double* v, double dt, double tol,
+                                 int* its, double* relres) {
+    if (!ctx || !c || !u || !v) return IMPEC_ERR_ARG;
+    IMPEC_TRY(set_dt(ctx, dt));
+    impec_status s = dispersion_cn_dev(ctx, c, u, v, 1.0, &ctx->dscal->dt, tol, its, relres);
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+impec_status impec_hyperbolic_solve(impec_ctx* ctx, double* c, const double* u, const double* v, double dt, int* pfs,
+                                    double* outflux) {
+    if (!ctx || !c || !u || !v || !pfs) return IMPEC_ERR_ARG;
+    IMPEC_TRY(set_dt(ctx, dt));
+    double z = outflux ? *outflux : 0.0;
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(&ctx->dscal->total_outflux, &z, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_TRY(hyperbolic_solve_dev(ctx, c, u, v, &ctx->dscal->dt, pfs));
+    IMPEC_TRY(sync_scalars(ctx));
+    if (outflux) *outflux = ctx->hscal->total_outflux;
+    return IMPEC_OK;
+}
+
+impec_status impec_diagnostics(impec_ctx* ctx, const double* c, const double* u, const double* v, double out[5]) {
+    if (!ctx || !c || !u || !v || !out) return IMPEC_ERR_ARG;
+    IMPEC_TRY(diagnostics_dev(ctx, c, u, v));
+    IMPEC_TRY(sync_scalars(ctx));
+    const double* r = ctx->hscal->red;
+    out[0] = r[0];
+    out[1] = r[1] * ctx->G.dx * ctx->G.dx;
+    out[2] = r[2];
+    out[3] = r[3];
+    out[4] = -r[4];
+    return IMPEC_OK;
+}
+
+impec_status impec_step(impec_ctx* ctx, double t_clip, impec_step_info* info) {
+    if (!ctx) return IMPEC_ERR_ARG;
+    impec_step_info tmp;
+    IMPEC_TRY(one_step(ctx, t_clip, true, info ? info : &tmp));
+    return IMPEC_OK;
+}
+
+impec_status impec_run_steps(impec_ctx* ctx, int n, impec_step_info* info) {
+    if (!ctx || n < 0) return IMPEC_ERR_ARG;
+    for (int s = 0; s < n; ++s) IMPEC_TRY(one_step(ctx, -1.0, false, (s == n - 1) ? info : nullptr));
+    if (n == 0 || !info) IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_set_time(impec_ctx* ctx, double t0) {
+    if (!ctx) return IMPEC_ERR_ARG;
+    ctx->t = ctx->t0 = t0;
+    ctx->total_outflux = 0;
+    ctx->counter_steps = 0;
+    double z = 0.0;
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(&ctx->dscal->total_outflux, &z, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_set_pin_kappa(impec_ctx* ctx, double kappa) {
+    if (!ctx || !(kappa != 0.0) || !std::isfinite(kappa)) return IMPEC_ERR_ARG;
+    ctx->pin_kappa = kappa;
+    return IMPEC_OK;
+}
+
+impec_status impec_velocity_upload(impec_ctx* ctx, const double* v_host, int g) {
+    if (!ctx || !v_host || g < 0) return IMPEC_ERR_ARG;
+    const int N1 = ctx->P.N1, N2 = ctx->P.N2, wv = N2 + 1 + 2 * g;
+    std::vector<double> hu((size_t)(N1 + 1) * N2), hv((size_t)N1 * (N2 + 1));
+    for (int i = 0; i <= N1; ++i)
+        for (int j = 0; j < N2; ++j) hu[IX(i, j, N2)] = v_host[((size_t)(i + g) * wv + (j + g)) * 2 + 0];
+    for (int i = 0; i < N1; ++i)
+        for (int j = 0; j <= N2; ++j) hv[IX(i, j, N2 + 1)] = v_host[((size_t)(i + g) * wv + (j + g)) * 2 + 1];
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->u, hu.data(), hu.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->v, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_pressure_upload(impec_ctx* ctx, const double* p_host, int g) {
+    if (!ctx || !p_host || g < 0) return IMPEC_ERR_ARG;
+    const int N1 = ctx->P.N1, N2 = ctx->P.N2, w = N2 + 2 * g;
+    std::vector<double> buf((size_t)N1 * N2);
+    for (int i = 0; i < N1; ++i) std::memcpy(&buf[IX(i, 0, N2)], p_host + (size_t)(i + g) * w + g, N2 * 8);
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->p, buf.data(), buf.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+// Reference ghost layouts on the host <-> engine device layout.
+impec_status impec_state_upload(impec_ctx* ctx, const double* c_host, const double* q_host, int g) {
+    if (!ctx || g < 0) return IMPEC_ERR_ARG;
+    const int N1 = ctx->P.N1, N2 = ctx->P.N2, w = N2 + 2 * g;
+    std::vector<double> buf((size_t)N1 * N2);
+    if (c_host) {
+        for (int i = 0; i < N1; ++i) std::memcpy(&buf[IX(i, 0, N2)], c_host + (size_t)(i + g) * w + g, N2 * 8);
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->c, buf.data(), buf.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+        IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    }
+    if (q_host) {
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->q, q_host, (size_t)N1 * N2 * 8, cudaMemcpyHostToDevice, ctx->stream));
+        IMPEC_TRY(impec_set_source(ctx, ctx->q));
+    }
+    return IMPEC_OK;
+}
+
+impec_status impec_state_download(impec_ctx* ctx, double* c_host, double* p_host, double* v_host, int g) {
+    if (!ctx || g < 0) return IMPEC_ERR_ARG;
+    const int N1 = ctx->P.N1, N2 = ctx->P.N2, w = N2 + 2 * g;
+    std::vector<double> buf((size_t)N1 * N2);
+    auto get = [&](const double* dev, double* host) -> impec_status {
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(buf.data(), dev, buf.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        for (int i = 0; i < N1; ++i) std::memcpy(host + (size_t)(i + g) * w + g, &buf[IX(i, 0, N2)], N2 * 8);
+        return IMPEC_OK;
+    };
+    if (c_host) IMPEC_TRY(get(ctx->c, c_host));
+    if (p_host) IMPEC_TRY(get(ctx->p, p_host));
+    if (v_host) {
+        const int wv = N2 + 1 + 2 * g;
+        std::vector<double> hu((size_t)(N1 + 1) * N2), hv((size_t)N1 * (N2 + 1));
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(hu.data(), ctx->u, hu.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(hv.data(), ctx->v, hv.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        for (int i = 0; i <= N1; ++i)
+            for (int j = 0; j < N2; ++j) v_host[((size_t)(i + g) * wv + (j + g)) * 2 + 0] = hu[IX(i, j, N2)];
+        for (int i = 0; i < N1; ++i)
+            for (int j = 0; j <= N2; ++j) v_host[((size_t)(i + g) * wv + (j + g)) * 2 + 1] = hv[IX(i, j, N2 + 1)];
+    }
+    return IMPEC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,188 @@
+/*
+ * impec2d.h -- C ABI of the GB300-native Impec2D IMPES engine (libimpec2d.so).
+ *
+ * Plain C types only.  Every call returns an impec_status; no call exits the process.
+ * Device-pointer entry points ("_dev" arrays) take CUDA device memory in the engine's
+ * device layout; the host entry points take host arrays in the reference's Blitz layout
+ * and copy them across inside the call.
+ *
+ * Device layout (row-major, j fastest, no ghost cells; ghosts are applied by reflection
+ * inside the kernels exactly as the reference's ghost fills define them):
+ *   cell fields c, p, q, K:  N1 x N2,        element (i,j) at i*N2 + j
+ *   x-face field u:           (N1+1) x N2,    u(i,j) is the face between cells (i-1,j), (i,j)
+ *   y-face field v:           N1 x (N2+1),    v(i,j) is the face between cells (i,j-1), (i,j)
+ * Host (reference) layout, src/Impec2DSolver.cpp:151-182:
+ *   c, p: (N1+2g) x (N2+2g);  v: (N1+1+2g) x (N2+1+2g) x 2 (k innermost);  q: N1*N2.
+ *
+ * Each entry point names the reference interface it replaces (pw359/Impec2D, src/...).
+ */
+#ifndef IMPEC2D_H
+#define IMPEC2D_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    IMPEC_OK = 0,
+    IMPEC_ERR_ARG = 1,          /* invalid argument or size */
+    IMPEC_ERR_CUDA = 2,         /* a CUDA call failed; see impec_last_error() */
+    IMPEC_ERR_NOT_CONVERGED = 3,/* solver hit its cycle limit above tolerance */
+    IMPEC_ERR_NAN = 4,          /* a NaN/Inf appeared in a residual or field */
+    IMPEC_ERR_NO_DEVICE = 5,    /* no CUDA device / extension not usable */
+    IMPEC_ERR_CONFIG = 6        /* .cfg parse or validation error */
+} impec_status;
+
+/* Enumerations keep the reference's values (src/SimParams.h:14-27). */
+enum { IMPEC_MEANCONC = 0, IMPEC_HARMONIC = 1 };
+enum { IMPEC_EXPLICIT = 0, IMPEC_CRANKNICOLSON = 1 };
+enum { IMPEC_ALTERNATING = 0, IMPEC_X_FIRST = 1, IMPEC_Y_FIRST = 2, IMPEC_STRANG = 3,
+       IMPEC_SYMMETRIC_PARALLEL = 4 };
+enum { IMPEC_UPWINDSPLIT = 0, IMPEC_MUSCL = 4 };
+enum { IMPEC_PARALLEL = 0, IMPEC_DIAGONAL = 1, IMPEC_HORIZONTAL = 2 };
+enum { IMPEC_BC_NEUMANN = 0, IMPEC_BC_PERIODIC = 1 };
+/* Pressure-solver precision: plain FP64 multigrid, or FP32 V-cycles inside FP64
+ * iterative refinement (residual, update, coarsest solve in FP64). */
+enum { IMPEC_PREC_FP64 = 0, IMPEC_PREC_MIXED = 1 };
+
+/* Numerical parameters: the subset of SimParams (src/SimParams.h:29-164) that the hot
+ * path reads, plus the engine's own options (marked "engine"). */
+typedef struct {
+    int N1, N2;
+    double x_lb, x_ub, y_lb, y_ub;
+    double mu_res, mu_inj;
+    int avgproc;              /* IMPEC_HARMONIC | IMPEC_MEANCONC */
+    double nu;                /* stencil weight: 1 = 5-point, <1 = 9-point */
+    double porosity, cfl, inj_fluid_conc, I;
+    int diffusion;            /* Crank-Nicolson Peaceman dispersion on/off */
+    double alpha_l, alpha_t;  /* cell units (multiplied by max(dx,dy)) */
+    double Dm;                /* engine: molecular diffusion, 0 = reference */
+    int ptype;                /* dt rule: IMPEC_CRANKNICOLSON ignores the diffusion limit */
+    double dt_diff_limit;
+    int dim_splitting;        /* IMPEC_SYMMETRIC_PARALLEL etc. */
+    int hmtype;               /* IMPEC_MUSCL | IMPEC_UPWINDSPLIT */
+    int stype;                /* IMPEC_PARALLEL | IMPEC_DIAGONAL (sets the pinned cell) */
+    int is_test, testno;      /* analytic permeability of the elliptic tests */
+    int bc;                   /* IMPEC_BC_NEUMANN, or IMPEC_BC_PERIODIC (advection test) */
+    double eps, para_eps;     /* elliptic / parabolic relative-residual tolerances */
+    int peaceman_guard;       /* engine: Peaceman term := 0 where |u| = 0 (reference: NaN) */
+    int cfl_porosity;         /* engine: CFL on interstitial speed |u|/phi (reference: 0) */
+    int precision;            /* engine: IMPEC_PREC_FP64 | IMPEC_PREC_MIXED */
+    int max_cycles;           /* engine: multigrid cycle limit per solve */
+    int warm_start;           /* engine: 1 = start from the previous pressure (reference: 0) */
+} impec_params;
+
+typedef struct impec_ctx impec_ctx;
+
+/* Last error message of this thread (static storage). */
+const char* impec_last_error(void);
+/* Fill *P with the defaults of examples/parallel.cfg for an N1 x N2 unit-square grid. */
+void impec_default_params(impec_params* P, int N1, int N2);
+
+/* Context: device workspaces for one grid.  stream may be NULL (legacy default stream).
+ * Replaces the constructors MGSolver::MGSolver (src/MGSolver.cpp:52-143) and
+ * HyperbolicSolver::HyperbolicSolver (src/HyperbolicSolver.cpp:63-67). */
+impec_status impec_ctx_create(const impec_params* P, void* cuda_stream, impec_ctx** out);
+impec_status impec_ctx_destroy(impec_ctx* ctx);
+impec_status impec_ctx_params(const impec_ctx* ctx, impec_params* P);
+/* Engine: per-cell permeability (device N1*N2 arrays, K22 may be NULL = K11; both NULL = 1).
+ * Replaces K_11/K_22 (src/EllipticSolver.cpp:418-470). */
+impec_status impec_set_permeability(impec_ctx* ctx, const double* K11_dev, const double* K22_dev);
+/* Source term (device N1*N2).  Builds the well list used by the TR integrator. */
+impec_status impec_set_source(impec_ctx* ctx, const double* q_dev);
+
+/* Pressure solve: EllipticSolver::Solve -> MGSolver::SolveLinearMultigrid
+ * (src/EllipticSolver.cpp:133-142, src/MGSolver.cpp:145-248).  Solves the reference's
+ * pinned 9-point (nu<1) or 5-point (nu=1) system to ||b-Ap||/||b|| <= tol.
+ * p_dev is the initial guess when warm_start is set, else it is overwritten. */
+impec_status impec_pressure_solve(impec_ctx* ctx, const double* c_dev, double* p_dev,
+                                  double tol, int* cycles, double* relres);
+/* Pressure operator assembly only (engine diagnostics / tests): writes the face
+ * mobilities lamx ((N1+1)*N2) and lamy (N1*(N2+1)) used by the solve. */
+impec_status impec_face_mobility(impec_ctx* ctx, const double* c_dev, double* lamx_dev,
+                                 double* lamy_dev);
+/* y = A x with the reference's pinned pressure matrix (src/MGSolver.cpp:268-570). */
+impec_status impec_pressure_apply(impec_ctx* ctx, const double* c_dev, const double* x_dev,
+                                  double* y_dev);
+
+/* Darcy face velocities: EllipticSolver::CalcVelocities (src/EllipticSolver.cpp:660-683). */
+impec_status impec_velocity(impec_ctx* ctx, const double* p_dev, const double* c_dev,
+                            double* u_dev, double* v_dev);
+/* HyperbolicSolver::MaxStableTimestep (src/HyperbolicSolver.cpp:73-198). */
+impec_status impec_max_stable_dt(impec_ctx* ctx, const double* u_dev, const double* v_dev,
+                                 double* dt);
+
+/* TRIntegrator::Integrate (src/TRIntegrator.cpp:49-71); *tmo = total_mass_outflux. */
+impec_status impec_tr_integrate(impec_ctx* ctx, double* c_dev, double dt, double* tmo);
+/* HyperbolicSplitSolver::Advect_X / Advect_Y (src/HyperbolicSplitSolver.cpp:113-159). */
+impec_status impec_advect_x(impec_ctx* ctx, double* c_dev, const double* u_dev, double dt);
+impec_status impec_advect_y(impec_ctx* ctx, double* c_dev, const double* v_dev, double dt);
+/* HyperbolicSplitSolver::AdvectSplit (src/HyperbolicSplitSolver.cpp:51-106).
+ * prev_first_sweep: 0 = X_SWEEP, 1 = Y_SWEEP (in/out). */
+impec_status impec_advect_split(impec_ctx* ctx, double* c_dev, const double* u_dev,
+                                const double* v_dev, double dt, int* prev_first_sweep);
+/* HyperbolicSolver::DiffusionSplitCN -> MGSolver::Solve_Parabolic_cc_to_c
+ * (src/HyperbolicSolver.cpp:217-223, src/MGSolver.cpp:846-1392). */
+impec_status impec_dispersion_cn(impec_ctx* ctx, double* c_dev, const double* u_dev,
+                                 const double* v_dev, double dt, double tol, int* its,
+                                 double* relres);
+/* HyperbolicSplitSolver::Solve (src/HyperbolicSplitSolver.cpp:162-198); *outflux
+ * accumulates |total_mass_outflux| of both source half steps. */
+impec_status impec_hyperbolic_solve(impec_ctx* ctx, double* c_dev, const double* u_dev,
+                                    const double* v_dev, double dt, int* prev_first_sweep,
+                                    double* outflux);
+
+/* Reductions of src/Impec2DSolver.cpp:530-620: out[0] total mass, out[1] divergence
+ * error, out[2] no-flow boundary error, out[3] max c, out[4] min c. */
+impec_status impec_diagnostics(impec_ctx* ctx, const double* c_dev, const double* u_dev,
+                               const double* v_dev, double out[5]);
+
+/* ---- resident simulation: one IMPES step per call, state kept in HBM ---- */
+typedef struct {
+    double t, dt, total_outflux, relres, mass_err;
+    int counter, its, para_its, prev_first_sweep;
+    int clipped;              /* 1 if dt was shortened to reach t_clip */
+} impec_step_info;
+/* Device state (c, p, u, v, q) is owned by the context; these return its pointers. */
+impec_status impec_state(impec_ctx* ctx, double** c_dev, double** p_dev, double** u_dev,
+                         double** v_dev, double** q_dev);
+/* Start time of the run (reference: starttime, src/Impec2DSolver.cpp:300); resets the
+ * engine clock t and the outflux accumulator used by the mass balance. */
+impec_status impec_set_time(impec_ctx* ctx, double t0);
+/* One pass of the loop body of Impec2DSolver::Solve (src/Impec2DSolver.cpp:339-415) on the
+ * resident state.  With t_clip >= 0, dt is shortened to t_clip - t when t + dt >= t_clip
+ * (output-time matching, :375-378); t_clip < 0 disables it. */
+impec_status impec_step(impec_ctx* ctx, double t_clip, impec_step_info* info);
+/* n steps with no host synchronisation between them (dt stays on the device; info of the
+ * last step is returned).  Used by throughput runs. */
+impec_status impec_run_steps(impec_ctx* ctx, int n, impec_step_info* info);
+
+/* ---- host-buffer entry points (reference Blitz layouts; copies inside the call) ---- */
+impec_status impec_state_upload(impec_ctx* ctx, const double* c_host, const double* q_host,
+                                int ghost);
+impec_status impec_state_download(impec_ctx* ctx, double* c_host, double* p_host,
+                                  double* v_host, int ghost);
+/* Host velocity (reference layout, v(i,j,k)) -> device u, v of the resident state. */
+impec_status impec_velocity_upload(impec_ctx* ctx, const double* v_host, int ghost);
+/* Host pressure (reference layout) -> device p of the resident state. */
+impec_status impec_pressure_upload(impec_ctx* ctx, const double* p_host, int ghost);
+/* Dirichlet-row coefficient kappa of the pinned cell (row = kappa/dA, src/MGSolver.cpp:518-567);
+ * 1 in production runs, chosen from the exact solution in the elliptic tests. */
+impec_status impec_set_pin_kappa(impec_ctx* ctx, double kappa);
+
+/* ---- configuration files (libconfig .cfg of the reference, src/SimParams.cpp:45-468) ---- */
+/* Parse a .cfg into engine parameters (+ start/end time).  Errors: IMPEC_ERR_CONFIG. */
+impec_status impec_cfg_load(const char* path, impec_params* P, double* tstart, double* tfinal);
+/* Source term q (host, N1*N2) of the .cfg's wells: Impec2DSolver::InitializeSource
+ * (src/Impec2DSolver.cpp:241-280). */
+impec_status impec_cfg_source(const char* path, double* q_host);
+/* Run a whole .cfg like the reference executable: Impec2DSolver(cfg).Run()
+ * (src/Driver.cpp:58-87); quiet suppresses the per-step console line. */
+impec_status impec_run_cfg(const char* path, int quiet);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

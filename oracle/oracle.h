@@ -77,6 +77,8 @@ void or_pressure_matrix(const or_params* P, const double* c, double* A9);
 /* Same matrix but the pinned rows keep their folded Neumann coefficients. */
 void or_pressure_matrix_neumann(const or_params* P, const double* c, double* A9);
 void or_pressure_rhs(const or_params* P, const double* q, double* b);
+/* Face mobilities KoverMu_11_im12j ((N1+1)*N2) and KoverMu_22_ijm12 (N1*(N2+1)). */
+void or_face_mobility(const or_params* P, const double* c, double* lamx, double* lamy);
 void or_matvec9(const or_params* P, const double* A9, const double* x, double* y);
 double or_relres9(const or_params* P, const double* A9, const double* x, const double* b);
 /* Direct banded LU (+ iterative refinement).  Returns 0 on success. */

@@ -427,6 +427,20 @@ void or_pressure_matrix_neumann(const or_params* P, const double* c, double* A9)
     assemble_pressure(P, c, A9, false);
 }
 
+// Face mobilities as used by GetParallelCoefficientsForCell / GetParallelU*:
+// lamx(i,j) = KoverMu_11_im12j(c(i-1,j), c(i,j), i, j) for i in [0,N1], j in [0,N2);
+// lamy(i,j) = KoverMu_22_ijm12(c(i,j-1), c(i,j), i, j) for i in [0,N1), j in [0,N2].
+void or_face_mobility(const or_params* P, const double* cflat, double* lamx, double* lamy) {
+    Geo G(P);
+    S2 c = sview(P, cflat);
+    for (int i = 0; i <= P->N1; ++i)
+        for (int j = 0; j < P->N2; ++j)
+            lamx[(size_t)i * P->N2 + j] = KoverMu_11_im12j(P, G, c(i - 1, j), c(i, j), i, j);
+    for (int i = 0; i < P->N1; ++i)
+        for (int j = 0; j <= P->N2; ++j)
+            lamy[(size_t)i * (P->N2 + 1) + j] = KoverMu_22_ijm12(P, G, c(i, j - 1), c(i, j), i, j);
+}
+
 // SetRHS_Elliptic (src/MGSolver.cpp:573-590): b = -q
 void or_pressure_rhs(const or_params* P, const double* q, double* b) {
     const size_t M = (size_t)P->N1 * P->N2;

@@ -1,0 +1,79 @@
+"""The .cfg front end (libconfig subset, SimParams semantics of src/SimParams.cpp:45-468):
+parses the reference's example files unchanged, reports missing keys as a status instead of
+exiting, and maps the engine options."""
+import glob
+import os
+
+import pytest
+
+import impec2d_gb300 as E
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_EXAMPLES = "/root/reference/examples"
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from impec2d_gb300 import build as B
+    B.build()
+
+
+def test_fixture_config1():
+    P, t0, t1 = E.load_cfg(os.path.join(HERE, "golden", "quarter_five_spot_128_upwind.cfg"))
+    assert (P.N1, P.N2) == (128, 128) and P.stype == E.DIAGONAL and P.hmtype == E.UPWINDSPLIT
+    assert P.porosity == 0.2 and P.cfl == 0.5 and P.cfl_porosity == 1 and P.nu == 1.0
+    assert (t0, t1) == (0.0, 0.06)
+    q = E.cfg_source(os.path.join(HERE, "golden", "quarter_five_spot_128_upwind.cfg"), 128, 128)
+    assert q[0] == pytest.approx(128 * 128) and q[-1] == pytest.approx(-128 * 128) and (q != 0).sum() == 2
+
+
+def test_fixture_config2():
+    P, t0, t1 = E.load_cfg(os.path.join(HERE, "golden", "parallel_1024_muscl_dispersion.cfg"))
+    assert (P.N1, P.N2) == (1024, 1024) and P.stype == E.PARALLEL and P.hmtype == E.MUSCL
+    assert P.diffusion == 1 and P.alpha_l == 1e-3 and P.alpha_t == 1e-4 and P.Dm == 1e-6
+    assert P.eps == 1e-10 and P.precision == E.PREC_FP64 and P.bc == E.BC_NEUMANN
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not mounted")
+def test_reference_examples_parse_unchanged():
+    files = sorted(glob.glob(os.path.join(REF_EXAMPLES, "*.cfg")))
+    assert len(files) == 5
+    for f in files:
+        P, t0, t1 = E.load_cfg(f)
+        assert P.N1 >= 2 and P.N2 >= 2 and t1 > t0
+        name = os.path.basename(f)
+        if name == "parallel.cfg":
+            assert (P.N1, P.stype, P.nu) == (141, E.PARALLEL, pytest.approx(2 / 3))
+        if name == "diagonal_dispersion.cfg":
+            assert (P.N1, P.N2, P.diffusion) == (100, 50, 1)
+        if name == "hyperbolic_test.cfg":
+            assert P.is_test == 1 and P.bc == E.BC_PERIODIC and P.cfl == 0.95
+
+
+def _write(tmp_path, text):
+    p = tmp_path / "x.cfg"
+    p.write_text(text)
+    return str(p)
+
+
+def test_missing_key_is_a_status(tmp_path):
+    base = open(os.path.join(HERE, "golden", "quarter_five_spot_128_upwind.cfg")).read()
+    bad = base.replace("mu_res = 41.0;", "")
+    with pytest.raises(E.ImpecError) as ei:
+        E.load_cfg(_write(tmp_path, bad))
+    assert ei.value.status == 6
+
+
+@pytest.mark.parametrize("edit", [("\"diagonal\"", "\"sideways\""), ("\"upwind_split\"", "\"weno\""),
+                                  ("dimensional_splitting = \"parallel\"", "dimensional_splitting = \"zigzag\""), ("{ para_method", "( para_method")])
+def test_invalid_values_are_rejected(tmp_path, edit):
+    base = open(os.path.join(HERE, "golden", "quarter_five_spot_128_upwind.cfg")).read()
+    with pytest.raises(E.ImpecError):
+        E.load_cfg(_write(tmp_path, base.replace(*edit)))
+
+
+def test_comments_lists_and_unknown_keys(tmp_path):
+    base = open(os.path.join(HERE, "golden", "quarter_five_spot_128_upwind.cfg")).read()
+    txt = base.replace("log_time_list = [];", "log_time_list = [0.01, 0.02, 3e-2]; /* block */ extra_key = \"x\";")
+    P, t0, t1 = E.load_cfg(_write(tmp_path, txt))
+    assert P.N1 == 128

@@ -1,0 +1,288 @@
+"""Per-operation parity of the CUDA engine (through the C ABI) against the CPU oracle.
+
+Tolerances (relative to the field's max magnitude): 1e-13 for single operators
+(mobility, operator apply, velocity, one transport sweep, TR); for linear solves the
+relative residual under the oracle's own matrix must reach the requested tolerance and
+the solution must agree with the oracle's banded-LU solve to within a condition-number
+allowance stated per test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import cell_ghost, dev, host, oparams, rel_err, smooth_field, source, vel_ghost, vel_split
+
+pytestmark = pytest.mark.gpu
+
+GRIDS = [(32, 32), (37, 29), (48, 64)]
+
+
+def _ctx(E, N1, N2, **kw):
+    P = E.default_params(N1, N2, **kw)
+    return P, E.Context(P)
+
+
+def _rand_c(N1, N2, seed):
+    return smooth_field(N1, N2, seed)
+
+
+@pytest.mark.parametrize("N1,N2", GRIDS)
+@pytest.mark.parametrize("avg", [1, 0])
+def test_face_mobility_bitexact(engine, oracle_lib, N1, N2, avg):
+    E = engine
+    P, ctx = _ctx(E, N1, N2, avgproc=avg)
+    OP = oparams(P)
+    c = _rand_c(N1, N2, 1)
+    lx, ly = np.zeros((N1 + 1) * N2), np.zeros(N1 * (N2 + 1))
+    oracle_lib.or_face_mobility(C.byref(OP), O.ptr(cell_ghost(OP, c)), O.ptr(lx), O.ptr(ly))
+    import torch
+    dlx = torch.zeros((N1 + 1) * N2, dtype=torch.float64, device="cuda")
+    dly = torch.zeros(N1 * (N2 + 1), dtype=torch.float64, device="cuda")
+    ctx.face_mobility(dev(c), dlx, dly)
+    # same operations in the same order: bit-identical
+    assert np.array_equal(host(dlx), lx)
+    assert np.array_equal(host(dly), ly)
+
+
+@pytest.mark.parametrize("N1,N2", GRIDS)
+@pytest.mark.parametrize("nu", [1.0, 2.0 / 3.0])
+@pytest.mark.parametrize("stype", [1, 0])
+def test_pressure_apply(engine, oracle_lib, N1, N2, nu, stype):
+    E = engine
+    if stype == 0 and N1 != N2:
+        pytest.skip("parallel configuration requires a square grid (src/SimParams.cpp:459-462)")
+    P, ctx = _ctx(E, N1, N2, nu=nu, stype=stype)
+    OP = oparams(P)
+    c = _rand_c(N1, N2, 2)
+    x = np.random.default_rng(3).normal(size=(N1, N2))
+    A = np.zeros(N1 * N2 * 9)
+    oracle_lib.or_pressure_matrix(C.byref(OP), O.ptr(cell_ghost(OP, c)), O.ptr(A))
+    y_or = np.zeros(N1 * N2)
+    oracle_lib.or_matvec9(C.byref(OP), O.ptr(A), O.ptr(x.ravel().copy()), O.ptr(y_or))
+    import torch
+    y = torch.zeros((N1, N2), dtype=torch.float64, device="cuda")
+    ctx.pressure_apply(dev(c), dev(x), y)
+    scale = np.abs(A.reshape(-1, 9)).sum(1).max() * np.abs(x).max()
+    assert np.abs(host(y).ravel() - y_or).max() <= 1e-13 * scale
+
+
+def _oracle_pressure(oracle_lib, OP, c, q):
+    p = np.zeros(O.scalar_shape(OP))
+    its, rr = C.c_int(), C.c_double()
+    rc = oracle_lib.or_pressure_solve(C.byref(OP), O.ptr(cell_ghost(OP, c)), O.ptr(q), O.ptr(p), 0, 1e-14,
+                                      C.byref(its), C.byref(rr))
+    assert rc == 0
+    return O.interior(OP, p).copy()
+
+
+@pytest.mark.parametrize("N1,N2", GRIDS + [(141, 141), (100, 50)])
+@pytest.mark.parametrize("nu", [1.0, 2.0 / 3.0])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_pressure_solve(engine, oracle_lib, N1, N2, nu, prec):
+    E = engine
+    stype = 0 if N1 == N2 == 141 else 1
+    P, ctx = _ctx(E, N1, N2, nu=nu, stype=stype, precision=prec, max_cycles=200)
+    OP = oparams(P)
+    c = _rand_c(N1, N2, 4)
+    q = source(OP)
+    ctx.set_source(dev(q))
+    import torch
+    p = torch.zeros((N1, N2), dtype=torch.float64, device="cuda")
+    tol = 1e-12
+    cyc, rr, _ = ctx.pressure_solve(dev(c), p, tol)
+    assert rr <= tol and cyc < 200
+    # relative residual of the device solution under the oracle's (reference) pinned matrix
+    A = np.zeros(N1 * N2 * 9)
+    b = np.zeros(N1 * N2)
+    oracle_lib.or_pressure_matrix(C.byref(OP), O.ptr(cell_ghost(OP, c)), O.ptr(A))
+    oracle_lib.or_pressure_rhs(C.byref(OP), O.ptr(q), O.ptr(b))
+    ph = host(p).ravel().copy()
+    rr_or = oracle_lib.or_relres9(C.byref(OP), O.ptr(A), O.ptr(ph), O.ptr(b))
+    assert rr_or <= 2 * tol
+    # agreement with the direct solve: kappa(A) ~ 1e5 at these sizes
+    p_or = _oracle_pressure(oracle_lib, OP, c, q)
+    assert rel_err(host(p), p_or) <= 1e-6
+
+
+@pytest.mark.parametrize("N1,N2", GRIDS)
+@pytest.mark.parametrize("nu", [1.0, 2.0 / 3.0])
+def test_velocity(engine, oracle_lib, N1, N2, nu):
+    E = engine
+    P, ctx = _ctx(E, N1, N2, nu=nu)
+    OP = oparams(P)
+    c = _rand_c(N1, N2, 5)
+    p = smooth_field(N1, N2, 6, -3.0, 2.0)
+    pg = cell_ghost(OP, p)
+    v = np.zeros(O.vel_shape(OP))
+    oracle_lib.or_calc_velocities(C.byref(OP), O.ptr(pg), O.ptr(v), O.ptr(cell_ghost(OP, c)))
+    u_or, v_or = vel_split(OP, v)
+    import torch
+    du = torch.zeros((N1 + 1, N2), dtype=torch.float64, device="cuda")
+    dv = torch.zeros((N1, N2 + 1), dtype=torch.float64, device="cuda")
+    ctx.velocity(dev(p), dev(c), du, dv)
+    scale = max(np.abs(u_or).max(), np.abs(v_or).max())
+    assert np.abs(host(du) - u_or).max() <= 1e-13 * scale
+    assert np.abs(host(dv) - v_or).max() <= 1e-13 * scale
+    dt_or = oracle_lib.or_max_stable_dt(C.byref(OP), O.ptr(v))
+    dt = ctx.max_stable_dt(dev(u_or), dev(v_or))
+    assert dt == pytest.approx(dt_or, rel=1e-14)
+
+
+def _vel_field(OP, seed):
+    """A consistent velocity field: oracle Darcy velocities of a smooth pressure."""
+    c = _rand_c(OP.N1, OP.N2, seed)
+    p = smooth_field(OP.N1, OP.N2, seed + 1, -1.0, 1.0) * 0.05
+    v = np.zeros(O.vel_shape(OP))
+    O.lib().or_calc_velocities(C.byref(OP), O.ptr(cell_ghost(OP, p)), O.ptr(v), O.ptr(cell_ghost(OP, c)))
+    return v
+
+
+@pytest.mark.parametrize("N1,N2", GRIDS)
+@pytest.mark.parametrize("scheme", [4, 0])
+@pytest.mark.parametrize("mode", [4, 0, 1, 2, 3])
+def test_advect_split(engine, oracle_lib, N1, N2, scheme, mode):
+    E = engine
+    P, ctx = _ctx(E, N1, N2, hmtype=scheme, dim_splitting=mode, porosity=0.7)
+    OP = oparams(P)
+    vg = _vel_field(OP, 7)
+    u, v = vel_split(OP, vg)
+    c = _rand_c(N1, N2, 8)
+    cg = cell_ghost(OP, c)
+    dt = 0.9 * oracle_lib.or_max_stable_advection_dt(C.byref(OP), O.ptr(vg)) * OP.porosity
+    for pfs0 in (0, 1):
+        cg2 = cg.copy()
+        pfs = C.c_int(pfs0)
+        oracle_lib.or_advect_split(C.byref(OP), O.ptr(cg2), O.ptr(vg), dt, C.byref(pfs))
+        dc = dev(c)
+        pfs_dev = ctx.advect_split(dc, dev(u), dev(v), dt, pfs0)
+        assert pfs_dev == pfs.value
+        assert rel_err(host(dc), O.interior(OP, cg2)) <= 1e-13
+
+
+@pytest.mark.parametrize("scheme", [4, 0])
+def test_advect_periodic(engine, oracle_lib, scheme):
+    """Periodic advection test setup of src/Impec2DSolver.cpp:848-1015 (constant velocity)."""
+    E = engine
+    N = 40
+    P, ctx = _ctx(E, N, N, hmtype=scheme, bc=1, is_test=1, cfl=0.95)
+    OP = oparams(P)
+    vg = np.zeros(O.vel_shape(OP))
+    vg[..., 0], vg[..., 1] = -1.0, 1.0
+    u, v = vel_split(OP, vg)
+    c = np.array([[oracle_lib.or_profile(C.byref(OP), 0, (i + .5) / N, (j + .5) / N) for j in range(N)]
+                  for i in range(N)])
+    cg = cell_ghost(OP, c, periodic=True)
+    dt = oracle_lib.or_max_stable_advection_dt(C.byref(OP), O.ptr(vg))
+    pfs = C.c_int(1)
+    oracle_lib.or_advect_split(C.byref(OP), O.ptr(cg), O.ptr(vg), dt, C.byref(pfs))
+    dc = dev(c)
+    ctx.advect_split(dc, dev(u), dev(v), dt, 1)
+    assert rel_err(host(dc), O.interior(OP, cg)) <= 1e-13
+
+
+@pytest.mark.parametrize("N1,N2", GRIDS)
+@pytest.mark.parametrize("stype", [1, 0])
+def test_tr_integrate(engine, oracle_lib, N1, N2, stype):
+    E = engine
+    if stype == 0 and N1 != N2:
+        pytest.skip("parallel configuration requires a square grid")
+    P, ctx = _ctx(E, N1, N2, stype=stype)
+    OP = oparams(P)
+    q = source(OP)
+    ctx.set_source(dev(q))
+    c = _rand_c(N1, N2, 9)
+    cg = cell_ghost(OP, c)
+    dt = 1e-4
+    tmo_or = oracle_lib.or_tr_integrate(C.byref(OP), O.ptr(cg), O.ptr(q), dt)
+    dc = dev(c)
+    tmo = ctx.tr_integrate(dc, dt)
+    assert rel_err(host(dc), O.interior(OP, cg)) <= 1e-15
+    assert tmo == pytest.approx(tmo_or, rel=1e-13, abs=1e-300)
+
+
+@pytest.mark.parametrize("N1,N2", GRIDS)
+@pytest.mark.parametrize("alpha", [(1e-3, 1e-4), (1.0, 0.1)])
+def test_dispersion_cn(engine, oracle_lib, N1, N2, alpha):
+    E = engine
+    P, ctx = _ctx(E, N1, N2, diffusion=1, alpha_l=alpha[0], alpha_t=alpha[1], para_eps=1e-13, max_cycles=400)
+    OP = oparams(P)
+    vg = _vel_field(OP, 10)
+    u, v = vel_split(OP, vg)
+    c = _rand_c(N1, N2, 11)
+    cg = cell_ghost(OP, c)
+    dt = 0.5 * oracle_lib.or_max_stable_dt(C.byref(OP), O.ptr(vg))
+    its, rr = C.c_int(), C.c_double()
+    assert oracle_lib.or_cn_solve(C.byref(OP), O.ptr(cg), O.ptr(vg), dt, 0, 1e-14, C.byref(its), C.byref(rr)) == 0
+    dc = dev(c)
+    its_d, rr_d = ctx.dispersion_cn(dc, dev(u), dev(v), dt, 1e-13)
+    assert rr_d <= 1e-13
+    assert rel_err(host(dc), O.interior(OP, cg)) <= 1e-11
+
+
+@pytest.mark.parametrize("cfg", ["diag_upwind", "par_muscl_disp", "diag_muscl_disp_nu"])
+def test_impes_steps_short_horizon(engine, oracle_lib, cfg):
+    """Whole IMPES steps (pressure, velocity, dt, split transport) against the oracle over a
+    short horizon, before the physical instability amplifies differences."""
+    E = engine
+    N = 48
+    kw = dict(diag_upwind=dict(stype=1, hmtype=0, nu=1.0),
+              par_muscl_disp=dict(stype=0, hmtype=4, nu=1.0, diffusion=1, alpha_l=1e-3, alpha_t=1e-4),
+              diag_muscl_disp_nu=dict(stype=1, hmtype=4, nu=2.0 / 3.0, diffusion=1, alpha_l=1.0, alpha_t=0.1))[cfg]
+    P, ctx = _ctx(E, N, N, eps=1e-13, para_eps=1e-13, max_cycles=200, **kw)
+    OP = oparams(P)
+    q = source(OP)
+    c0 = np.zeros((N, N))
+    cptr, pptr, uptr, vptr, qptr = ctx.state_ptrs()
+    ctx.upload(cell_ghost(OP, c0), q, ghost=2)
+    c = cell_ghost(OP, c0)
+    p = np.zeros(O.scalar_shape(OP))
+    vv = np.zeros(O.vel_shape(OP))
+    S = O.State()
+    S.prev_first_sweep = 1
+    tidx = C.c_int(0)
+    for k in range(10):
+        oracle_lib.or_impes_step(C.byref(OP), C.byref(S), O.ptr(c), O.ptr(p), O.ptr(vv), O.ptr(q), None, 0,
+                                 C.byref(tidx), 0, 1e-14)
+        info = ctx.step()
+        assert info.dt == pytest.approx(S.dt, rel=1e-9)
+    ch, ph, vh = np.zeros_like(c), np.zeros_like(p), np.zeros_like(vv)
+    ctx.download(ch, ph, vh, ghost=2)
+    assert rel_err(O.interior(OP, ch), O.interior(OP, c)) <= 1e-9
+    assert rel_err(O.interior(OP, ph), O.interior(OP, p)) <= 1e-8
+    assert info.mass_err < 1e-12
+
+
+def test_large_grid_properties(engine, oracle_lib):
+    """1024^2 parallel configuration: size-independent invariants (mass balance, no-flow,
+    div u = q) and solver convergence to 1e-10 in both precisions."""
+    E = engine
+    N = 1024
+    for prec in (0, 1):
+        P = E.default_params(N, N, stype=0, x_ub=2 ** 0.5, y_ub=2 ** 0.5, hmtype=4, diffusion=1, alpha_l=1e-3,
+                             alpha_t=1e-4, Dm=1e-6, eps=1e-10, para_eps=1e-10, precision=prec)
+        ctx = E.Context(P)
+        OP = oparams(P)
+        q = source(OP)
+        ctx.upload(cell_ghost(OP, np.zeros((N, N))), q, ghost=2)
+        for k in range(3):
+            info = ctx.step()
+            assert info.relres <= 1e-10
+        cptr, pptr, uptr, vptr, _ = ctx.state_ptrs()
+        import torch
+        c = torch.empty((N, N), dtype=torch.float64, device="cuda")
+        u = torch.empty((N + 1, N), dtype=torch.float64, device="cuda")
+        v = torch.empty((N, N + 1), dtype=torch.float64, device="cuda")
+        ch = np.zeros(O.scalar_shape(OP))
+        vh = np.zeros(O.vel_shape(OP))
+        ctx.download(ch, None, vh, ghost=2)
+        uh, vvh = vel_split(OP, vh)
+        c.copy_(dev(O.interior(OP, ch)))
+        u.copy_(dev(uh))
+        v.copy_(dev(vvh))
+        mass, div_err, vel_err, cmax, cmin = ctx.diagnostics(c, u, v)
+        assert info.mass_err < 1e-11
+        assert vel_err < 1e-9 * np.abs(uh).max()
+        assert div_err < 1e-6
+        ctx.close()

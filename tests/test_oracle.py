@@ -1,0 +1,186 @@
+"""CPU checks of the oracle against the reference's own known answers, plus the equivalences
+the CUDA kernels are built on (ghost fills == index reflection; pinned system == consistent
+singular Neumann system + constant shift)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import cell_ghost, smooth_field, source, vel_split
+
+
+def _advection_error(L, N, vel, profile=0, cfl=0.95):
+    """TestAdvection / Advection (src/Impec2DSolver.cpp:773-990) for one resolution."""
+    P = O.make_params(N1=N, N2=N, is_test=1, cfl=cfl, hmtype=O.MUSCL, dim_splitting=O.SYMMETRIC_PARALLEL)
+    c = np.zeros(O.scalar_shape(P))
+    v = np.zeros(O.vel_shape(P))
+    for i in range(N):
+        for j in range(N):
+            c[i + 2, j + 2] = L.or_profile(C.byref(P), profile, (i + .5) / N, (j + .5) / N)
+    v[..., 0], v[..., 1] = vel
+    q = np.zeros(N * N)
+    dtmax = L.or_max_stable_advection_dt(C.byref(P), O.ptr(v))
+    t, tfinal, tidx, dt = 0.0, 1.0, 0, dtmax
+    pfs, out = C.c_int(1), C.c_double(0)
+    while t < tfinal:
+        if tidx < 1 and t + dt >= tfinal:
+            dt = tfinal - t
+            tidx += 1
+        else:
+            dt = dtmax
+        L.or_hyperbolic_solve(C.byref(P), O.ptr(c), O.ptr(v), O.ptr(q), dt, C.byref(pfs), C.byref(out), 0)
+        t += dt
+    return L.or_advection_norm(C.byref(P), O.ptr(c), profile, 1)
+
+
+def test_advection_convergence_order_known_answer(oracle_lib):
+    """examples/hyperbolic_test.cfg:129-139 documents order 1.87621 for MUSCL (van Leer), sine
+    profile, L1 norm, CFL 0.95, 50^2 doubled over 4 levels.  The shipped code advects with the
+    diagonal velocity (-L, L) (src/Impec2DSolver.cpp:1003-1015); the fitted slope (least squares of
+    log err vs log dx, as GnuPlotter::PlotConvergence does) must match within 0.05."""
+    Ns = [50, 100, 200, 400]
+    errs = [_advection_error(oracle_lib, N, (-1.0, 1.0)) for N in Ns]
+    order = np.polyfit(np.log([1.0 / N for N in Ns]), np.log(errs), 1)[0]
+    assert abs(order - 1.87621) < 0.05, order
+
+
+@pytest.mark.parametrize("testno", [1, 4])
+@pytest.mark.parametrize("nu", [1.0, 2.0 / 3.0])
+def test_elliptic_manufactured_second_order(oracle_lib, testno, nu):
+    """EllipticSolver::TestNeumann (src/EllipticSolver.cpp:155-311) with examples/elliptic_test.cfg
+    settings (20x30 doubled, mu_res 1, mean_concentration): the L1 pressure error converges at order 2."""
+    errs = []
+    for k in range(4):
+        P = O.make_params(N1=20 * 2 ** k, N2=30 * 2 ** k, x_ub=2 * np.pi, y_ub=2 * np.pi, is_test=1, testno=testno,
+                          mu_res=1.0, mu_inj=1.0, avgproc=O.MEANCONC, nu=nu)
+        e = np.zeros(3)
+        assert oracle_lib.or_elliptic_test(C.byref(P), O.ptr(e)) == 0
+        errs.append(e[0])
+    orders = -np.diff(np.log(errs)) / np.log(2)
+    assert np.all(np.abs(orders[1:] - 2.0) < 0.1), orders
+
+
+def test_ghost_fills_are_index_reflections(oracle_lib):
+    """The kernels replace FillGhostCellsNeumannScalar/Velocity (src/Util.cpp:283-438) by index
+    reflection: scalars even about the boundary face, the normal velocity component odd."""
+    N1, N2, g = 7, 5, 2
+    P = O.make_params(N1=N1, N2=N2)
+    rng = np.random.default_rng(0)
+    a = O.with_ghosts(P, rng.normal(size=(N1, N2)))
+
+    def rc(i, n):
+        return -1 - i if i < 0 else (2 * n - 1 - i if i >= n else i)
+
+    for i in range(-g, N1 + g):
+        for j in range(-g, N2 + g):
+            assert a[i + g, j + g] == a[rc(i, N1) + g, rc(j, N2) + g]
+    v = np.zeros(O.vel_shape(P))
+    v[g:g + N1 + 1, g:g + N2, 0] = rng.normal(size=(N1 + 1, N2))
+    v[g:g + N1, g:g + N2 + 1, 1] = rng.normal(size=(N1, N2 + 1))
+    oracle_lib.or_fill_velocity_neumann(C.byref(P), O.ptr(v))
+
+    def rf(f, n):
+        return (-f, -1.0) if f < 0 else ((2 * n - f, -1.0) if f > n else (f, 1.0))
+
+    for i in range(-g, N1 + g + 1):  # u: faces in x (odd), cells in y (even)
+        for j in range(-g, N2 + g):
+            fi, s = rf(i, N1)
+            assert v[i + g, j + g, 0] == s * v[fi + g, rc(j, N2) + g, 0]
+    for i in range(-g, N1 + g):  # v: cells in x (even), faces in y (odd)
+        for j in range(-g, N2 + g + 1):
+            fj, s = rf(j, N2)
+            assert v[i + g, j + g, 1] == s * v[rc(i, N1) + g, fj + g, 1]
+
+
+def test_x_sweep_keeps_ghost_rows_mirrored(oracle_lib):
+    """Advect_X also updates ghost rows (src/HyperbolicSplitSolver.cpp:128-131); they stay exact
+    mirror images of interior rows, which lets the Y sweep read them by reflection."""
+    N1, N2, g = 12, 9, 2
+    P = O.make_params(N1=N1, N2=N2, hmtype=O.MUSCL)
+    c = O.with_ghosts(P, smooth_field(N1, N2, 1))
+    v = np.zeros(O.vel_shape(P))
+    v[g:g + N1 + 1, g:g + N2, 0] = smooth_field(N1 + 1, N2, 2, -1, 1)
+    v[g:g + N1, g:g + N2 + 1, 1] = smooth_field(N1, N2 + 1, 3, -1, 1)
+    oracle_lib.or_fill_velocity_neumann(C.byref(P), O.ptr(v))
+    oracle_lib.or_advect_x(C.byref(P), O.ptr(c), O.ptr(v), 0.01)
+    for i in range(N1):
+        assert c[i + g, g - 1] == c[i + g, g]
+        assert c[i + g, g - 2] == c[i + g, g + 1]
+        assert c[i + g, g + N2] == c[i + g, g + N2 - 1]
+        assert c[i + g, g + N2 + 1] == c[i + g, g + N2 - 2]
+
+
+@pytest.mark.parametrize("nu", [1.0, 2.0 / 3.0])
+@pytest.mark.parametrize("N1,N2", [(24, 24), (19, 27)])
+def test_pinned_system_equals_shifted_neumann(oracle_lib, nu, N1, N2):
+    """The reference's pinned system (src/MGSolver.cpp:518-567) and the consistent singular
+    Neumann system + constant shift (the engine's formulation) have the same solution."""
+    P = O.make_params(N1=N1, N2=N2, nu=nu)
+    c = O.with_ghosts(P, smooth_field(N1, N2, 4))
+    q = source(P)
+    A = np.zeros(N1 * N2 * 9)
+    b = np.zeros(N1 * N2)
+    oracle_lib.or_pressure_matrix(C.byref(P), O.ptr(c), O.ptr(A))
+    oracle_lib.or_pressure_rhs(C.byref(P), O.ptr(q), O.ptr(b))
+    x_lu = np.zeros(N1 * N2)
+    assert oracle_lib.or_solve_banded(C.byref(P), O.ptr(A), O.ptr(b), O.ptr(x_lu)) == 0
+    An = np.zeros(N1 * N2 * 9)
+    oracle_lib.or_pressure_matrix_neumann(C.byref(P), O.ptr(c), O.ptr(An))
+    assert np.abs(An.reshape(-1, 9).sum(1)).max() < 1e-10 * np.abs(An).max()  # zero row sums
+    pin = N2 + 1
+    x = np.zeros(N1 * N2)
+    cyc, rr = C.c_int(), C.c_double()
+    pin_value = b[pin] / A[pin * 9]
+    assert oracle_lib.or_mg_solve(C.byref(P), O.ptr(An), O.ptr(b), O.ptr(x), 1e-13, 200, C.byref(cyc), C.byref(rr), 1,
+                                  1, pin_value) == 0
+    assert oracle_lib.or_relres9(C.byref(P), O.ptr(A), O.ptr(x), O.ptr(b)) < 1e-12
+    assert np.abs(x - x_lu).max() <= 1e-9 * np.abs(x_lu).max()
+
+
+@pytest.mark.parametrize("stype,nu,diff,hm", [(O.DIAGONAL, 1.0, 0, O.UPWINDSPLIT), (O.PARALLEL, 2 / 3, 1, O.MUSCL)])
+def test_impes_mass_balance_and_invariants(oracle_lib, stype, nu, diff, hm):
+    """Runtime invariants printed by the reference (src/Impec2DSolver.cpp:530-588): mass balance,
+    no-flow boundary and div u = q, over 15 IMPES steps at porosity 1."""
+    N = 32
+    P = O.make_params(N1=N, N2=N, stype=stype, nu=nu, diffusion=diff, hmtype=hm, alpha_l=1.0, alpha_t=0.1)
+    q = source(P)
+    c, p, v = np.zeros(O.scalar_shape(P)), np.zeros(O.scalar_shape(P)), np.zeros(O.vel_shape(P))
+    S = O.State()
+    S.prev_first_sweep = 1
+    tidx = C.c_int(0)
+    for _ in range(15):
+        assert oracle_lib.or_impes_step(C.byref(P), C.byref(S), O.ptr(c), O.ptr(p), O.ptr(v), O.ptr(q), None, 0,
+                                        C.byref(tidx), 0, 1e-13) == 0
+        assert S.mass_err < 1e-13
+        assert S.div_err < 1e-9
+        assert S.vel_err < 1e-12
+
+
+def test_porosity_cfl_quirk_documented(oracle_lib):
+    """The reference's dt (src/HyperbolicSolver.cpp:123-198) ignores porosity while the flux divides
+    by it (:208-210): with porosity 0.2 and CFL 0.5 the explicit transport is unstable.  The engine
+    therefore offers cfl_porosity (dt scaled by porosity); this test records the quirk."""
+    N = 32
+    P = O.make_params(N1=N, N2=N, porosity=0.2, hmtype=O.UPWINDSPLIT, nu=1.0)
+    q = source(P)
+    c, p, v = np.zeros(O.scalar_shape(P)), np.zeros(O.scalar_shape(P)), np.zeros(O.vel_shape(P))
+    S = O.State()
+    S.prev_first_sweep = 1
+    tidx = C.c_int(0)
+    for _ in range(40):
+        oracle_lib.or_impes_step(C.byref(P), C.byref(S), O.ptr(c), O.ptr(p), O.ptr(v), O.ptr(q), None, 0,
+                                 C.byref(tidx), 0, 1e-12)
+    cc = O.interior(P, c)
+    assert not np.all(np.isfinite(cc)) or np.abs(cc).max() > 10.0
+
+
+def test_quarter_circle_wells_balance(oracle_lib):
+    """InitQuarterCircle* (src/Util.cpp:508-559): injection and production balance exactly."""
+    for stype in (O.DIAGONAL, O.PARALLEL):
+        P = O.make_params(N1=64, N2=64, stype=stype, well_profile=O.CIRCULAR, well_rc=0.1)
+        q = source(P)
+        assert abs(q.sum()) < 1e-9 * np.abs(q).sum()
+        nwell = 1 if stype == O.DIAGONAL else 2
+        dA = (1.0 / 64) ** 2
+        assert q[q > 0].sum() * dA == pytest.approx(nwell * P.I, rel=1e-12)
