@@ -98,7 +98,43 @@ _SIGS = {
     "impec_cfg_load": (C.c_int, [C.c_char_p, C.POINTER(Params), _PD, _PD]),
     "impec_cfg_source": (C.c_int, [C.c_char_p, _PD]),
     "impec_run_cfg": (C.c_int, [C.c_char_p, C.c_int]),
+    "impec_launch_count": (C.c_int, [_VP, C.POINTER(C.c_longlong)]),
+    "impec_pressure_solve_resident": (C.c_int, [_VP, C.c_int, _PI, _PD]),
+    "impec_time_kernel": (C.c_int, [_VP, C.c_int, C.c_int, _PD, _PD]),
 }
+
+KERNELS = {0: "k_rb_face5<double> (fine RB-GS sweep, FP64)", 1: "k_rb_face5<float> (fine RB-GS sweep, FP32)",
+           2: "k_fine_resid (FP64 residual + norm)", 3: "k_sweep_x (MUSCL x-sweep)", 4: "k_sweep_y (MUSCL y-sweep)"}
+
+
+def launch_count(ctx) -> int:
+    n = C.c_longlong()
+    _chk(lib().impec_launch_count(ctx.h, C.byref(n)), "launch_count")
+    return n.value
+
+
+def time_kernel(ctx, which: int, reps: int = 20):
+    ms, b = C.c_double(), C.c_double()
+    _chk(lib().impec_time_kernel(ctx.h, which, reps, C.byref(ms), C.byref(b)), "time_kernel")
+    return ms.value, b.value
+
+
+def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None):
+    """Achieved bandwidth of the dominant kernel (CUDA events on its stream) against the
+    measured HBM copy bandwidth."""
+    import json
+    which = 1 if precision == "mixed" else 0
+    ms, b = time_kernel(ctx, which)
+    peak, src = 6800.0, "fallback"
+    path = peaks_path or os.path.join(os.path.dirname(HERE), "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            peak, src = float(json.load(open(path))["hbm_gbs"]), "measured"
+        except Exception:  # noqa: BLE001
+            pass
+    ach = b / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": KERNELS[which], "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": ach / peak, "peak_source": src, "bytes_per_launch": b, "ms_per_launch": ms, "traffic": None}
 
 
 def load_cfg(path: str):
@@ -248,6 +284,12 @@ class Context:
         ps = [C.c_void_p() for _ in range(5)]
         _chk(lib().impec_state(self.h, *[C.byref(x) for x in ps]), "state")
         return [x.value for x in ps]
+
+    def pressure_solve_resident(self, sync=True):
+        cyc, rr = C.c_int(), C.c_double()
+        _chk(lib().impec_pressure_solve_resident(self.h, 1 if sync else 0, C.byref(cyc), C.byref(rr)),
+             "pressure_solve_resident")
+        return cyc.value, rr.value
 
     def set_time(self, t0: float):
         _chk(lib().impec_set_time(self.h, t0), "set_time")

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_sum(const double* __restrict__ 
 
 impec_status reduce_launch_sum(impec_ctx* ctx, const double* x, size_t n, double* out_dev) {
     int blocks = ctx->num_sms * 2;
-    k_sum<<<blocks, RED_THREADS, 0, ctx->stream>>>(x, n, ctx->partials, ctx->max_blocks, ctx->counter, out_dev);
+    ++ctx->nlaunch, k_sum<<<blocks, RED_THREADS, 0, ctx->stream>>>(x, n, ctx->partials, ctx->max_blocks, ctx->counter, out_dev);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -175,6 +175,9 @@ impec_status impec_ctx_create(const impec_params* P, void* stream, impec_ctx** o
 impec_status impec_ctx_destroy(impec_ctx* ctx) {
     if (!ctx) return IMPEC_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream); else cudaDeviceSynchronize();
+    invalidate_step_graph(ctx);
+    if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
+    if (ctx->body_stream) cudaStreamDestroy(ctx->body_stream);
     pressure_free(ctx);
     double* bufs[] = {ctx->c, ctx->p, ctx->q, ctx->u, ctx->v, ctx->t1, ctx->t2, ctx->t3, ctx->muK11,
                       ctx->muK22 == ctx->muK11 ? nullptr : ctx->muK22, ctx->lamx, ctx->lamy, ctx->f, ctx->r,
@@ -198,6 +201,7 @@ impec_status impec_ctx_params(const impec_ctx* ctx, impec_params* P) {
 
 impec_status impec_set_permeability(impec_ctx* ctx, const double* K11, const double* K22) {
     if (!ctx) return IMPEC_ERR_ARG;
+    invalidate_step_graph(ctx);
     const size_t n = (size_t)ctx->P.N1 * ctx->P.N2;
     if (ctx->K22 && ctx->K22 != ctx->K11) cudaFree(ctx->K22);
     if (ctx->K11) cudaFree(ctx->K11);
@@ -232,6 +236,7 @@ impec_status impec_set_source(impec_ctx* ctx, const double* q_dev) {
             idx.push_back((int)k);
             val.push_back(hq[k]);
         }
+    invalidate_step_graph(ctx);
     if (ctx->well_idx) cudaFree(ctx->well_idx);
     if (ctx->well_q) cudaFree(ctx->well_q);
     ctx->well_idx = nullptr;

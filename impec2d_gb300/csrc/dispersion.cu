@@ -36,8 +36,8 @@ __global__ void k_peaceman(PeaceArgs A, const double* __restrict__ u, const doub
         double vv = 1. / 4 * (v[IX(im, j + 1, n2 + 1)] + v[IX(i0, j + 1, n2 + 1)] + v[IX(im, j, n2 + 1)] +
                               v[IX(i0, j, n2 + 1)]);
         double u2 = uu * uu, v2 = vv * vv;
-        double nrm = sqrt(u2 + v2);
-        double fl = A.phi * A.al / nrm, ft = A.phi * A.at / nrm;
+        double inv = rsqrt(u2 + v2);  // 1/|u|
+        double fl = A.phi * A.al * inv, ft = A.phi * A.at * inv;
         if (A.guard && u2 + v2 == 0) fl = ft = 0;
         double d11 = fl * u2 + ft * v2;
         double d12 = fl * (uu * vv) + ft * (-uu * vv);
@@ -51,8 +51,8 @@ __global__ void k_peaceman(PeaceArgs A, const double* __restrict__ u, const doub
         double uu = 1. / 4 * (u[IX(i + 1, jm, n2)] + u[IX(i + 1, j0, n2)] + u[IX(i, jm, n2)] + u[IX(i, j0, n2)]);
         double vv = v[IX(i, j, n2 + 1)];
         double u2 = uu * uu, v2 = vv * vv;
-        double nrm = sqrt(u2 + v2);
-        double fl = A.phi * A.al / nrm, ft = A.phi * A.at / nrm;
+        double inv = rsqrt(u2 + v2);
+        double fl = A.phi * A.al * inv, ft = A.phi * A.at * inv;
         if (A.guard && u2 + v2 == 0) fl = ft = 0;
         double d21 = fl * (uu * vv) + ft * (-uu * vv);
         double d22 = fl * v2 + ft * u2;
@@ -65,31 +65,37 @@ __global__ void k_peaceman(PeaceArgs A, const double* __restrict__ u, const doub
 
 struct CNArgs {
     int n1, n2;
-    double dx, dy;
+    // dt-free factors of GetCoefficients_Parabolic / SetRHS_Parabolic
+    double k8xy;   // 1 / (8 dx dy)
+    double k4xx;   // 4 / (dx dx)
+    double k4yy;   // 4 / (dy dy)
+    double kxy;    // 1 / (dx dy)
+    double k2xx;   // 1 / (2 dx dx)
+    double k2yy;   // 1 / (2 dy dy)
 };
 
-// GetCoefficients_Parabolic (src/MGSolver.cpp:923-948), folding (:1031-1289), and
-// SetRHS_Parabolic (:1324-1371).  dt = scale * dt_dev[0].
-__global__ void k_cn_assemble(CNArgs A, const double* __restrict__ dfx, const double* __restrict__ dfy,
-                              const double* __restrict__ c, const double* __restrict__ dt_dev, double scale,
-                              double* __restrict__ a9, double* __restrict__ idiag, double* __restrict__ rhs) {
+// GetCoefficients_Parabolic (src/MGSolver.cpp:923-948) with the Neumann folding of
+// SetMatrixCoefficients_Parabolic (:997-1321).  dt = scale * dt_dev[0].
+__global__ void k_cn_matrix(CNArgs A, const double* __restrict__ dfx, const double* __restrict__ dfy,
+                            const double* __restrict__ dt_dev, double scale, double* __restrict__ a9,
+                            double* __restrict__ idiag) {
     int j = blockIdx.x * DBX + threadIdx.x, i = blockIdx.y * DBY + threadIdx.y;
     const int n1 = A.n1, n2 = A.n2;
     if (i >= n1 || j >= n2) return;
     const double dt = scale * dt_dev[0];
-    const double dx = A.dx, dy = A.dy;
     size_t kx0 = IX(i, j, n2), kx1 = IX(i + 1, j, n2), ky0 = IX(i, j, n2 + 1), ky1 = IX(i, j + 1, n2 + 1);
     double d11_im = dfx[2 * kx0], d12_im = dfx[2 * kx0 + 1], d11_ip = dfx[2 * kx1], d12_ip = dfx[2 * kx1 + 1];
     double d22_jm = dfy[2 * ky0], d21_jm = dfy[2 * ky0 + 1], d22_jp = dfy[2 * ky1], d21_jp = dfy[2 * ky1 + 1];
-    double NW = dt / (8. * dx * dy) * (d12_im + d21_jp);
-    double NE = -dt / (8. * dx * dy) * (d12_ip + d21_jp);
-    double N = -dt / 8. * (4. / (dy * dy) * d22_jp + 1. / (dx * dy) * (-d12_im + d12_ip));
-    double SW = -dt / (8. * dx * dy) * (d12_im + d21_jm);
-    double SE = dt / (8. * dx * dy) * (d12_ip + d21_jm);
-    double S = -dt / 8. * (4. / (dy * dy) * d22_jm + 1. / (dx * dy) * (-d12_ip + d12_im));
-    double W = -dt / 8. * (4. / (dx * dx) * d11_im + 1. / (dx * dy) * (-d21_jp + d21_jm));
-    double C = 1. + dt / (2. * dx * dx) * (d11_ip + d11_im) + dt / (2. * dy * dy) * (d22_jp + d22_jm);
-    double E = -dt / 8. * (4. / (dx * dx) * d11_ip + 1. / (dx * dy) * (-d21_jm + d21_jp));
+    const double e8 = dt * A.k8xy, d8 = dt * 0.125;
+    double NW = e8 * (d12_im + d21_jp);
+    double NE = -e8 * (d12_ip + d21_jp);
+    double N = -d8 * (A.k4yy * d22_jp + A.kxy * (-d12_im + d12_ip));
+    double SW = -e8 * (d12_im + d21_jm);
+    double SE = e8 * (d12_ip + d21_jm);
+    double S = -d8 * (A.k4yy * d22_jm + A.kxy * (-d12_ip + d12_im));
+    double W = -d8 * (A.k4xx * d11_im + A.kxy * (-d21_jp + d21_jm));
+    double C = 1. + dt * A.k2xx * (d11_ip + d11_im) + dt * A.k2yy * (d22_jp + d22_jm);
+    double E = -d8 * (A.k4xx * d11_ip + A.kxy * (-d21_jm + d21_jp));
     double o[9] = {C, W, SW, S, SE, E, NE, N, NW};
     const int k = i, l = j;
     auto set = [&](double a0, double a1, double a2, double a3, double a4, double a5, double a6, double a7, double a8) {
@@ -106,14 +112,29 @@ __global__ void k_cn_assemble(CNArgs A, const double* __restrict__ dfx, const do
     const size_t n = (size_t)n1 * n2, kk = IX(i, j, n2);
     for (int e = 0; e < 9; ++e) a9[e * n + kk] = o[e];
     idiag[kk] = 1.0 / o[0];
-    // right-hand side with mirrored ghost values
-    auto cc = [&](int a, int b) { return c[IX(refl_cell(a, n1), refl_cell(b, n2), n2)]; };
-    rhs[kk] = cc(i, j) + dt / 8. * (4. / (dx * dx) * (d11_ip * (cc(i + 1, j) - cc(i, j)) - d11_im * (cc(i, j) - cc(i - 1, j))) +
-                                    1. / (dx * dy) * (d12_ip * (cc(i, j + 1) + cc(i + 1, j + 1) - cc(i, j - 1) - cc(i + 1, j - 1)) -
-                                                      d12_im * (cc(i, j + 1) + cc(i - 1, j + 1) - cc(i - 1, j - 1) - cc(i, j - 1))) +
-                                    1. / (dx * dy) * (d21_jp * (cc(i + 1, j) + cc(i + 1, j + 1) - cc(i - 1, j + 1) - cc(i - 1, j)) -
-                                                      d21_jm * (cc(i + 1, j) + cc(i + 1, j - 1) - cc(i - 1, j) - cc(i - 1, j - 1))) +
-                                    4. / (dy * dy) * (d22_jp * (cc(i, j + 1) - cc(i, j)) - d22_jm * (cc(i, j) - cc(i, j - 1))));
+}
+
+// SetRHS_Parabolic (src/MGSolver.cpp:1324-1371) with mirrored ghost values of c.
+__global__ void k_cn_rhs(CNArgs A, const double* __restrict__ dfx, const double* __restrict__ dfy,
+                         const double* __restrict__ c, const double* __restrict__ dt_dev, double scale,
+                         double* __restrict__ rhs) {
+    int j = blockIdx.x * DBX + threadIdx.x, i = blockIdx.y * DBY + threadIdx.y;
+    const int n1 = A.n1, n2 = A.n2;
+    if (i >= n1 || j >= n2) return;
+    const double dt = scale * dt_dev[0];
+    size_t kx0 = IX(i, j, n2), kx1 = IX(i + 1, j, n2), ky0 = IX(i, j, n2 + 1), ky1 = IX(i, j + 1, n2 + 1);
+    double d11_im = dfx[2 * kx0], d12_im = dfx[2 * kx0 + 1], d11_ip = dfx[2 * kx1], d12_ip = dfx[2 * kx1 + 1];
+    double d22_jm = dfy[2 * ky0], d21_jm = dfy[2 * ky0 + 1], d22_jp = dfy[2 * ky1], d21_jp = dfy[2 * ky1 + 1];
+    const int im = refl_cell(i - 1, n1), ip = refl_cell(i + 1, n1), jm = refl_cell(j - 1, n2), jp = refl_cell(j + 1, n2);
+    auto cc = [&](int a, int b) { return c[IX(a, b, n2)]; };
+    const double c0 = cc(i, j);
+    double t1 = A.k4xx * (d11_ip * (cc(ip, j) - c0) - d11_im * (c0 - cc(im, j)));
+    double t2 = A.kxy * (d12_ip * (cc(i, jp) + cc(ip, jp) - cc(i, jm) - cc(ip, jm)) -
+                         d12_im * (cc(i, jp) + cc(im, jp) - cc(im, jm) - cc(i, jm)));
+    double t3 = A.kxy * (d21_jp * (cc(ip, j) + cc(ip, jp) - cc(im, jp) - cc(im, j)) -
+                         d21_jm * (cc(ip, j) + cc(ip, jm) - cc(im, j) - cc(im, jm)));
+    double t4 = A.k4yy * (d22_jp * (cc(i, jp) - c0) - d22_jm * (c0 - cc(i, jm)));
+    rhs[IX(i, j, n2)] = c0 + dt * 0.125 * (t1 + t2 + t3 + t4);
 }
 
 __device__ __forceinline__ double cn_off(int i, int j, int n1, int n2, const double* __restrict__ a9,
@@ -136,7 +157,7 @@ __global__ void k_cn_gs(int n1, int n2, const double* __restrict__ a9, const dou
     x[IX(i, j, n2)] = (b[IX(i, j, n2)] - cn_off(i, j, n1, n2, a9, x)) * idiag[IX(i, j, n2)];
 }
 
-// ||b - A x||^2 and ||b||^2
+// ||b - A x||^2 and ||b||^2 into out[0], out[1]
 __global__ void __launch_bounds__(RED_THREADS) k_cn_resid(int n1, int n2, const double* __restrict__ a9,
                                                           const double* __restrict__ b, const double* __restrict__ x,
                                                           double* partials, int mb, unsigned* counter, double* out) {
@@ -151,46 +172,103 @@ __global__ void __launch_bounds__(RED_THREADS) k_cn_resid(int n1, int n2, const 
     grid_reduce<2>(acc, 0u, partials, mb, counter, out);
 }
 
-impec_status dispersion_cn_dev(impec_ctx* ctx, double* c, const double* u, const double* v, double dt_scale,
-                               const double* dt_dev, double tol, int* its, double* relres) {
+__global__ void k_cn_check(DevScalars* S, double tol, int max_its, int inc, cudaGraphConditionalHandle h, int use_h) {
+    if (inc) { S->cn_cycles++; S->cn_cycles_total++; }
+    double bn = S->red[3], rn = S->red[2];
+    double rr = bn > 0 ? sqrt(rn / bn) : sqrt(rn);
+    S->cn_relres = rr;
+    const bool bad = !(rr == rr) || isinf(rr);
+    const bool go = !bad && rr > tol && S->cn_cycles < max_its;
+    if (bad) S->flags |= FLAG_CN_NAN;
+    else if (!go && rr > tol) S->flags |= FLAG_CN_NOT_CONVERGED;
+    S->go = go ? 1 : 0;
+    if (use_h) cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+static CNArgs cn_args(impec_ctx* ctx) {
+    const Geo& G = ctx->G;
+    return CNArgs{ctx->P.N1, ctx->P.N2, 1. / (8. * G.dx * G.dy), 4. / (G.dx * G.dx), 4. / (G.dy * G.dy),
+                  1. / (G.dx * G.dy), 1. / (2. * G.dx * G.dx), 1. / (2. * G.dy * G.dy)};
+}
+
+// Peaceman face tensors and the CN matrix for the half step dt = scale * dt_dev (launch only).
+impec_status cn_setup(impec_ctx* ctx, const double* u, const double* v, double dt_scale, const double* dt_dev) {
     const impec_params& P = ctx->P;
     const int n1 = P.N1, n2 = P.N2;
     const Geo& G = ctx->G;
     const double maxdx = G.dx > G.dy ? G.dx : G.dy;
     PeaceArgs pa{n1, n2, P.porosity, P.alpha_l * maxdx, P.alpha_t * maxdx, P.porosity * P.Dm, P.peaceman_guard};
     dim3 b(DBX, DBY);
+    ++ctx->nlaunch;
     k_peaceman<<<dim3((n2 + 1 + DBX - 1) / DBX, (n1 + 1 + DBY - 1) / DBY), b, 0, ctx->stream>>>(pa, u, v, ctx->dfx,
                                                                                                  ctx->dfy);
+    ++ctx->nlaunch;
+    k_cn_matrix<<<dim3((n2 + DBX - 1) / DBX, (n1 + DBY - 1) / DBY), b, 0, ctx->stream>>>(
+        cn_args(ctx), ctx->dfx, ctx->dfy, dt_dev, dt_scale, ctx->cn_a9, ctx->cn_idiag);
     IMPEC_LAUNCH_CHECK();
-    CNArgs ca{n1, n2, G.dx, G.dy};
-    k_cn_assemble<<<dim3((n2 + DBX - 1) / DBX, (n1 + DBY - 1) / DBY), b, 0, ctx->stream>>>(
-        ca, ctx->dfx, ctx->dfy, c, dt_dev, dt_scale, ctx->cn_a9, ctx->cn_idiag, ctx->cn_b);
+    return IMPEC_OK;
+}
+
+impec_status cn_residual(impec_ctx* ctx, const double* c) {
+    ++ctx->nlaunch;
+    k_cn_resid<<<ctx->num_sms * 2, RED_THREADS, 0, ctx->stream>>>(ctx->P.N1, ctx->P.N2, ctx->cn_a9, ctx->cn_b, c,
+                                                                   ctx->partials, ctx->max_blocks, ctx->counter,
+                                                                   ctx->dscal->red + 2);
     IMPEC_LAUNCH_CHECK();
-    // x starts from c (the reference starts from 0; only the iteration count differs)
-    const int rb = ctx->num_sms * 2;
+    return IMPEC_OK;
+}
+
+// Right-hand side from c, cycle counter reset, initial residual (launch only).
+impec_status cn_prepare(impec_ctx* ctx, const double* c, double dt_scale, const double* dt_dev) {
+    const int n1 = ctx->P.N1, n2 = ctx->P.N2;
+    ++ctx->nlaunch;
+    k_cn_rhs<<<dim3((n2 + DBX - 1) / DBX, (n1 + DBY - 1) / DBY), dim3(DBX, DBY), 0, ctx->stream>>>(
+        cn_args(ctx), ctx->dfx, ctx->dfy, c, dt_dev, dt_scale, ctx->cn_b);
+    IMPEC_LAUNCH_CHECK();
+    IMPEC_CUDA_TRY(cudaMemsetAsync(&ctx->dscal->cn_cycles, 0, sizeof(int), ctx->stream));
+    return cn_residual(ctx, c);
+}
+
+impec_status cn_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h) {
+    ++ctx->nlaunch;
+    k_cn_check<<<1, 1, 0, ctx->stream>>>(ctx->dscal, tol, ctx->P.max_cycles, inc, h, use_h);
+    IMPEC_LAUNCH_CHECK();
+    return IMPEC_OK;
+}
+
+// One four-colour Gauss-Seidel sweep (x starts from c: the reference starts from 0, only the
+// iteration count differs) followed by the new residual (launch only).
+impec_status cn_iteration(impec_ctx* ctx, double* c) {
+    const int n1 = ctx->P.N1, n2 = ctx->P.N2;
     dim3 g4(((n2 + 1) / 2 + DBX - 1) / DBX, ((n1 + 1) / 2 + DBY - 1) / DBY);
-    int k = 0;
-    double rr = 0;
-    impec_status st = IMPEC_OK;
-    for (;;) {
-        k_cn_resid<<<rb, RED_THREADS, 0, ctx->stream>>>(n1, n2, ctx->cn_a9, ctx->cn_b, c, ctx->partials,
-                                                         ctx->max_blocks, ctx->counter, ctx->dscal->red + 2);
-        IMPEC_LAUNCH_CHECK();
-        IMPEC_TRY(sync_scalars(ctx));
-        double bn = ctx->hscal->red[3];
-        rr = bn > 0 ? sqrt(ctx->hscal->red[2] / bn) : sqrt(ctx->hscal->red[2]);
-        if (!std::isfinite(rr)) { st = IMPEC_ERR_NAN; break; }
-        if (rr <= tol) break;
-        if (k >= P.max_cycles) { st = IMPEC_ERR_NOT_CONVERGED; break; }
-        for (int col = 0; col < 4; ++col)
-            k_cn_gs<<<g4, b, 0, ctx->stream>>>(n1, n2, ctx->cn_a9, ctx->cn_idiag, ctx->cn_b, c, col >> 1, col & 1);
-        IMPEC_LAUNCH_CHECK();
-        ++k;
+    for (int col = 0; col < 4; ++col) {
+        ++ctx->nlaunch;
+        k_cn_gs<<<g4, dim3(DBX, DBY), 0, ctx->stream>>>(n1, n2, ctx->cn_a9, ctx->cn_idiag, ctx->cn_b, c, col >> 1,
+                                                       col & 1);
     }
-    if (its) *its = k;
-    if (relres) *relres = rr;
-    ctx->last_para_its = k;
-    return st;
+    IMPEC_LAUNCH_CHECK();
+    return cn_residual(ctx, c);
+}
+
+// Host-driven CN solve of one half step (per-operation entry point).
+impec_status dispersion_cn_dev(impec_ctx* ctx, double* c, const double* u, const double* v, double dt_scale,
+                               const double* dt_dev, double tol, int* its, double* relres) {
+    IMPEC_CUDA_TRY(cudaMemsetAsync(&ctx->dscal->flags, 0, sizeof(int), ctx->stream));
+    IMPEC_TRY(cn_setup(ctx, u, v, dt_scale, dt_dev));
+    IMPEC_TRY(cn_prepare(ctx, c, dt_scale, dt_dev));
+    IMPEC_TRY(cn_check(ctx, tol, 0, 0, 0));
+    for (;;) {
+        IMPEC_TRY(sync_scalars(ctx));
+        if (!ctx->hscal->go) break;
+        IMPEC_TRY(cn_iteration(ctx, c));
+        IMPEC_TRY(cn_check(ctx, tol, 1, 0, 0));
+    }
+    if (its) *its = ctx->hscal->cn_cycles;
+    if (relres) *relres = ctx->hscal->cn_relres;
+    ctx->last_para_its = ctx->hscal->cn_cycles;
+    if (ctx->hscal->flags & FLAG_CN_NAN) return IMPEC_ERR_NAN;
+    if (ctx->hscal->flags & FLAG_CN_NOT_CONVERGED) return IMPEC_ERR_NOT_CONVERGED;
+    return IMPEC_OK;
 }
 
 }  // namespace impec

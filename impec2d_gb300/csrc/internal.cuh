@@ -66,12 +66,16 @@ struct Level {
     float *x32 = nullptr, *b32 = nullptr;
 };
 
+enum { FLAG_MG_NOT_CONVERGED = 1, FLAG_MG_NAN = 2, FLAG_CN_NOT_CONVERGED = 4, FLAG_CN_NAN = 8 };
+
 // Device-resident scalars of a step (so a step needs no host round trip).
 struct DevScalars {
     double dt, t, maxvel, tmo_pre, tmo_post, total_outflux;
     double fsum, fnorm2, rnorm2, pin_value;  // fsum,fnorm2 adjacent: written as a pair
     double red[8];
-    int cycles, flags;
+    double relres, cn_relres, t_clip;
+    int mg_cycles, cn_cycles, cn_cycles_total, flags, go, clipped, steps;
+    long long graph_launches;  // kernels executed by step-graph replays
 };
 
 }  // namespace impec
@@ -114,6 +118,13 @@ struct impec_ctx {
     int counter_steps = 0, prev_first_sweep = 1, last_its = 0, last_para_its = 0;
     double last_relres = 0;
     bool have_source = false;
+    long long nlaunch = 0;                         // kernel launches issued (captured ones included)
+    // resident-step CUDA graph
+    cudaStream_t cap_stream = nullptr, body_stream = nullptr;
+    cudaGraphExec_t step_exec[2] = {nullptr, nullptr};
+    cudaGraphExec_t pressure_exec = nullptr;
+    long long pressure_outer_launches = 0;
+    long long step_outer_launches = 0, step_mg_body_launches = 0, step_cn_body_launches = 0;
 };
 
 namespace impec {
@@ -124,6 +135,11 @@ impec_status pressure_alloc(impec_ctx* ctx);
 void pressure_free(impec_ctx* ctx);
 impec_status face_mobility(impec_ctx* ctx, const double* c);
 impec_status pressure_apply_ref(impec_ctx* ctx, const double* x, double* y);
+impec_status pressure_prepare(impec_ctx* ctx, const double* c, const double* p);
+impec_status pressure_residual(impec_ctx* ctx);
+impec_status pressure_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h);
+impec_status pressure_iteration(impec_ctx* ctx);
+impec_status pressure_finish(impec_ctx* ctx, double* p);
 // elliptic velocity
 impec_status velocity(impec_ctx* ctx, const double* p, const double* c, double* u, double* v);
 impec_status max_stable_dt_dev(impec_ctx* ctx, const double* u, const double* v);
@@ -135,8 +151,16 @@ impec_status advect_y_dev(impec_ctx* ctx, const double* cin, double* cout, const
 impec_status advect_split_dev(impec_ctx* ctx, double* c, const double* u, const double* v, const double* dt_dev, int* pfs);
 impec_status average_dev(impec_ctx* ctx, double* c, const double* a, const double* b);
 // dispersion.cu
+impec_status cn_setup(impec_ctx* ctx, const double* u, const double* v, double dt_scale, const double* dt_dev);
+impec_status cn_prepare(impec_ctx* ctx, const double* c, double dt_scale, const double* dt_dev);
+impec_status cn_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h);
+impec_status cn_iteration(impec_ctx* ctx, double* c);
 impec_status dispersion_cn_dev(impec_ctx* ctx, double* c, const double* u, const double* v, double dt_scale,
                                const double* dt_dev, double tol, int* its, double* relres);
+// graph.cu
+impec_status launch_step_graph(impec_ctx* ctx, double t_clip);
+impec_status launch_pressure_graph(impec_ctx* ctx);
+void invalidate_step_graph(impec_ctx* ctx);
 // step.cu
 impec_status hyperbolic_solve_dev(impec_ctx* ctx, double* c, const double* u, const double* v, const double* dt_dev,
                                   int* pfs);

@@ -472,6 +472,10 @@ __global__ void k_apply_ref(Level F, const double* __restrict__ x, int pin, doub
     y[k] = -v / dA;
 }
 
+#include "mgfused.cuh"
+
+constexpr size_t MG_COARSE_SMEM = 160 * 1024;
+
 // ---------------------------------------------------------------- host orchestration
 static int red_blocks(impec_ctx* ctx) { return ctx->num_sms * 2 < ctx->max_blocks ? ctx->num_sms * 2 : ctx->max_blocks; }
 
@@ -515,6 +519,15 @@ impec_status pressure_alloc(impec_ctx* ctx) {
     ctx->dense_n = ctx->L.back().n1 * ctx->L.back().n2;
     IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dense_inv, (size_t)ctx->dense_n * ctx->dense_n * 8 * 2));
     IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_dense_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 64 * 8));
+    const int cs = (int)MG_COARSE_SMEM;
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_coarse_vcycle<double, FACE5>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs));
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_coarse_vcycle<double, EXP9>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs));
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_coarse_vcycle<float, FACE5>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs));
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_coarse_vcycle<float, EXP9>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs));
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_pre<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<double, TBH_PRE>()));
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_post<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<double, TBH_POST>()));
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_pre<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<float, TBH_PRE>()));
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_post<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<float, TBH_POST>()));
     return IMPEC_OK;
 }
 
@@ -535,15 +548,15 @@ impec_status face_mobility(impec_ctx* ctx, const double* c) {
     const int n1 = P.N1, n2 = P.N2;
     const int harm = P.avgproc == IMPEC_HARMONIC;
     double* w2 = ctx->K22 ? ctx->muK22 : nullptr;
-    k_cell_w<<<grid2(n1, n2), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, c, ctx->K11, ctx->K22, ctx->G.mob1over4,
+    ++ctx->nlaunch, k_cell_w<<<grid2(n1, n2), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, c, ctx->K11, ctx->K22, ctx->G.mob1over4,
                                                                P.mu_res, harm, ctx->muK11, w2);
     IMPEC_LAUNCH_CHECK();
     const double* W2 = w2 ? w2 : ctx->muK11;
-    k_face_lam<<<grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, ctx->muK11, W2, harm, ctx->lamx,
+    ++ctx->nlaunch, k_face_lam<<<grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, ctx->muK11, W2, harm, ctx->lamx,
                                                                           ctx->lamy);
     IMPEC_LAUNCH_CHECK();
     if (P.nu < 1.0) {
-        k_corner<<<grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, ctx->muK11, W2, harm, ctx->G,
+        ++ctx->nlaunch, k_corner<<<grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, ctx->muK11, W2, harm, ctx->G,
                                                                             ctx->cm11, ctx->cm22, ctx->cm12);
         IMPEC_LAUNCH_CHECK();
     }
@@ -557,44 +570,44 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
     const Geo& G = ctx->G;
     if (F.kind == FACE5) {
         double sx = G.dA * (1. / (G.dx * G.dx)), sy = G.dA * (1. / (G.dy * G.dy));
-        k_face5_fine<<<grid2(F.n1 + 1, F.n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, ctx->lamx, ctx->lamy,
+        ++ctx->nlaunch, k_face5_fine<<<grid2(F.n1 + 1, F.n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, ctx->lamx, ctx->lamy,
                                                                                   sx, sy, F.tx, F.ty);
     } else {
-        k_exp9_fine<<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, ctx->lamx, ctx->lamy, ctx->cm11,
+        ++ctx->nlaunch, k_exp9_fine<<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, ctx->lamx, ctx->lamy, ctx->cm11,
                                                                          ctx->cm22, ctx->cm12, P.nu, G, F.a9);
     }
     IMPEC_LAUNCH_CHECK();
     for (size_t l = 0; l + 1 < ctx->L.size(); ++l) {
         Level &A = ctx->L[l], &B = ctx->L[l + 1];
         if (A.kind == FACE5)
-            k_face5_coarsen<<<grid2(B.n1 + 1, B.n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(A.n1, A.n2, A.tx, A.ty, B.n1,
+            ++ctx->nlaunch, k_face5_coarsen<<<grid2(B.n1 + 1, B.n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(A.n1, A.n2, A.tx, A.ty, B.n1,
                                                                                         B.n2, B.tx, B.ty);
         else
-            k_exp9_coarsen<<<grid2(B.n1, B.n2), dim3(BX, BY), 0, ctx->stream>>>(A.n1, A.n2, A.a9, B.n1, B.n2, B.a9);
+            ++ctx->nlaunch, k_exp9_coarsen<<<grid2(B.n1, B.n2), dim3(BX, BY), 0, ctx->stream>>>(A.n1, A.n2, A.a9, B.n1, B.n2, B.a9);
         IMPEC_LAUNCH_CHECK();
     }
     const bool mixed = P.precision == IMPEC_PREC_MIXED;
     for (Level& Lv : ctx->L) {
-        k_idiag<<<grid2(Lv.n1, Lv.n2), dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, Lv.kind, Lv.tx, Lv.ty, Lv.a9,
+        ++ctx->nlaunch, k_idiag<<<grid2(Lv.n1, Lv.n2), dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, Lv.kind, Lv.tx, Lv.ty, Lv.a9,
                                                                         Lv.idiag);
         IMPEC_LAUNCH_CHECK();
         if (mixed) {
             const size_t n = Lv.n();
             int nb = ctx->num_sms * 4;
-            k_to_float<<<nb, 256, 0, ctx->stream>>>(n, Lv.idiag, Lv.idiag32);
+            ++ctx->nlaunch, k_to_float<<<nb, 256, 0, ctx->stream>>>(n, Lv.idiag, Lv.idiag32);
             if (Lv.kind == FACE5) {
-                k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)(Lv.n1 + 1) * Lv.n2, Lv.tx, Lv.tx32);
-                k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)Lv.n1 * (Lv.n2 + 1), Lv.ty, Lv.ty32);
+                ++ctx->nlaunch, k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)(Lv.n1 + 1) * Lv.n2, Lv.tx, Lv.tx32);
+                ++ctx->nlaunch, k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)Lv.n1 * (Lv.n2 + 1), Lv.ty, Lv.ty32);
             } else {
-                k_to_float<<<nb, 256, 0, ctx->stream>>>(n * 9, Lv.a9, Lv.a932);
+                ++ctx->nlaunch, k_to_float<<<nb, 256, 0, ctx->stream>>>(n * 9, Lv.a9, Lv.a932);
             }
             IMPEC_LAUNCH_CHECK();
         }
     }
     Level& C = ctx->L.back();
-    k_dense_build<<<1, 256, 0, ctx->stream>>>(C, C.tx, C.ty, C.a9, 1, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n);
+    ++ctx->nlaunch, k_dense_build<<<1, 256, 0, ctx->stream>>>(C, C.tx, C.ty, C.a9, 1, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n);
     IMPEC_LAUNCH_CHECK();
-    k_dense_invert<<<1, 256, 2 * ctx->dense_n * ctx->dense_n * 8, ctx->stream>>>(
+    ++ctx->nlaunch, k_dense_invert<<<1, 256, 2 * ctx->dense_n * ctx->dense_n * 8, ctx->stream>>>(
         ctx->dense_n, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n, ctx->dense_inv);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
@@ -622,15 +635,76 @@ static void smooth(impec_ctx* ctx, Level& Lv, int sweeps, bool reverse) {
         if (Lv.kind == FACE5) {
             dim3 g((Lv.n2 / 2 + 1 + BX - 1) / BX, (Lv.n1 + BY - 1) / BY);
             for (int cc = 0; cc < 2; ++cc)
-                k_rb_face5<T><<<g, dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, tx, ty, id, b, x, reverse ? 1 - cc : cc);
+                ++ctx->nlaunch, k_rb_face5<T><<<g, dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, tx, ty, id, b, x, reverse ? 1 - cc : cc);
         } else {
             dim3 g(((Lv.n2 + 1) / 2 + BX - 1) / BX, ((Lv.n1 + 1) / 2 + BY - 1) / BY);
             for (int cc = 0; cc < 4; ++cc) {
                 int col = reverse ? 3 - cc : cc;
-                k_gs4_exp9<T><<<g, dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, a9, id, b, x, col >> 1, col & 1);
+                ++ctx->nlaunch, k_gs4_exp9<T><<<g, dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, a9, id, b, x, col >> 1, col & 1);
             }
         }
     }
+}
+
+// Shared-memory bytes the coarse CTA needs for levels l .. L-1.
+template <class T>
+static size_t coarse_bytes(const impec_ctx* ctx, size_t l) {
+    size_t b = 0;
+    for (size_t k = l; k < ctx->L.size(); ++k) {
+        const Level& Lv = ctx->L[k];
+        const size_t n = Lv.n();
+        b += Lv.kind == FACE5 ? (size_t)(Lv.n1 + 1) * Lv.n2 + (size_t)Lv.n1 * (Lv.n2 + 1) + 3 * n : 12 * n;
+    }
+    return b * sizeof(T);
+}
+
+static long env_long(const char* name, long dflt) {
+    const char* e = getenv(name);
+    return e && *e ? strtol(e, nullptr, 10) : dflt;
+}
+
+// First level handled by the single-CTA coarse V-cycle: the largest level whose cell count is
+// within the precision's limit (FP64 work on one SM is slow, FP32 is 57x faster per SM).
+template <class T>
+static size_t coarse_start(const impec_ctx* ctx) {
+    const size_t cells = (size_t)(sizeof(T) == 8 ? env_long("IMPEC_MG_COARSE_CELLS64", 256)
+                                                 : env_long("IMPEC_MG_COARSE_CELLS32", 4096));
+    for (size_t l = 0; l < ctx->L.size(); ++l)
+        if (ctx->L[l].n() <= cells && coarse_bytes<T>(ctx, l) <= MG_COARSE_SMEM) return l;
+    return ctx->L.size() - 1;
+}
+
+template <class T>
+static void launch_coarse(impec_ctx* ctx, size_t lc) {
+    CoarseArgs<T> A{};
+    A.nl = (int)(ctx->L.size() - lc);
+    A.singular = 1;
+    A.dn = ctx->dense_n;
+    A.dinv = ctx->dense_inv;
+    for (int k = 0; k < A.nl; ++k) {
+        Level& Lv = ctx->L[lc + k];
+        const T *tx, *ty, *a9, *id;
+        T *x, *b;
+        level_ptrs<T>(Lv, tx, ty, a9, id, x, b);
+        A.n1[k] = Lv.n1;
+        A.n2[k] = Lv.n2;
+        A.tx[k] = tx; A.ty[k] = ty; A.a9[k] = a9; A.id[k] = id;
+        if (k == 0) { A.x0 = x; A.b0 = b; }
+    }
+    const size_t smem = coarse_bytes<T>(ctx, lc);
+    ++ctx->nlaunch;
+    if (ctx->L[lc].kind == FACE5)
+        k_coarse_vcycle<T, FACE5><<<1, 1024, smem, ctx->stream>>>(A);
+    else
+        k_coarse_vcycle<T, EXP9><<<1, 1024, smem, ctx->stream>>>(A);
+}
+
+// Temporally blocked level kernels: used for FP32 levels (all), FP64 levels only on request
+// (each CTA's FP64 work is latency-bound on one SM).
+template <class T>
+static bool use_fused_level(size_t l) {
+    if (sizeof(T) == 4) return env_long("IMPEC_MG_FUSED32", 1) != 0;
+    return env_long("IMPEC_MG_FUSED64", 0) != 0 && (l > 0 || env_long("IMPEC_MG_FUSE_FINE", 0) != 0);
 }
 
 template <class T>
@@ -639,78 +713,149 @@ static void vcycle(impec_ctx* ctx, size_t l) {
     const T *tx, *ty, *a9, *id;
     T *x, *b;
     level_ptrs<T>(F, tx, ty, a9, id, x, b);
-    if (l + 1 == ctx->L.size()) {
-        k_dense_solve<T><<<1, 64, 0, ctx->stream>>>(ctx->dense_n, ctx->dense_inv, b, x, 1);
+    const size_t lc = coarse_start<T>(ctx);
+    if (l == lc) {
+        launch_coarse<T>(ctx, lc);
         return;
     }
-    smooth<T>(ctx, F, 2, false);
     Level& C = ctx->L[l + 1];
     const T *ctx_, *cty, *ca9, *cid;
     T *cx, *cb;
     level_ptrs<T>(C, ctx_, cty, ca9, cid, cx, cb);
+    const bool fused = F.kind == FACE5 && use_fused_level<T>(l);
+    if (fused) {  // two launches for this level: smooth+residual+restrict, prolong+smooth
+        dim3 g((F.n2 + TB - 1) / TB, (F.n1 + TB - 1) / TB);
+        ++ctx->nlaunch;
+        k_level_pre<T><<<g, TBT, tb_smem<T, TBH_PRE>(), ctx->stream>>>(F.n1, F.n2, tx, ty, id, b, x, C.n2, cb, cx, C.n1);
+        vcycle<T>(ctx, l + 1);
+        ++ctx->nlaunch;
+        k_level_post<T><<<g, TBT, tb_smem<T, TBH_POST>(), ctx->stream>>>(F.n1, F.n2, tx, ty, id, b, x, C.n1, C.n2, cx);
+        return;
+    }
+    smooth<T>(ctx, F, 2, false);
+    ++ctx->nlaunch;
     k_restrict<T><<<grid2(C.n1, C.n2), dim3(BX, BY), 0, ctx->stream>>>(F, tx, ty, a9, b, x, C.n1, C.n2, cb, cx);
     vcycle<T>(ctx, l + 1);
+    ++ctx->nlaunch;
     k_prolong<T><<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, x, C.n1, C.n2, cx);
     smooth<T>(ctx, F, 2, true);
 }
 
-impec_status pressure_solve(impec_ctx* ctx, const double* c, double* p, double tol, int* cycles, double* relres) {
+// Convergence check of the multigrid loop (one thread): relres = ||r||/||f||; decides whether
+// another cycle runs and, inside a graph, sets the WHILE node's condition.
+__global__ void k_mg_check(DevScalars* S, double tol, int max_cycles, int inc, cudaGraphConditionalHandle h,
+                           int use_h) {
+    if (inc) S->mg_cycles++;
+    double fn = S->fnorm2, rn = S->rnorm2;
+    double rr = fn > 0 ? sqrt(rn / fn) : sqrt(rn);
+    S->relres = rr;
+    const bool bad = !(rr == rr) || isinf(rr);
+    const bool go = !bad && rr > tol && S->mg_cycles < max_cycles;
+    if (bad) S->flags |= FLAG_MG_NAN;
+    else if (!go && rr > tol) S->flags |= FLAG_MG_NOT_CONVERGED;
+    S->go = go ? 1 : 0;
+    if (use_h) cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+static int pin_index(impec_ctx* ctx) { return (int)IX(ctx->pin_i, ctx->pin_j, ctx->L[0].n2); }
+
+// Operator, hierarchy, consistent rhs, initial iterate and initial residual (launch only).
+impec_status pressure_prepare(impec_ctx* ctx, const double* c, const double* p) {
     const impec_params& P = ctx->P;
     IMPEC_TRY(pressure_setup(ctx, c));
     Level& F = ctx->L[0];
     const size_t n = F.n();
-    const int pin = (int)IX(ctx->pin_i, ctx->pin_j, F.n2);
+    const int pin = pin_index(ctx);
     const int rb = red_blocks(ctx);
     DevScalars* S = ctx->dscal;
+    ++ctx->nlaunch;
     k_rhs<<<rb, RED_THREADS, 0, ctx->stream>>>(n, ctx->q, ctx->G.dA, ctx->f, ctx->partials, ctx->max_blocks,
                                                 ctx->counter, &S->fsum);
+    ++ctx->nlaunch;
     k_fix_pin<<<1, 1, 0, ctx->stream>>>(ctx->f, ctx->q, pin, ctx->G.dA, ctx->pin_kappa, S);
     IMPEC_LAUNCH_CHECK();
-    double* x = F.x;
     if (P.warm_start)
-        IMPEC_CUDA_TRY(cudaMemcpyAsync(x, p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(F.x, p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     else
-        IMPEC_CUDA_TRY(cudaMemsetAsync(x, 0, n * 8, ctx->stream));
-    const bool mixed = P.precision == IMPEC_PREC_MIXED;
-    // F.b aliases the consistent rhs for the FP64 cycle
+        IMPEC_CUDA_TRY(cudaMemsetAsync(F.x, 0, n * 8, ctx->stream));
     IMPEC_CUDA_TRY(cudaMemcpyAsync(F.b, ctx->f, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
-    int k = 0;
-    double rr = 0;
-    impec_status st = IMPEC_OK;
-    for (;;) {
-        k_fine_resid<<<rb, RED_THREADS, 0, ctx->stream>>>(F, ctx->f, x, pin, mixed ? F.b32 : nullptr, ctx->partials,
-                                                           ctx->max_blocks, ctx->counter, &S->rnorm2);
-        IMPEC_LAUNCH_CHECK();
-        IMPEC_TRY(sync_scalars(ctx));
-        double fn = ctx->hscal->fnorm2;
-        rr = fn > 0 ? sqrt(ctx->hscal->rnorm2 / fn) : sqrt(ctx->hscal->rnorm2);
-        if (!std::isfinite(rr)) { st = IMPEC_ERR_NAN; break; }
-        if (rr <= tol) break;
-        if (k >= P.max_cycles) { st = IMPEC_ERR_NOT_CONVERGED; break; }
-        if (mixed) {
-            IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
-            vcycle<float>(ctx, 0);
-            k_add_f32<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, x, F.x32);
-        } else {
-            vcycle<double>(ctx, 0);
-        }
-        IMPEC_LAUNCH_CHECK();
-        ++k;
-    }
-    k_shift<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, x, pin, S);
+    IMPEC_CUDA_TRY(cudaMemsetAsync(&S->mg_cycles, 0, sizeof(int), ctx->stream));
+    return pressure_residual(ctx);
+}
+
+// FP64 fine residual and its norm (r32 for the mixed-precision correction).
+impec_status pressure_residual(impec_ctx* ctx) {
+    Level& F = ctx->L[0];
+    const bool mixed = ctx->P.precision == IMPEC_PREC_MIXED;
+    ++ctx->nlaunch;
+    k_fine_resid<<<red_blocks(ctx), RED_THREADS, 0, ctx->stream>>>(F, ctx->f, F.x, pin_index(ctx),
+                                                                  mixed ? F.b32 : nullptr, ctx->partials,
+                                                                  ctx->max_blocks, ctx->counter, &ctx->dscal->rnorm2);
     IMPEC_LAUNCH_CHECK();
-    IMPEC_CUDA_TRY(cudaMemcpyAsync(p, x, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status pressure_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h) {
+    ++ctx->nlaunch;
+    k_mg_check<<<1, 1, 0, ctx->stream>>>(ctx->dscal, tol, ctx->P.max_cycles, inc, h, use_h);
+    IMPEC_LAUNCH_CHECK();
+    return IMPEC_OK;
+}
+
+// One multigrid cycle on the current iterate followed by the new residual (launch only).
+impec_status pressure_iteration(impec_ctx* ctx) {
+    Level& F = ctx->L[0];
+    const size_t n = F.n();
+    if (ctx->P.precision == IMPEC_PREC_MIXED) {
+        IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
+        vcycle<float>(ctx, 0);
+        ++ctx->nlaunch;
+        k_add_f32<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, F.x, F.x32);
+    } else {
+        vcycle<double>(ctx, 0);
+    }
+    IMPEC_LAUNCH_CHECK();
+    return pressure_residual(ctx);
+}
+
+// Constant shift to the pinned value and copy to p (launch only).
+impec_status pressure_finish(impec_ctx* ctx, double* p) {
+    Level& F = ctx->L[0];
+    const size_t n = F.n();
+    ++ctx->nlaunch;
+    k_shift<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, F.x, pin_index(ctx), ctx->dscal);
+    IMPEC_LAUNCH_CHECK();
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(p, F.x, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    return IMPEC_OK;
+}
+
+// Host-driven solve (per-operation entry point): one host round trip per cycle.
+impec_status pressure_solve(impec_ctx* ctx, const double* c, double* p, double tol, int* cycles, double* relres) {
+    IMPEC_CUDA_TRY(cudaMemsetAsync(&ctx->dscal->flags, 0, sizeof(int), ctx->stream));
+    IMPEC_TRY(pressure_prepare(ctx, c, p));
+    IMPEC_TRY(pressure_check(ctx, tol, 0, 0, 0));
+    for (;;) {
+        IMPEC_TRY(sync_scalars(ctx));
+        if (!ctx->hscal->go) break;
+        IMPEC_TRY(pressure_iteration(ctx));
+        IMPEC_TRY(pressure_check(ctx, tol, 1, 0, 0));
+    }
+    IMPEC_TRY(pressure_finish(ctx, p));
+    const int k = ctx->hscal->mg_cycles;
+    const double rr = ctx->hscal->relres;
     if (cycles) *cycles = k;
     if (relres) *relres = rr;
     ctx->last_its = k;
     ctx->last_relres = rr;
-    return st;
+    if (ctx->hscal->flags & FLAG_MG_NAN) return IMPEC_ERR_NAN;
+    if (ctx->hscal->flags & FLAG_MG_NOT_CONVERGED) return IMPEC_ERR_NOT_CONVERGED;
+    return IMPEC_OK;
 }
 
 impec_status pressure_apply_ref(impec_ctx* ctx, const double* x, double* y) {
     Level& F = ctx->L[0];
     const int pin = (int)IX(ctx->pin_i, ctx->pin_j, F.n2);
-    k_apply_ref<<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F, x, pin, ctx->G.dA, ctx->pin_kappa, y);
+    ++ctx->nlaunch, k_apply_ref<<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F, x, pin, ctx->G.dA, ctx->pin_kappa, y);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -777,7 +922,7 @@ impec_status velocity(impec_ctx* ctx, const double* p, const double* c, double* 
     const impec_params& P = ctx->P;
     const Geo& G = ctx->G;
     VelArgs A{P.N1, P.N2, P.nu, 1.0 / G.dx, 1.0 / G.dy, 1.0 / G.dxi, 1.0 / G.deta, G.cost, G.sina, G.sint, G.cosa};
-    k_velocity<<<grid2(P.N1 + 1, P.N2 + 1), dim3(BX, BY), 0, ctx->stream>>>(A, p, ctx->lamx, ctx->lamy, ctx->cm11,
+    ++ctx->nlaunch, k_velocity<<<grid2(P.N1 + 1, P.N2 + 1), dim3(BX, BY), 0, ctx->stream>>>(A, p, ctx->lamx, ctx->lamy, ctx->cm11,
                                                                             ctx->cm22, ctx->cm12, u, v);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
@@ -826,13 +971,58 @@ impec_status max_stable_dt_dev(impec_ctx* ctx, const double* u, const double* v)
     const impec_params& P = ctx->P;
     const Geo& G = ctx->G;
     const int rb = red_blocks(ctx);
-    k_maxvel<<<rb, RED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, u, v, P.diffusion, P.alpha_l, P.alpha_t, G.dx,
+    ++ctx->nlaunch, k_maxvel<<<rb, RED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, u, v, P.diffusion, P.alpha_l, P.alpha_t, G.dx,
                                                    ctx->partials, ctx->max_blocks, ctx->counter, ctx->dscal->red);
     double cfl = P.cfl_porosity ? P.cfl * P.porosity : P.cfl;
     const int use_diff = P.diffusion && P.ptype != IMPEC_CRANKNICOLSON;
-    k_finish_dt<<<1, 1, 0, ctx->stream>>>(ctx->dscal, G.dx, G.dy, cfl, use_diff, P.dt_diff_limit);
+    ++ctx->nlaunch, k_finish_dt<<<1, 1, 0, ctx->stream>>>(ctx->dscal, G.dx, G.dy, cfl, use_diff, P.dt_diff_limit);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
 
 }  // namespace impec
+
+using namespace impec;
+
+extern "C" impec_status impec_time_kernel(impec_ctx* ctx, int which, int reps, double* ms, double* bytes) {
+    if (!ctx || reps <= 0 || which < 0 || which > 4) return IMPEC_ERR_ARG;
+    Level& F = ctx->L[0];
+    const double n = (double)F.n();
+    if (which == 1 && ctx->P.precision != IMPEC_PREC_MIXED) {  // FP32 copies of the fine level
+        const int nb = ctx->num_sms * 4;
+        if (F.kind == FACE5) {
+            k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)(F.n1 + 1) * F.n2, F.tx, F.tx32);
+            k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)F.n1 * (F.n2 + 1), F.ty, F.ty32);
+        } else {
+            k_to_float<<<nb, 256, 0, ctx->stream>>>(F.n() * 9, F.a9, F.a932);
+        }
+        k_to_float<<<nb, 256, 0, ctx->stream>>>(F.n(), F.idiag, F.idiag32);
+        k_to_float<<<nb, 256, 0, ctx->stream>>>(F.n(), F.b, F.b32);
+        k_to_float<<<nb, 256, 0, ctx->stream>>>(F.n(), F.x, F.x32);
+        IMPEC_LAUNCH_CHECK();
+    }
+    cudaEvent_t e0, e1;
+    IMPEC_CUDA_TRY(cudaEventCreate(&e0));
+    IMPEC_CUDA_TRY(cudaEventCreate(&e1));
+    const double coef = F.kind == FACE5 ? 2.0 : 9.0;  // operator planes per cell
+    double b = 0;
+    IMPEC_CUDA_TRY(cudaEventRecord(e0, ctx->stream));
+    for (int r = 0; r < reps; ++r) {
+        switch (which) {
+            case 0: smooth<double>(ctx, F, 1, false); b = n * 8 * (4 + coef); break;  // x,b,idiag r + x w + operator
+            case 1: smooth<float>(ctx, F, 1, false); b = n * 4 * (4 + coef); break;
+            case 2: IMPEC_TRY(pressure_residual(ctx)); b = n * 8 * (2 + coef) + (ctx->P.precision ? 4 * n : 0); break;
+            case 3: IMPEC_TRY(advect_x_dev(ctx, ctx->c, ctx->t1, ctx->u, 1.0, &ctx->dscal->dt)); b = n * 24; break;
+            case 4: IMPEC_TRY(advect_y_dev(ctx, ctx->c, ctx->t1, ctx->v, 1.0, &ctx->dscal->dt)); b = n * 24; break;
+        }
+    }
+    IMPEC_CUDA_TRY(cudaEventRecord(e1, ctx->stream));
+    IMPEC_CUDA_TRY(cudaEventSynchronize(e1));
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms) *ms = t / reps;
+    if (bytes) *bytes = b;
+    return IMPEC_OK;
+}

@@ -15,15 +15,34 @@ static impec_status set_dt(impec_ctx* ctx, double dt) {
     return IMPEC_OK;
 }
 
-// HyperbolicSplitSolver::Solve with SPLIT2ND (src/HyperbolicSplitSolver.cpp:162-198).
+static impec_status cn_solve_host(impec_ctx* ctx, double* c, double tol) {
+    IMPEC_TRY(cn_prepare(ctx, c, 0.5, &ctx->dscal->dt));
+    IMPEC_TRY(cn_check(ctx, tol, 0, 0, 0));
+    for (;;) {
+        IMPEC_TRY(sync_scalars(ctx));
+        if (!ctx->hscal->go) break;
+        IMPEC_TRY(cn_iteration(ctx, c));
+        IMPEC_TRY(cn_check(ctx, tol, 1, 0, 0));
+    }
+    if (ctx->hscal->flags & FLAG_CN_NAN) return IMPEC_ERR_NAN;
+    if (ctx->hscal->flags & FLAG_CN_NOT_CONVERGED) return IMPEC_ERR_NOT_CONVERGED;
+    return IMPEC_OK;
+}
+
+// HyperbolicSplitSolver::Solve with SPLIT2ND (src/HyperbolicSplitSolver.cpp:162-198), host
+// driven.  Both Crank-Nicolson half steps share v and dt/2, hence one matrix per call.
 impec_status hyperbolic_solve_dev(impec_ctx* ctx, double* c, const double* u, const double* v, const double* dt_dev,
                                   int* pfs) {
     const impec_params& P = ctx->P;
+    IMPEC_CUDA_TRY(cudaMemsetAsync(&ctx->dscal->flags, 0, sizeof(int), ctx->stream));
     IMPEC_TRY(tr_integrate_dev(ctx, c, 0.5, dt_dev, 0));
-    if (P.diffusion) IMPEC_TRY(dispersion_cn_dev(ctx, c, u, v, 0.5, dt_dev, P.para_eps, nullptr, nullptr));
+    if (P.diffusion) {
+        IMPEC_TRY(cn_setup(ctx, u, v, 0.5, dt_dev));
+        IMPEC_TRY(cn_solve_host(ctx, c, P.para_eps));
+    }
     IMPEC_TRY(advect_split_dev(ctx, c, u, v, dt_dev, pfs));
     IMPEC_TRY(tr_integrate_dev(ctx, c, 0.5, dt_dev, 1));
-    if (P.diffusion) IMPEC_TRY(dispersion_cn_dev(ctx, c, u, v, 0.5, dt_dev, P.para_eps, nullptr, nullptr));
+    if (P.diffusion) IMPEC_TRY(cn_solve_host(ctx, c, P.para_eps));
     return IMPEC_OK;
 }
 
@@ -55,7 +74,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_diag(int n1, int n2, const doub
 
 static impec_status diagnostics_dev(impec_ctx* ctx, const double* c, const double* u, const double* v) {
     const impec_params& P = ctx->P;
-    k_diag<<<ctx->num_sms * 2, RED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, u, v, ctx->have_source ? ctx->q : nullptr,
+    ++ctx->nlaunch, k_diag<<<ctx->num_sms * 2, RED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, u, v, ctx->have_source ? ctx->q : nullptr,
                                                               1.0 / ctx->G.dx, 1.0 / ctx->G.dy, ctx->partials,
                                                               ctx->max_blocks, ctx->counter, ctx->dscal->red);
     IMPEC_LAUNCH_CHECK();
@@ -69,43 +88,35 @@ static double mass_error(const impec_ctx* ctx, double mass, double t) {
     return fabs((mass + ctx->total_outflux - influx) / influx);
 }
 
-static impec_status one_step(impec_ctx* ctx, double t_clip, bool sync_dt, impec_step_info* info) {
-    const impec_params& P = ctx->P;
-    int cyc = 0;
-    double rr = 0;
-    IMPEC_TRY(pressure_solve(ctx, ctx->c, ctx->p, P.eps, &cyc, &rr));
-    IMPEC_TRY(velocity(ctx, ctx->p, ctx->c, ctx->u, ctx->v));
-    IMPEC_TRY(max_stable_dt_dev(ctx, ctx->u, ctx->v));
-    double dt = 0;
-    int clipped = 0;
-    if (sync_dt) {
-        IMPEC_TRY(sync_scalars(ctx));
-        dt = ctx->hscal->dt;
-        if (t_clip >= 0 && ctx->t + dt >= t_clip) {  // output-time matching, src/Impec2DSolver.cpp:375-378
-            dt = t_clip - ctx->t;
-            IMPEC_TRY(set_dt(ctx, dt));
-            clipped = 1;
-        }
-    }
-    IMPEC_TRY(hyperbolic_solve_dev(ctx, ctx->c, ctx->u, ctx->v, &ctx->dscal->dt, &ctx->prev_first_sweep));
+// One resident IMPES step through the step graph; with info, waits and reports.
+static impec_status one_step(impec_ctx* ctx, double t_clip, impec_step_info* info) {
+    IMPEC_TRY(launch_step_graph(ctx, t_clip));
     ctx->counter_steps++;
-    if (sync_dt) ctx->t += dt;
-    if (info) {
-        IMPEC_TRY(sync_scalars(ctx));
-        if (!sync_dt) ctx->t += ctx->hscal->dt;
-        ctx->total_outflux = ctx->hscal->total_outflux;
-        info->t = ctx->t;
-        info->dt = ctx->hscal->dt;
-        info->total_outflux = ctx->total_outflux;
-        info->relres = rr;
-        info->counter = ctx->counter_steps;
-        info->its = cyc;
-        info->para_its = ctx->last_para_its;
-        info->prev_first_sweep = ctx->prev_first_sweep;
-        info->clipped = clipped;
-        IMPEC_TRY(diagnostics_dev(ctx, ctx->c, ctx->u, ctx->v));
-        IMPEC_TRY(sync_scalars(ctx));
-        info->mass_err = mass_error(ctx, ctx->hscal->red[0], ctx->t);
+    if (!info) return IMPEC_OK;
+    IMPEC_TRY(sync_scalars(ctx));
+    const DevScalars& H = *ctx->hscal;
+    ctx->t = H.t;
+    ctx->total_outflux = H.total_outflux;
+    ctx->last_its = H.mg_cycles;
+    ctx->last_relres = H.relres;
+    ctx->last_para_its = H.cn_cycles_total;
+    info->t = H.t;
+    info->dt = H.dt;
+    info->total_outflux = H.total_outflux;
+    info->relres = H.relres;
+    info->counter = ctx->counter_steps;
+    info->its = H.mg_cycles;
+    info->para_its = H.cn_cycles_total;
+    info->prev_first_sweep = ctx->prev_first_sweep;
+    info->clipped = H.clipped;
+    const int flags = H.flags;
+    IMPEC_TRY(diagnostics_dev(ctx, ctx->c, ctx->u, ctx->v));
+    IMPEC_TRY(sync_scalars(ctx));
+    info->mass_err = mass_error(ctx, ctx->hscal->red[0], ctx->t);
+    if (flags & (FLAG_MG_NAN | FLAG_CN_NAN)) { set_error("NaN in a residual"); return IMPEC_ERR_NAN; }
+    if (flags & (FLAG_MG_NOT_CONVERGED | FLAG_CN_NOT_CONVERGED)) {
+        set_error(flags & FLAG_MG_NOT_CONVERGED ? "pressure multigrid hit max_cycles" : "Crank-Nicolson hit max_cycles");
+        return IMPEC_ERR_NOT_CONVERGED;
     }
     return IMPEC_OK;
 }
@@ -230,14 +241,15 @@ impec_status impec_diagnostics(impec_ctx* ctx, const double* c, const double* u,
 impec_status impec_step(impec_ctx* ctx, double t_clip, impec_step_info* info) {
     if (!ctx) return IMPEC_ERR_ARG;
     impec_step_info tmp;
-    IMPEC_TRY(one_step(ctx, t_clip, true, info ? info : &tmp));
-    return IMPEC_OK;
+    return one_step(ctx, t_clip, info ? info : &tmp);
 }
 
 impec_status impec_run_steps(impec_ctx* ctx, int n, impec_step_info* info) {
     if (!ctx || n < 0) return IMPEC_ERR_ARG;
-    for (int s = 0; s < n; ++s) IMPEC_TRY(one_step(ctx, -1.0, false, (s == n - 1) ? info : nullptr));
-    if (n == 0 || !info) IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    for (int s = 0; s + 1 < n; ++s) IMPEC_TRY(one_step(ctx, -1.0, nullptr));
+    if (n > 0 && info) return one_step(ctx, -1.0, info);
+    if (n > 0) IMPEC_TRY(one_step(ctx, -1.0, nullptr));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return IMPEC_OK;
 }
 
@@ -248,6 +260,7 @@ impec_status impec_set_time(impec_ctx* ctx, double t0) {
     ctx->counter_steps = 0;
     double z = 0.0;
     IMPEC_CUDA_TRY(cudaMemcpyAsync(&ctx->dscal->total_outflux, &z, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(&ctx->dscal->t, &ctx->t0, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return IMPEC_OK;
 }
@@ -279,6 +292,25 @@ impec_status impec_pressure_upload(impec_ctx* ctx, const double* p_host, int g) 
     for (int i = 0; i < N1; ++i) std::memcpy(&buf[IX(i, 0, N2)], p_host + (size_t)(i + g) * w + g, N2 * 8);
     IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->p, buf.data(), buf.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
     IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+impec_status impec_pressure_solve_resident(impec_ctx* ctx, int sync, int* cycles, double* relres) {
+    if (!ctx) return IMPEC_ERR_ARG;
+    IMPEC_TRY(launch_pressure_graph(ctx));
+    if (!sync) return IMPEC_OK;
+    IMPEC_TRY(sync_scalars(ctx));
+    if (cycles) *cycles = ctx->hscal->mg_cycles;
+    if (relres) *relres = ctx->hscal->relres;
+    if (ctx->hscal->flags & FLAG_MG_NAN) return IMPEC_ERR_NAN;
+    if (ctx->hscal->flags & FLAG_MG_NOT_CONVERGED) return IMPEC_ERR_NOT_CONVERGED;
+    return IMPEC_OK;
+}
+
+impec_status impec_launch_count(impec_ctx* ctx, long long* n) {
+    if (!ctx || !n) return IMPEC_ERR_ARG;
+    IMPEC_TRY(sync_scalars(ctx));
+    *n = ctx->nlaunch + ctx->hscal->graph_launches;
     return IMPEC_OK;
 }
 

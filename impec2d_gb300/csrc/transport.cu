@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_tr(int nw, const int* __restric
 
 impec_status tr_integrate_dev(impec_ctx* ctx, double* c, double dt_scale, const double* dt_dev, int slot) {
     if (!ctx->have_source || ctx->nwells == 0) return IMPEC_OK;
-    k_tr<<<1, RED_THREADS, 0, ctx->stream>>>(ctx->nwells, ctx->well_idx, ctx->well_q, c, dt_dev, dt_scale,
+    ++ctx->nlaunch, k_tr<<<1, RED_THREADS, 0, ctx->stream>>>(ctx->nwells, ctx->well_idx, ctx->well_q, c, dt_dev, dt_scale,
                                              ctx->P.inj_fluid_conc, ctx->dscal, slot);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
@@ -67,16 +67,26 @@ __device__ __forceinline__ void hancock(double cm, double c0, double cp, double 
     sr = UR + df;
 }
 
+// Reflected (or wrapped) cell index, clamped into [0, n): tile loads may reach further than
+// two cells past the boundary on small grids; those values never reach an in-domain output.
 template <int BC>
-__device__ __forceinline__ int cell_at(int i, int n) { return BC == IMPEC_BC_PERIODIC ? wrap_cell(i, n) : refl_cell(i, n); }
+__device__ __forceinline__ int cell_at(int i, int n) {
+    int r = BC == IMPEC_BC_PERIODIC ? wrap_cell(i, n) : refl_cell(i, n);
+    return r < 0 ? 0 : (r >= n ? n - 1 : r);
+}
 
 // Normal face velocity along the sweep direction, ghost faces by odd reflection (Neumann)
 // or wrap-around (periodic).
 template <int BC>
 __device__ __forceinline__ double face_at(const double* __restrict__ u, int f, int n, size_t stride_f, size_t off) {
-    if (BC == IMPEC_BC_PERIODIC) return u[(size_t)wrap_face(f, n) * stride_f + off];
+    if (BC == IMPEC_BC_PERIODIC) {
+        int w = wrap_face(f, n);
+        w = w < 0 ? 0 : (w > n ? n : w);
+        return u[(size_t)w * stride_f + off];
+    }
     double s = 1.0;
     int ff = refl_face(f, n, s);
+    ff = ff < 0 ? 0 : (ff > n ? n : ff);
     return s * u[(size_t)ff * stride_f + off];
 }
 
@@ -142,6 +152,126 @@ __global__ void k_average(size_t n, double* __restrict__ c, const double* __rest
         c[k] = 0.5 * (a[k] + b[k]);
 }
 
+// ---------------------------------------------------------------- fused symmetric-parallel update
+// One CTA owns a TI x TJ tile of the output.  It loads c (2-cell halo), the x-face velocities
+// u and the y-face velocities v it needs (ghost values by the reflections above), then
+// computes in shared memory  XY = Y(X(c)),  YX = X(Y(c))  and writes (XY + YX)/2, which is
+// AdvectSplit's SYMMETRIC_PARALLEL branch (src/HyperbolicSplitSolver.cpp:87-103).  Each
+// sweep first computes the two Hancock states of every cell it needs once, then the fluxes
+// and updates; the arithmetic per cell is that of sweep_cell, so results are identical.
+constexpr int TI = 16, TJ = 32, FUSED_THREADS = 256;
+constexpr int CW = TJ + 4;                // row width of c, c1 (j in [j0-2, j0+TJ+2))
+constexpr int VW = TJ + 3;                // row width of v faces (fj in [j0-1, j0+TJ+2))
+constexpr int HMAX = (TI + 4) * (TJ + 2) > (TI + 2) * (TJ + 4) ? (TI + 4) * (TJ + 2) : (TI + 2) * (TJ + 4);
+
+template <int SCHEME>
+__device__ __forceinline__ void states(double cm, double c0, double cp, double ul, double ur, double kap, double& sl,
+                                       double& sr) {
+    if (SCHEME == IMPEC_UPWINDSPLIT) { sl = sr = c0; return; }
+    hancock(cm, c0, cp, ul, ur, kap, sl, sr);
+}
+
+template <int SCHEME, int BC>
+__global__ void __launch_bounds__(FUSED_THREADS) k_advect_symmetric(int n1, int n2, const double* __restrict__ cin,
+                                                                     double* __restrict__ cout,
+                                                                     const double* __restrict__ u,
+                                                                     const double* __restrict__ v,
+                                                                     const double* __restrict__ dt_dev, double inv_dx_phi,
+                                                                     double inv_dy_phi) {
+    __shared__ double sc[(TI + 4) * CW];   // c, rows i0-2 .. i0+TI+1
+    __shared__ double su[(TI + 3) * CW];   // u faces fi in [i0-1, i0+TI+1], cols j0-2 ..
+    __shared__ double sv[(TI + 4) * VW];   // v faces, rows i0-2 .., fj in [j0-1, j0+TJ+1]
+    __shared__ double s1[TI * CW];         // X(c) on rows i0..i0+TI-1, cols j0-2 ..
+    __shared__ double s2[(TI + 4) * TJ];   // Y(c) on rows i0-2 .., cols j0 ..
+    __shared__ double sxy[TI * TJ];        // Y(X(c))
+    __shared__ double hl[HMAX], hr[HMAX];  // Hancock states at the left / right face of a cell
+    const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ, t = threadIdx.x;
+    const double dt = dt_dev[0];
+    const double lx = dt * inv_dx_phi, kx = 0.5 * lx, ly = dt * inv_dy_phi, ky = 0.5 * ly;
+    // ---- loads (reflected ghosts) ----
+    for (int k = t; k < (TI + 4) * CW; k += FUSED_THREADS) {
+        int a = k / CW, b = k % CW;
+        sc[k] = cin[IX(cell_at<BC>(i0 - 2 + a, n1), cell_at<BC>(j0 - 2 + b, n2), n2)];
+    }
+    for (int k = t; k < (TI + 3) * CW; k += FUSED_THREADS) {
+        int a = k / CW, b = k % CW;
+        su[k] = face_at<BC>(u, i0 - 1 + a, n1, n2, cell_at<BC>(j0 - 2 + b, n2));
+    }
+    for (int k = t; k < (TI + 4) * VW; k += FUSED_THREADS) {
+        int a = k / VW, b = k % VW;
+        sv[k] = face_at<BC>(v + IX(cell_at<BC>(i0 - 2 + a, n1), 0, n2 + 1), j0 - 1 + b, n2, 1, 0);
+    }
+    __syncthreads();
+    // ---- XY path, X sweep: cells i in [i0-1, i0+TI], rows b in [0, CW) ----
+    for (int k = t; k < (TI + 2) * CW; k += FUSED_THREADS) {
+        int a = k / CW, b = k % CW;  // cell i = i0-1+a, c row index a+1
+        states<SCHEME>(sc[a * CW + b], sc[(a + 1) * CW + b], sc[(a + 2) * CW + b], su[a * CW + b], su[(a + 1) * CW + b],
+                       kx, hl[k], hr[k]);
+    }
+    __syncthreads();
+    for (int k = t; k < TI * CW; k += FUSED_THREADS) {
+        int a = k / CW, b = k % CW;  // cell i = i0+a: states at a+1, faces fi = i0+a (su row a+1), i0+a+1
+        double uw = su[(a + 1) * CW + b], ue = su[(a + 2) * CW + b];
+        double Fw = uw * (uw > 0 ? hr[a * CW + b] : hl[(a + 1) * CW + b]);
+        double Fe = ue * (ue > 0 ? hr[(a + 1) * CW + b] : hl[(a + 2) * CW + b]);
+        s1[k] = sc[(a + 2) * CW + b] + lx * (Fw - Fe);
+    }
+    __syncthreads();
+    // ---- XY path, Y sweep on s1: cells j in [j0-1, j0+TJ], rows a in [0, TI) ----
+    for (int k = t; k < TI * (TJ + 2); k += FUSED_THREADS) {
+        int a = k / (TJ + 2), b = k % (TJ + 2);  // cell j = j0-1+b -> s1 col b+1; faces fj = j, j+1 -> sv col b, b+1
+        const double* row = s1 + a * CW;
+        const double* vr = sv + (a + 2) * VW;
+        states<SCHEME>(row[b], row[b + 1], row[b + 2], vr[b], vr[b + 1], ky, hl[k], hr[k]);
+    }
+    __syncthreads();
+    for (int k = t; k < TI * TJ; k += FUSED_THREADS) {
+        int a = k / TJ, b = k % TJ;  // cell j = j0+b: states index b+1
+        const double* vr = sv + (a + 2) * VW;
+        const int h = a * (TJ + 2);
+        double vs = vr[b + 1], vn = vr[b + 2];
+        double Fs = vs * (vs > 0 ? hr[h + b] : hl[h + b + 1]);
+        double Fn = vn * (vn > 0 ? hr[h + b + 1] : hl[h + b + 2]);
+        sxy[k] = s1[a * CW + b + 2] + ly * (Fs - Fn);
+    }
+    __syncthreads();
+    // ---- YX path, Y sweep on c: rows a in [0, TI+4) (i = i0-2+a), cells j in [j0-1, j0+TJ] ----
+    for (int k = t; k < (TI + 4) * (TJ + 2); k += FUSED_THREADS) {
+        int a = k / (TJ + 2), b = k % (TJ + 2);
+        const double* row = sc + a * CW;
+        const double* vr = sv + a * VW;
+        states<SCHEME>(row[b], row[b + 1], row[b + 2], vr[b], vr[b + 1], ky, hl[k], hr[k]);
+    }
+    __syncthreads();
+    for (int k = t; k < (TI + 4) * TJ; k += FUSED_THREADS) {
+        int a = k / TJ, b = k % TJ;
+        const double* vr = sv + a * VW;
+        const int h = a * (TJ + 2);
+        double vs = vr[b + 1], vn = vr[b + 2];
+        double Fs = vs * (vs > 0 ? hr[h + b] : hl[h + b + 1]);
+        double Fn = vn * (vn > 0 ? hr[h + b + 1] : hl[h + b + 2]);
+        s2[k] = sc[a * CW + b + 2] + ly * (Fs - Fn);
+    }
+    __syncthreads();
+    // ---- YX path, X sweep on s2: cells i in [i0-1, i0+TI] (s2 rows a+1), cols b in [0, TJ) ----
+    for (int k = t; k < (TI + 2) * TJ; k += FUSED_THREADS) {
+        int a = k / TJ, b = k % TJ;
+        states<SCHEME>(s2[a * TJ + b], s2[(a + 1) * TJ + b], s2[(a + 2) * TJ + b], su[a * CW + b + 2],
+                       su[(a + 1) * CW + b + 2], kx, hl[k], hr[k]);
+    }
+    __syncthreads();
+    for (int k = t; k < TI * TJ; k += FUSED_THREADS) {
+        int a = k / TJ, b = k % TJ;
+        const int gi = i0 + a, gj = j0 + b;
+        if (gi >= n1 || gj >= n2) continue;
+        double uw = su[(a + 1) * CW + b + 2], ue = su[(a + 2) * CW + b + 2];
+        double Fw = uw * (uw > 0 ? hr[a * TJ + b] : hl[(a + 1) * TJ + b]);
+        double Fe = ue * (ue > 0 ? hr[(a + 1) * TJ + b] : hl[(a + 2) * TJ + b]);
+        double yx = s2[(a + 2) * TJ + b] + lx * (Fw - Fe);
+        cout[IX(gi, gj, n2)] = 0.5 * (sxy[k] + yx);
+    }
+}
+
 static dim3 tgrid(int n1, int n2) { return dim3((n2 + TBX - 1) / TBX, (n1 + TBY - 1) / TBY); }
 
 impec_status advect_x_dev(impec_ctx* ctx, const double* cin, double* cout, const double* u, double dt_scale,
@@ -149,6 +279,7 @@ impec_status advect_x_dev(impec_ctx* ctx, const double* cin, double* cout, const
     const impec_params& P = ctx->P;
     const double f = 1.0 / (ctx->G.dx * P.porosity);
     dim3 g = tgrid(P.N1, P.N2), b(TBX, TBY);
+    ++ctx->nlaunch;
     const bool per = P.bc == IMPEC_BC_PERIODIC;
     if (P.hmtype == IMPEC_MUSCL) {
         if (per) k_sweep_x<IMPEC_MUSCL, IMPEC_BC_PERIODIC><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
@@ -166,6 +297,7 @@ impec_status advect_y_dev(impec_ctx* ctx, const double* cin, double* cout, const
     const impec_params& P = ctx->P;
     const double f = 1.0 / (ctx->G.dy * P.porosity);
     dim3 g = tgrid(P.N1, P.N2), b(TBX, TBY);
+    ++ctx->nlaunch;
     const bool per = P.bc == IMPEC_BC_PERIODIC;
     if (P.hmtype == IMPEC_MUSCL) {
         if (per) k_sweep_y<IMPEC_MUSCL, IMPEC_BC_PERIODIC><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
@@ -180,7 +312,7 @@ impec_status advect_y_dev(impec_ctx* ctx, const double* cin, double* cout, const
 
 impec_status average_dev(impec_ctx* ctx, double* c, const double* a, const double* b) {
     const size_t n = (size_t)ctx->P.N1 * ctx->P.N2;
-    k_average<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, c, a, b);
+    ++ctx->nlaunch, k_average<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, c, a, b);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -223,13 +355,22 @@ impec_status advect_split_dev(impec_ctx* ctx, double* c, const double* u, const 
             IMPEC_TRY(advect_x_dev(ctx, t2, c, u, 0.5, dt_dev, t3));
             *pfs = 0;
             break;
-        default:  // SYMMETRIC_PARALLEL: average of XY and YX applied to copies of c
-            IMPEC_TRY(advect_x_dev(ctx, c, t1, u, 1.0, dt_dev));
-            IMPEC_TRY(advect_y_dev(ctx, t1, t2, v, 1.0, dt_dev));
-            IMPEC_TRY(advect_y_dev(ctx, c, t1, v, 1.0, dt_dev));
-            IMPEC_TRY(advect_x_dev(ctx, t1, t3, u, 1.0, dt_dev));
-            IMPEC_TRY(average_dev(ctx, c, t2, t3));
+        default: {  // SYMMETRIC_PARALLEL: one fused pass, c -> t1, then swap into c
+            const double fx = 1.0 / (ctx->G.dx * P.porosity), fy = 1.0 / (ctx->G.dy * P.porosity);
+            dim3 g((P.N2 + TJ - 1) / TJ, (P.N1 + TI - 1) / TI);
+            const bool per = P.bc == IMPEC_BC_PERIODIC;
+            ++ctx->nlaunch;
+            if (P.hmtype == IMPEC_MUSCL) {
+                if (per) k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_PERIODIC><<<g, FUSED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+                else k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_NEUMANN><<<g, FUSED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+            } else {
+                if (per) k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC><<<g, FUSED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+                else k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN><<<g, FUSED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+            }
+            IMPEC_LAUNCH_CHECK();
+            IMPEC_CUDA_TRY(cudaMemcpyAsync(c, t1, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
             *pfs = 0;
+        }
     }
     (void)bytes;
     return IMPEC_OK;

@@ -159,6 +159,19 @@ impec_status impec_step(impec_ctx* ctx, double t_clip, impec_step_info* info);
  * last step is returned).  Used by throughput runs. */
 impec_status impec_run_steps(impec_ctx* ctx, int n, impec_step_info* info);
 
+/* Pressure solve of the resident state (c -> p) as one CUDA graph (no host round trip per
+ * cycle).  With sync = 0 the call only enqueues; cycles/relres are then not written. */
+impec_status impec_pressure_solve_resident(impec_ctx* ctx, int sync, int* cycles, double* relres);
+/* Kernel launches executed by this context so far (stream launches + step-graph replays). */
+impec_status impec_launch_count(impec_ctx* ctx, long long* n);
+/* Engine instrumentation: times `reps` stream launches of one hot kernel on the resident
+ * state with CUDA events.  which: 0 fine-level red-black Gauss-Seidel sweep (both colours,
+ * FP64), 1 the same in FP32, 2 FP64 fine residual + norm, 3 one x-sweep of the transport,
+ * 4 one y-sweep of the transport.  Returns the mean time per launch and the algorithmic
+ * bytes one launch moves. */
+impec_status impec_time_kernel(impec_ctx* ctx, int which, int reps, double* ms_per_launch,
+                               double* bytes_per_launch);
+
 /* ---- host-buffer entry points (reference Blitz layouts; copies inside the call) ---- */
 impec_status impec_state_upload(impec_ctx* ctx, const double* c_host, const double* q_host,
                                 int ghost);
