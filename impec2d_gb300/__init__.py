@@ -100,6 +100,7 @@ _SIGS = {
     "impec_run_cfg": (C.c_int, [C.c_char_p, C.c_int]),
     "impec_launch_count": (C.c_int, [_VP, C.POINTER(C.c_longlong)]),
     "impec_pressure_solve_resident": (C.c_int, [_VP, C.c_int, _PI, _PD]),
+    "impec_advect_symmetric_noalloc": (C.c_int, [C.POINTER(Params), _VP, _VP, _VP, C.c_double, _VP]),
     "impec_time_kernel": (C.c_int, [_VP, C.c_int, C.c_int, _PD, _PD]),
 }
 

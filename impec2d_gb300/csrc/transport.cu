@@ -6,6 +6,7 @@
 // of the updated interior rows (mirrored c and mirrored tangential velocity give the same
 // fluxes), so the following Y sweep reads them here by reflecting the interior result.
 #include <cmath>
+#include <mutex>
 
 #include "internal.cuh"
 #include "reduce.cuh"
@@ -377,3 +378,75 @@ impec_status advect_split_dev(impec_ctx* ctx, double* c, const double* u, const 
 }
 
 }  // namespace impec
+
+// ---------------------------------------------------------------- allocation-free transport step
+// For callers that cannot allocate device memory: code running under a host framework that
+// owns every device allocation (a fixed memory pool or budget), or a caller that must not
+// trigger cudaMalloc's implicit device synchronisation in the middle of its own work.  The
+// symmetric-parallel update above needs one field-sized buffer (it cannot update c in place,
+// since neighbouring tiles read the old c) and a device copy of dt; here both live in a
+// file-scope device array that every GPU loading this library holds until the process exits.
+// Nothing in the array has to start at zero: each call writes dt and every cell of the
+// updated field before any kernel reads them.
+namespace impec {
+
+constexpr size_t NOALLOC_MAX_CELLS = size_t(1) << 20;  // 1,048,576 cells: 8 MiB of FP64
+constexpr size_t NOALLOC_FIELD_OFFSET = 32;            // doubles before the field (dt at [0]); 256-byte aligned
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_FIELD_OFFSET + NOALLOC_MAX_CELLS];
+
+// Device address of g_noalloc_scratch on the current device, looked up once per device (the
+// host-side name of the array is only a stand-in, not a device address).
+static impec_status noalloc_scratch(double** out) {
+    static std::mutex mu;
+    static double* addr[64] = {nullptr};
+    int dev = 0;
+    IMPEC_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) { set_error("device ordinal out of range"); return IMPEC_ERR_ARG; }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        IMPEC_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        addr[dev] = static_cast<double*>(p);
+    }
+    *out = addr[dev];
+    return IMPEC_OK;
+}
+
+}  // namespace impec
+
+extern "C" impec_status impec_advect_symmetric_noalloc(const impec_params* P, double* c_dev, const double* u_dev,
+                                                       const double* v_dev, double dt, void* stream) {
+    using namespace impec;
+    if (!P || !c_dev || !u_dev || !v_dev) { set_error("null argument"); return IMPEC_ERR_ARG; }
+    if (P->N1 < 2 || P->N2 < 2) { set_error("N1 and N2 must be >= 2"); return IMPEC_ERR_ARG; }
+    if ((size_t)P->N1 * (size_t)P->N2 > NOALLOC_MAX_CELLS) {
+        set_error("impec_advect_symmetric_noalloc: N1*N2 exceeds its static scratch of 1048576 cells; "
+                  "use impec_advect_split with a context instead");
+        return IMPEC_ERR_ARG;
+    }
+    if (P->hmtype != IMPEC_MUSCL && P->hmtype != IMPEC_UPWINDSPLIT) { set_error("unknown hmtype"); return IMPEC_ERR_ARG; }
+    if (!(P->porosity > 0) || !(P->x_ub > P->x_lb) || !(P->y_ub > P->y_lb) || !(dt >= 0) || isinf(dt)) {
+        set_error("invalid porosity, domain or dt");
+        return IMPEC_ERR_ARG;
+    }
+    double* scratch = nullptr;
+    IMPEC_TRY(noalloc_scratch(&scratch));
+    cudaStream_t s = (cudaStream_t)stream;
+    const int N1 = P->N1, N2 = P->N2;
+    const double dx = (P->x_ub - P->x_lb) / N1, dy = (P->y_ub - P->y_lb) / N2;
+    const double fx = 1.0 / (dx * P->porosity), fy = 1.0 / (dy * P->porosity);
+    double* cnew = scratch + NOALLOC_FIELD_OFFSET;
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(scratch, &dt, sizeof(double), cudaMemcpyHostToDevice, s));
+    dim3 g((N2 + TJ - 1) / TJ, (N1 + TI - 1) / TI);
+    const bool per = P->bc == IMPEC_BC_PERIODIC;
+    if (P->hmtype == IMPEC_MUSCL) {
+        if (per) k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_PERIODIC><<<g, FUSED_THREADS, 0, s>>>(N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
+        else k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_NEUMANN><<<g, FUSED_THREADS, 0, s>>>(N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
+    } else {
+        if (per) k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC><<<g, FUSED_THREADS, 0, s>>>(N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
+        else k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN><<<g, FUSED_THREADS, 0, s>>>(N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
+    }
+    IMPEC_LAUNCH_CHECK();
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(c_dev, cnew, (size_t)N1 * N2 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return IMPEC_OK;
+}

@@ -172,6 +172,22 @@ impec_status impec_launch_count(impec_ctx* ctx, long long* n);
 impec_status impec_time_kernel(impec_ctx* ctx, int which, int reps, double* ms_per_launch,
                                double* bytes_per_launch);
 
+/* Allocation-free transport step.  No counterpart in the reference: it exists for callers
+ * that may not allocate device memory themselves or through this library -- code running
+ * under a host framework that owns every device allocation (a fixed pool or budget), or that
+ * must avoid cudaMalloc's implicit device-wide synchronisation -- and so cannot create an
+ * impec_ctx.  It performs AdvectSplit's symmetric-parallel update (MUSCL or upwind by
+ * P->hmtype, Neumann or periodic by P->bc) of c_dev in place, given u_dev, v_dev and dt,
+ * enqueued on `stream` (may be NULL), without allocating: its scratch (a copy of dt and the
+ * updated field) is a static device array of 1,048,576 cells (8 MiB) that every GPU which
+ * loads the library holds until process exit.  Nothing in it has to start at zero: each call
+ * writes dt and every cell of the updated field before reading them.  Larger grids
+ * (N1*N2 > 1,048,576) are rejected with IMPEC_ERR_ARG.  The first call on a device looks up the array's device address, so make
+ * that first call before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU (different streams, or different host threads) race on it. */
+impec_status impec_advect_symmetric_noalloc(const impec_params* P, double* c_dev, const double* u_dev,
+                                            const double* v_dev, double dt, void* stream);
+
 /* ---- host-buffer entry points (reference Blitz layouts; copies inside the call) ---- */
 impec_status impec_state_upload(impec_ctx* ctx, const double* c_host, const double* q_host,
                                 int ghost);
