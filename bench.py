@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch each kernel on the stream instead of replaying the step graph (for ncu)")
     return ap.parse_args()
 
 
@@ -167,6 +169,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.no_graph:
+        os.environ["IMPEC_NO_GRAPH"] = "1"  # read by the engine at each step
     import numpy as np
     import torch
 

@@ -102,6 +102,7 @@ _SIGS = {
     "impec_pressure_solve_resident": (C.c_int, [_VP, C.c_int, _PI, _PD]),
     "impec_advect_symmetric_noalloc": (C.c_int, [C.POINTER(Params), _VP, _VP, _VP, C.c_double, _VP]),
     "impec_time_kernel": (C.c_int, [_VP, C.c_int, C.c_int, _PD, _PD]),
+    "impec_measure_fp64": (C.c_int, [_PD]),
 }
 
 KERNELS = {0: "k_rb_face5<double> (fine RB-GS sweep, FP64)", 1: "k_rb_face5<float> (fine RB-GS sweep, FP32)",
@@ -114,15 +115,29 @@ def launch_count(ctx) -> int:
     return n.value
 
 
+def measure_fp64() -> float:
+    """FP64 fused multiply-adds per second of the current device (measured)."""
+    v = C.c_double()
+    _chk(lib().impec_measure_fp64(C.byref(v)), "measure_fp64")
+    return v.value
+
+
 def time_kernel(ctx, which: int, reps: int = 20):
     ms, b = C.c_double(), C.c_double()
     _chk(lib().impec_time_kernel(ctx.h, which, reps, C.byref(ms), C.byref(b)), "time_kernel")
     return ms.value, b.value
 
 
-def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None):
+# FP64 operations (FMA, MUL or ADD, one per lane) per cell of one launch of each probed kernel,
+# as the ncu instruction counts show them: the fine sweep is 4 DFMA + 1 DMUL per cell and colour.
+_FP64_OPS_PER_CELL = {0: 5.0, 2: 6.0}
+
+
+def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None, traffic_path: str | None = None):
     """Achieved bandwidth of the dominant kernel (CUDA events on its stream) against the
-    measured HBM copy bandwidth."""
+    measured HBM copy bandwidth, and its FP64 operation rate against the measured DFMA rate
+    of the device.  ``traffic`` (DRAM bytes per launch) comes from the ncu capture recorded in
+    profiles/traffic.json when that file names the kernel."""
     import json
     which = 1 if precision == "mixed" else 0
     ms, b = time_kernel(ctx, which)
@@ -134,8 +149,25 @@ def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None):
         except Exception:  # noqa: BLE001
             pass
     ach = b / (ms * 1e-3) / 1e9
-    return {"bound": "hbm", "kernel": KERNELS[which], "achieved": ach, "peak": peak, "unit": "GB/s",
-            "frac": ach / peak, "peak_source": src, "bytes_per_launch": b, "ms_per_launch": ms, "traffic": None}
+    out = {"bound": "hbm", "kernel": KERNELS[which], "achieved": ach, "peak": peak, "unit": "GB/s",
+           "frac": ach / peak, "peak_source": src, "bytes_per_launch": b, "ms_per_launch": ms, "traffic": None}
+    tpath = traffic_path or os.path.join(os.path.dirname(HERE), "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            t = json.load(open(tpath)).get(KERNELS[which].split(" ")[0])
+            if t:
+                out["traffic"] = float(t["dram_bytes_per_launch"])
+                out["traffic_source"] = t["source"]
+        except Exception:  # noqa: BLE001
+            pass
+    if which in _FP64_OPS_PER_CELL:
+        n = float(P.N1) * float(P.N2)
+        ops = _FP64_OPS_PER_CELL[which] * n
+        fma = measure_fp64()
+        out["fp64"] = {"achieved_ops_per_s": ops / (ms * 1e-3), "peak_ops_per_s": fma,
+                       "frac": ops / (ms * 1e-3) / fma, "ops_per_launch": ops,
+                       "peak_source": "measured (impec_measure_fp64: DFMA lanes per second)"}
+    return out
 
 
 def load_cfg(path: str):
@@ -195,6 +227,8 @@ def default_params(N1: int, N2: int, **kw) -> Params:
 def _p(t):
     if t is None:
         return None
+    if isinstance(t, int):  # raw device address (e.g. from Context.state_ptrs)
+        return C.c_void_p(t)
     import torch
     assert t.is_cuda and t.dtype == torch.float64 and t.is_contiguous(), "float64 contiguous CUDA tensor expected"
     return C.c_void_p(t.data_ptr())

@@ -27,6 +27,7 @@ struct PeaceArgs {
 // SetupDiffusionTensorG (src/MGSolver.cpp:886-919) at y-face (i,j): out (d22, d21)
 __global__ void k_peaceman(PeaceArgs A, const double* __restrict__ u, const double* __restrict__ v,
                            double* __restrict__ dfx, double* __restrict__ dfy) {
+    pdl_enter();
     int j = blockIdx.x * DBX + threadIdx.x, i = blockIdx.y * DBY + threadIdx.y;
     const int n1 = A.n1, n2 = A.n2;
     if (i <= n1 && j < n2) {
@@ -79,6 +80,7 @@ struct CNArgs {
 __global__ void k_cn_matrix(CNArgs A, const double* __restrict__ dfx, const double* __restrict__ dfy,
                             const double* __restrict__ dt_dev, double scale, double* __restrict__ a9,
                             double* __restrict__ idiag) {
+    pdl_enter();
     int j = blockIdx.x * DBX + threadIdx.x, i = blockIdx.y * DBY + threadIdx.y;
     const int n1 = A.n1, n2 = A.n2;
     if (i >= n1 || j >= n2) return;
@@ -118,6 +120,7 @@ __global__ void k_cn_matrix(CNArgs A, const double* __restrict__ dfx, const doub
 __global__ void k_cn_rhs(CNArgs A, const double* __restrict__ dfx, const double* __restrict__ dfy,
                          const double* __restrict__ c, const double* __restrict__ dt_dev, double scale,
                          double* __restrict__ rhs) {
+    pdl_enter();
     int j = blockIdx.x * DBX + threadIdx.x, i = blockIdx.y * DBY + threadIdx.y;
     const int n1 = A.n1, n2 = A.n2;
     if (i >= n1 || j >= n2) return;
@@ -150,29 +153,42 @@ __device__ __forceinline__ double cn_off(int i, int j, int n1, int n2, const dou
     return s;
 }
 
+// One colour (i parity ci, j parity cj) of a four-colour Gauss-Seidel sweep.  Each thread
+// updates two cells of the colour, 2 * DBY rows apart, with all loads issued before either
+// update (the cells of one colour do not couple).
 __global__ void k_cn_gs(int n1, int n2, const double* __restrict__ a9, const double* __restrict__ idiag,
                         const double* __restrict__ b, double* __restrict__ x, int ci, int cj) {
-    int j = 2 * (blockIdx.x * DBX + threadIdx.x) + cj, i = 2 * (blockIdx.y * DBY + threadIdx.y) + ci;
-    if (i >= n1 || j >= n2) return;
-    x[IX(i, j, n2)] = (b[IX(i, j, n2)] - cn_off(i, j, n1, n2, a9, x)) * idiag[IX(i, j, n2)];
+    pdl_enter();
+    const int j = 2 * (blockIdx.x * DBX + threadIdx.x) + cj, i0 = 2 * (blockIdx.y * 2 * DBY + threadIdx.y) + ci;
+    double v[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int i = i0 + 2 * DBY * r;
+        if (i < n1 && j < n2) v[r] = (b[IX(i, j, n2)] - cn_off(i, j, n1, n2, a9, x)) * idiag[IX(i, j, n2)];
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int i = i0 + 2 * DBY * r;
+        if (i < n1 && j < n2) x[IX(i, j, n2)] = v[r];
+    }
 }
 
 // ||b - A x||^2 and ||b||^2 into out[0], out[1]
 __global__ void __launch_bounds__(RED_THREADS) k_cn_resid(int n1, int n2, const double* __restrict__ a9,
                                                           const double* __restrict__ b, const double* __restrict__ x,
                                                           double* partials, int mb, unsigned* counter, double* out) {
+    pdl_enter();
     double acc[2] = {0.0, 0.0};
-    const size_t n = (size_t)n1 * n2;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-        int i = (int)(k / n2), j = (int)(k % n2);
+    for_cells(n1, n2, [&](int i, int j, size_t k) {
         double r = b[k] - (a9[k] * x[k] + cn_off(i, j, n1, n2, a9, x));
         acc[0] += r * r;
         acc[1] += b[k] * b[k];
-    }
+    });
     grid_reduce<2>(acc, 0u, partials, mb, counter, out);
 }
 
 __global__ void k_cn_check(DevScalars* S, double tol, int max_its, int inc, cudaGraphConditionalHandle h, int use_h) {
+    pdl_enter();
     if (inc) { S->cn_cycles++; S->cn_cycles_total++; }
     double bn = S->red[3], rn = S->red[2];
     double rr = bn > 0 ? sqrt(rn / bn) : sqrt(rn);
@@ -200,18 +216,19 @@ impec_status cn_setup(impec_ctx* ctx, const double* u, const double* v, double d
     PeaceArgs pa{n1, n2, P.porosity, P.alpha_l * maxdx, P.alpha_t * maxdx, P.porosity * P.Dm, P.peaceman_guard};
     dim3 b(DBX, DBY);
     ++ctx->nlaunch;
-    k_peaceman<<<dim3((n2 + 1 + DBX - 1) / DBX, (n1 + 1 + DBY - 1) / DBY), b, 0, ctx->stream>>>(pa, u, v, ctx->dfx,
+    launch_k(ctx->stream, k_peaceman, dim3((n2 + 1 + DBX - 1) / DBX, (n1 + 1 + DBY - 1) / DBY), b, 0, pa, u, v, ctx->dfx,
                                                                                                  ctx->dfy);
     ++ctx->nlaunch;
-    k_cn_matrix<<<dim3((n2 + DBX - 1) / DBX, (n1 + DBY - 1) / DBY), b, 0, ctx->stream>>>(
+    launch_k(ctx->stream, k_cn_matrix, dim3((n2 + DBX - 1) / DBX, (n1 + DBY - 1) / DBY), b, 0, 
         cn_args(ctx), ctx->dfx, ctx->dfy, dt_dev, dt_scale, ctx->cn_a9, ctx->cn_idiag);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
 
 impec_status cn_residual(impec_ctx* ctx, const double* c) {
+    const int cap = red_cap(ctx->num_sms, ctx->max_blocks);
     ++ctx->nlaunch;
-    k_cn_resid<<<ctx->num_sms * 2, RED_THREADS, 0, ctx->stream>>>(ctx->P.N1, ctx->P.N2, ctx->cn_a9, ctx->cn_b, c,
+    launch_k(ctx->stream, k_cn_resid, seg_blocks(ctx->P.N1, ctx->P.N2, cap), RED_THREADS, 0, ctx->P.N1, ctx->P.N2, ctx->cn_a9, ctx->cn_b, c,
                                                                    ctx->partials, ctx->max_blocks, ctx->counter,
                                                                    ctx->dscal->red + 2);
     IMPEC_LAUNCH_CHECK();
@@ -222,7 +239,7 @@ impec_status cn_residual(impec_ctx* ctx, const double* c) {
 impec_status cn_prepare(impec_ctx* ctx, const double* c, double dt_scale, const double* dt_dev) {
     const int n1 = ctx->P.N1, n2 = ctx->P.N2;
     ++ctx->nlaunch;
-    k_cn_rhs<<<dim3((n2 + DBX - 1) / DBX, (n1 + DBY - 1) / DBY), dim3(DBX, DBY), 0, ctx->stream>>>(
+    launch_k(ctx->stream, k_cn_rhs, dim3((n2 + DBX - 1) / DBX, (n1 + DBY - 1) / DBY), dim3(DBX, DBY), 0, 
         cn_args(ctx), ctx->dfx, ctx->dfy, c, dt_dev, dt_scale, ctx->cn_b);
     IMPEC_LAUNCH_CHECK();
     IMPEC_CUDA_TRY(cudaMemsetAsync(&ctx->dscal->cn_cycles, 0, sizeof(int), ctx->stream));
@@ -231,7 +248,7 @@ impec_status cn_prepare(impec_ctx* ctx, const double* c, double dt_scale, const 
 
 impec_status cn_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h) {
     ++ctx->nlaunch;
-    k_cn_check<<<1, 1, 0, ctx->stream>>>(ctx->dscal, tol, ctx->P.max_cycles, inc, h, use_h);
+    launch_k(ctx->stream, k_cn_check, 1, 1, 0, ctx->dscal, tol, ctx->P.max_cycles, inc, h, use_h);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -240,10 +257,10 @@ impec_status cn_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalH
 // iteration count differs) followed by the new residual (launch only).
 impec_status cn_iteration(impec_ctx* ctx, double* c) {
     const int n1 = ctx->P.N1, n2 = ctx->P.N2;
-    dim3 g4(((n2 + 1) / 2 + DBX - 1) / DBX, ((n1 + 1) / 2 + DBY - 1) / DBY);
+    dim3 g4(((n2 + 1) / 2 + DBX - 1) / DBX, ((n1 + 1) / 2 + 2 * DBY - 1) / (2 * DBY));
     for (int col = 0; col < 4; ++col) {
         ++ctx->nlaunch;
-        k_cn_gs<<<g4, dim3(DBX, DBY), 0, ctx->stream>>>(n1, n2, ctx->cn_a9, ctx->cn_idiag, ctx->cn_b, c, col >> 1,
+        launch_k(ctx->stream, k_cn_gs, g4, dim3(DBX, DBY), 0, n1, n2, ctx->cn_a9, ctx->cn_idiag, ctx->cn_b, c, col >> 1,
                                                        col & 1);
     }
     IMPEC_LAUNCH_CHECK();

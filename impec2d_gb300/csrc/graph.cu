@@ -14,6 +14,7 @@
 namespace impec {
 
 __global__ void k_step_begin(DevScalars* S) {
+    pdl_enter();
     S->flags = 0;
     S->cn_cycles_total = 0;
     S->clipped = 0;
@@ -21,6 +22,7 @@ __global__ void k_step_begin(DevScalars* S) {
 
 // Output-time matching (src/Impec2DSolver.cpp:375-378) on the device.
 __global__ void k_clip_dt(DevScalars* S) {
+    pdl_enter();
     if (S->t_clip >= 0 && S->t + S->dt >= S->t_clip) {
         S->dt = S->t_clip - S->t;
         S->clipped = 1;
@@ -30,6 +32,7 @@ __global__ void k_clip_dt(DevScalars* S) {
 // Advances the clock and counts the kernels this replay executed: the fixed nodes plus the
 // loop bodies times their trip counts.
 __global__ void k_advance(DevScalars* S, long long outer, long long mg_body, long long cn_body) {
+    pdl_enter();
     S->t += S->dt;
     S->steps++;
     S->graph_launches += outer + mg_body * S->mg_cycles + cn_body * S->cn_cycles_total;
@@ -107,7 +110,7 @@ static impec_status capture_step(impec_ctx* ctx, int pfs_in, cudaGraph_t* out) {
     long long mg_body = 0;
     auto body = [&]() -> impec_status {
         ++ctx->nlaunch;
-        k_step_begin<<<1, 1, 0, ctx->stream>>>(S);
+        launch_k(ctx->stream, k_step_begin, 1, 1, 0, S);
         IMPEC_TRY(pressure_prepare(ctx, ctx->c, ctx->p));
         IMPEC_TRY(capture_while(
             ctx, [&](cudaGraphConditionalHandle h) { return pressure_check(ctx, P.eps, 0, h, 1); },
@@ -120,7 +123,7 @@ static impec_status capture_step(impec_ctx* ctx, int pfs_in, cudaGraph_t* out) {
         IMPEC_TRY(velocity(ctx, ctx->p, ctx->c, ctx->u, ctx->v));
         IMPEC_TRY(max_stable_dt_dev(ctx, ctx->u, ctx->v));
         ++ctx->nlaunch;
-        k_clip_dt<<<1, 1, 0, ctx->stream>>>(S);
+        launch_k(ctx->stream, k_clip_dt, 1, 1, 0, S);
         // HyperbolicSplitSolver::Solve (src/HyperbolicSplitSolver.cpp:162-198)
         IMPEC_TRY(tr_integrate_dev(ctx, ctx->c, 0.5, dt, 0));
         if (P.diffusion) {
@@ -133,7 +136,7 @@ static impec_status capture_step(impec_ctx* ctx, int pfs_in, cudaGraph_t* out) {
         if (P.diffusion) IMPEC_TRY(capture_cn_solve(ctx, ctx->c));
         ++ctx->nlaunch;
         const long long loops = mg_body + (P.diffusion ? 2 * ctx->step_cn_body_launches : 0);
-        k_advance<<<1, 1, 0, ctx->stream>>>(S, ctx->nlaunch - n0 - loops, mg_body,
+        launch_k(ctx->stream, k_advance, 1, 1, 0, S, ctx->nlaunch - n0 - loops, mg_body,
                                             P.diffusion ? ctx->step_cn_body_launches : 0);
         IMPEC_LAUNCH_CHECK();
         return IMPEC_OK;
@@ -220,7 +223,7 @@ void invalidate_step_graph(impec_ctx* ctx) {
 static impec_status step_stream(impec_ctx* ctx, double t_clip) {
     DevScalars* S = ctx->dscal;
     ++ctx->nlaunch;
-    k_step_begin<<<1, 1, 0, ctx->stream>>>(S);
+    launch_k(ctx->stream, k_step_begin, 1, 1, 0, S);
     int cyc = 0;
     double rr = 0;
     impec_status st = pressure_solve(ctx, ctx->c, ctx->p, ctx->P.eps, &cyc, &rr);
@@ -229,10 +232,10 @@ static impec_status step_stream(impec_ctx* ctx, double t_clip) {
     IMPEC_TRY(max_stable_dt_dev(ctx, ctx->u, ctx->v));
     IMPEC_CUDA_TRY(cudaMemcpyAsync(&S->t_clip, &t_clip, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     ++ctx->nlaunch;
-    k_clip_dt<<<1, 1, 0, ctx->stream>>>(S);
+    launch_k(ctx->stream, k_clip_dt, 1, 1, 0, S);
     IMPEC_TRY(hyperbolic_solve_dev(ctx, ctx->c, ctx->u, ctx->v, &S->dt, &ctx->prev_first_sweep));
     ++ctx->nlaunch;
-    k_advance<<<1, 1, 0, ctx->stream>>>(S, 0, 0, 0);
+    launch_k(ctx->stream, k_advance, 1, 1, 0, S, 0, 0, 0);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/impec2d.h"
@@ -60,13 +61,44 @@ struct Level {
     double* ty = nullptr;    // FACE5: n1*(n2+1)
     double* a9 = nullptr;    // EXP9: 9 planes of n1*n2, folded (no coupling outside the grid)
     double* idiag = nullptr; // 1 / diagonal
+    double* diag = nullptr;  // diagonal (FACE5: sum of the four faces; EXP9: plane 0)
     double *x = nullptr, *b = nullptr;
     // FP32 copies for the mixed-precision cycle
-    float *tx32 = nullptr, *ty32 = nullptr, *a932 = nullptr, *idiag32 = nullptr;
+    float *tx32 = nullptr, *ty32 = nullptr, *a932 = nullptr, *idiag32 = nullptr, *diag32 = nullptr;
     float *x32 = nullptr, *b32 = nullptr;
 };
 
 enum { FLAG_MG_NOT_CONVERGED = 1, FLAG_MG_NAN = 2, FLAG_CN_NOT_CONVERGED = 4, FLAG_CN_NAN = 8 };
+
+// ---- programmatic dependent launch
+// Every kernel of the engine starts with pdl_enter(): it waits until the kernel before it in
+// the stream has completed and its writes are visible (griddepcontrol.wait), then allows the
+// next kernel's CTAs to be scheduled (griddepcontrol.launch_dependents), so the next launch's
+// latency overlaps this kernel's run.  Since each kernel waits for its predecessor before
+// touching memory, a kernel also sees the writes of every earlier kernel in the stream.
+// Both instructions do nothing in a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+bool pdl_enabled();  // programmatic launches only with IMPEC_PDL=1
+
+// kernel<<<g, b, smem, s>>>(args...) with the programmatic-serialisation attribute.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(cudaStream_t s, void (*k)(KArgs...), dim3 g, dim3 b, size_t smem, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // Device-resident scalars of a step (so a step needs no host round trip).
 struct DevScalars {
@@ -85,6 +117,7 @@ struct impec_ctx {
     impec::Geo G;
     cudaStream_t stream = nullptr;
     int device = 0, num_sms = 148;
+    int cl_size = 0;  // CTAs per cluster of the cluster V-cycle (0: cluster launches unavailable)
     // resident state
     double *c = nullptr, *p = nullptr, *u = nullptr, *v = nullptr, *q = nullptr;
     double *K11 = nullptr, *K22 = nullptr;  // owned copies, or nullptr (K = 1)

@@ -21,6 +21,7 @@ struct CoarseArgs {
     const T* ty[MGC_MAXL];
     const T* a9[MGC_MAXL];
     const T* id[MGC_MAXL];
+    const T* dg[MGC_MAXL];  // diagonals (FACE5; EXP9 uses plane 0 of a9)
     T* x0;           // iterate of the first handled level (global)
     const T* b0;     // its right-hand side (global)
     const double* dinv;
@@ -60,41 +61,43 @@ __device__ void cv_smooth(int n1, int n2, const T* tx, const T* ty, const T* a9,
     }
 }
 
+// Same arithmetic as resid() of the level kernels: s = b + sum t * x_nb (or b - sum a_e * x_nb),
+// r = s - diag * x.
 template <class T, int KIND>
-__device__ __forceinline__ T cv_resid(int i, int j, int n1, int n2, const T* tx, const T* ty, const T* a9, const T* b,
-                                      const T* x) {
+__device__ __forceinline__ T cv_resid(int i, int j, int n1, int n2, const T* tx, const T* ty, const T* a9, const T* dg,
+                                      const T* b, const T* x) {
+    const int k = IX(i, j, n2);
+    T s = b[k];
     if (KIND == FACE5) {
-        T tw = tx[IX(i, j, n2)], te = tx[IX(i + 1, j, n2)], ts = ty[IX(i, j, n2 + 1)], tn = ty[IX(i, j + 1, n2 + 1)];
-        T s = 0;
-        if (i > 0) s += tw * x[IX(i - 1, j, n2)];
-        if (i < n1 - 1) s += te * x[IX(i + 1, j, n2)];
-        if (j > 0) s += ts * x[IX(i, j - 1, n2)];
-        if (j < n2 - 1) s += tn * x[IX(i, j + 1, n2)];
-        T diag = tw + te + ts + tn;
-        return b[IX(i, j, n2)] - (diag * x[IX(i, j, n2)] - s);
+        if (i > 0) s += tx[k] * x[k - n2];
+        if (i < n1 - 1) s += tx[k + n2] * x[k + n2];
+        if (j > 0) s += ty[IX(i, j, n2 + 1)] * x[k - 1];
+        if (j < n2 - 1) s += ty[IX(i, j + 1, n2 + 1)] * x[k + 1];
+        return s - dg[k] * x[k];
     }
-    const int n = n1 * n2, k = IX(i, j, n2);
-    T s = 0;
+    const int n = n1 * n2;
     for (int e = 1; e < 9; ++e) {
         int ii = i + c_off[e][0], jj = j + c_off[e][1];
         if (ii < 0 || ii >= n1 || jj < 0 || jj >= n2) continue;
-        s += a9[e * n + k] * x[IX(ii, jj, n2)];
+        s -= a9[e * n + k] * x[IX(ii, jj, n2)];
     }
-    return b[k] - (a9[k] * x[k] + s);
+    return s - a9[k] * x[k];
 }
 
 template <class T, int KIND>
 __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char cv_raw[];
     T* sm = reinterpret_cast<T*>(cv_raw);
-    T *tx[MGC_MAXL], *ty[MGC_MAXL], *a9[MGC_MAXL], *id[MGC_MAXL], *x[MGC_MAXL], *b[MGC_MAXL];
+    T *tx[MGC_MAXL], *ty[MGC_MAXL], *a9[MGC_MAXL], *id[MGC_MAXL], *dg[MGC_MAXL], *x[MGC_MAXL], *b[MGC_MAXL];
     size_t off = 0;
     for (int l = 0; l < A.nl; ++l) {
         const int n1 = A.n1[l], n2 = A.n2[l], n = n1 * n2;
-        tx[l] = ty[l] = a9[l] = nullptr;
+        tx[l] = ty[l] = a9[l] = dg[l] = nullptr;
         if (KIND == FACE5) {
             tx[l] = sm + off; off += (size_t)(n1 + 1) * n2;
             ty[l] = sm + off; off += (size_t)n1 * (n2 + 1);
+            dg[l] = sm + off; off += n;
         } else {
             a9[l] = sm + off; off += (size_t)9 * n;
         }
@@ -107,6 +110,7 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
         if (KIND == FACE5) {
             for (int k = threadIdx.x; k < (n1 + 1) * n2; k += blockDim.x) tx[l][k] = A.tx[l][k];
             for (int k = threadIdx.x; k < n1 * (n2 + 1); k += blockDim.x) ty[l][k] = A.ty[l][k];
+            for (int k = threadIdx.x; k < n; k += blockDim.x) dg[l][k] = A.dg[l][k];
         } else {
             for (int k = threadIdx.x; k < 9 * n; k += blockDim.x) a9[l][k] = A.a9[l][k];
         }
@@ -127,7 +131,7 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
             for (int a = 0; a < 2; ++a)
                 for (int bb = 0; bb < 2; ++bb) {
                     int i = 2 * I + a, j = 2 * J + bb;
-                    if (i < n1 && j < n2) s += cv_resid<T, KIND>(i, j, n1, n2, tx[l], ty[l], a9[l], b[l], x[l]);
+                    if (i < n1 && j < n2) s += cv_resid<T, KIND>(i, j, n1, n2, tx[l], ty[l], a9[l], dg[l], b[l], x[l]);
                 }
             b[l + 1][K] = s;
             x[l + 1][K] = 0;
@@ -172,9 +176,12 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
             if (I2 < 0 || I2 >= c1) I2 = I;
             if (J2 < 0 || J2 >= c2) J2 = J;
             const T* xc = x[l + 1];
-            T e = T(0.5625) * xc[IX(I, J, c2)] + T(0.1875) * xc[IX(I2, J, c2)] + T(0.1875) * xc[IX(I, J2, c2)] +
-                  T(0.0625) * xc[IX(I2, J2, c2)];
-            x[l][k] += e;
+            T v = x[l][k];
+            v += T(0.5625) * xc[IX(I, J, c2)];
+            v += T(0.1875) * xc[IX(I2, J, c2)];
+            v += T(0.1875) * xc[IX(I, J2, c2)];
+            v += T(0.0625) * xc[IX(I2, J2, c2)];
+            x[l][k] = v;
         }
         __syncthreads();
         cv_smooth<T, KIND>(n1, n2, tx[l], ty[l], a9[l], id[l], b[l], x[l], true);
@@ -239,6 +246,7 @@ __global__ void __launch_bounds__(TBT) k_level_pre(int n1, int n2, const T* __re
                                                    const T* __restrict__ gid, const T* __restrict__ gb,
                                                    T* __restrict__ gx, int c2, T* __restrict__ bc,
                                                    T* __restrict__ xc, int nc1) {
+    pdl_enter();
     constexpr int H = TBH_PRE, R = TB + 2 * H;
     extern __shared__ __align__(16) unsigned char tb_raw[];
     T* x = reinterpret_cast<T*>(tb_raw);
@@ -283,6 +291,7 @@ __global__ void __launch_bounds__(TBT) k_level_post(int n1, int n2, const T* __r
                                                     const T* __restrict__ gty, const T* __restrict__ gid,
                                                     const T* __restrict__ gb, T* __restrict__ gx, int c1, int c2,
                                                     const T* __restrict__ xc) {
+    pdl_enter();
     constexpr int H = TBH_POST, R = TB + 2 * H;
     extern __shared__ __align__(16) unsigned char tb_raw[];
     T* x = reinterpret_cast<T*>(tb_raw);

@@ -13,6 +13,8 @@
 // Internally the operator is stored in integrated form with positive diagonal:
 // A_int = -dA * A_ref, f = dA * q, so that ||f - A_int x|| / ||f|| equals the reference's
 // relative residual ||b - A x|| / ||b||.
+#include <cooperative_groups.h>
+
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -26,12 +28,19 @@ constexpr int BX = 32, BY = 8;
 static inline dim3 grid2(int n1, int n2) { return dim3((n2 + BX - 1) / BX, (n1 + BY - 1) / BY); }
 #define IX(i, j, n2) ((size_t)(i) * (n2) + (j))
 
+// Tuning switches read from the environment (defaults are the measured best on GB300).
+static long env_long(const char* name, long dflt) {
+    const char* e = getenv(name);
+    return e && *e ? strtol(e, nullptr, 10) : dflt;
+}
+
 // ---------------------------------------------------------------- mobility
 // Cell value w = mu/K (harmonic averaging) or K/mu (arithmetic averaging), where
 // mu(c) = 1/(x^4) * mu_res, x = 1 - c + M^(1/4) c   (src/EllipticSolver.cpp:692-695).
 __global__ void k_cell_w(int n1, int n2, const double* __restrict__ c, const double* __restrict__ K1,
                          const double* __restrict__ K2, double m14, double mu_res, int harmonic,
                          double* __restrict__ w1, double* __restrict__ w2) {
+    pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i >= n1 || j >= n2) return;
     size_t k = IX(i, j, n2);
@@ -50,6 +59,7 @@ __global__ void k_cell_w(int n1, int n2, const double* __restrict__ c, const dou
 // neighbours outside the grid mirrored (FillGhostCellsNeumannScalar).
 __global__ void k_face_lam(int n1, int n2, const double* __restrict__ w1, const double* __restrict__ w2,
                            int harmonic, double* __restrict__ lamx, double* __restrict__ lamy) {
+    pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i <= n1 && j < n2) {  // x-face between cells (i-1,j) and (i,j)
         double a = w1[IX(refl_cell(i - 1, n1), j, n2)], b = w1[IX(refl_cell(i, n1), j, n2)];
@@ -68,6 +78,7 @@ __global__ void k_face_lam(int n1, int n2, const double* __restrict__ w1, const 
 __global__ void k_corner(int n1, int n2, const double* __restrict__ w1, const double* __restrict__ w2,
                          int harmonic, Geo G, double* __restrict__ m11, double* __restrict__ m22,
                          double* __restrict__ m12) {
+    pdl_enter();
     int cj = blockIdx.x * BX + threadIdx.x, ci = blockIdx.y * BY + threadIdx.y;
     if (ci > n1 || cj > n2) return;
     const int i = ci - 1, j = cj - 1;  // reference corner (i+1/2, j+1/2)
@@ -87,6 +98,7 @@ __global__ void k_corner(int n1, int n2, const double* __restrict__ w1, const do
 // nu = 1: face transmissibilities dA/dx^2 * lambda with zero flux through the boundary.
 __global__ void k_face5_fine(int n1, int n2, const double* __restrict__ lamx, const double* __restrict__ lamy,
                              double sx, double sy, double* __restrict__ tx, double* __restrict__ ty) {
+    pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i <= n1 && j < n2) tx[IX(i, j, n2)] = (i == 0 || i == n1) ? 0.0 : lamx[IX(i, j, n2)] * sx;
     if (i < n1 && j <= n2) ty[IX(i, j, n2 + 1)] = (j == 0 || j == n2) ? 0.0 : lamy[IX(i, j, n2 + 1)] * sy;
@@ -140,6 +152,7 @@ __device__ void ref_row(int i, int j, int n1, int n2, const double* __restrict__
 __global__ void k_exp9_fine(int n1, int n2, const double* __restrict__ lamx, const double* __restrict__ lamy,
                             const double* __restrict__ m11, const double* __restrict__ m22,
                             const double* __restrict__ m12, double nu, Geo G, double* __restrict__ a9) {
+    pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i >= n1 || j >= n2) return;
     double o[9];
@@ -154,6 +167,7 @@ __constant__ int c_off[9][2] = {{0, 0}, {-1, 0}, {-1, -1}, {0, -1}, {1, -1}, {1,
 // ---------------------------------------------------------------- coarse operators
 __global__ void k_face5_coarsen(int n1f, int n2f, const double* __restrict__ txf, const double* __restrict__ tyf,
                                 int n1c, int n2c, double* __restrict__ txc, double* __restrict__ tyc) {
+    pdl_enter();
     int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
     if (I <= n1c && J < n2c) {
         int fi = 2 * I;
@@ -177,6 +191,7 @@ __global__ void k_face5_coarsen(int n1f, int n2f, const double* __restrict__ txf
 
 __global__ void k_exp9_coarsen(int n1f, int n2f, const double* __restrict__ af, int n1c, int n2c,
                                double* __restrict__ ac) {
+    pdl_enter();
     int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
     if (I >= n1c || J >= n2c) return;
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -201,7 +216,8 @@ __global__ void k_exp9_coarsen(int n1f, int n2f, const double* __restrict__ af, 
 }
 
 __global__ void k_idiag(int n1, int n2, int kind, const double* __restrict__ tx, const double* __restrict__ ty,
-                        const double* __restrict__ a9, double* __restrict__ idiag) {
+                        const double* __restrict__ a9, double* __restrict__ diag, double* __restrict__ idiag) {
+    pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i >= n1 || j >= n2) return;
     double d;
@@ -209,10 +225,12 @@ __global__ void k_idiag(int n1, int n2, int kind, const double* __restrict__ tx,
         d = tx[IX(i, j, n2)] + tx[IX(i + 1, j, n2)] + ty[IX(i, j, n2 + 1)] + ty[IX(i, j + 1, n2 + 1)];
     else
         d = a9[IX(i, j, n2)];
+    diag[IX(i, j, n2)] = d;
     idiag[IX(i, j, n2)] = d != 0.0 ? 1.0 / d : 0.0;
 }
 
 __global__ void k_to_float(size_t n, const double* __restrict__ a, float* __restrict__ b) {
+    pdl_enter();
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
         b[k] = (float)a[k];
 }
@@ -247,23 +265,39 @@ __device__ __forceinline__ T offsum_exp9(int i, int j, int n1, int n2, const T* 
 }
 
 // ---------------------------------------------------------------- smoothers
+// One colour of a red-black sweep.  Each thread updates two cells of the colour, RB_ROWS * BY /
+// 2 rows apart, with all loads issued before either update: the FP64 pipe, not load latency,
+// then sets the pace.  The arithmetic per cell is s = b + sum t * x_nb, x = s * idiag.
+constexpr int RB_ROWS = 2;
+
 template <class T>
 __global__ void k_rb_face5(int n1, int n2, const T* __restrict__ tx, const T* __restrict__ ty,
                            const T* __restrict__ idiag, const T* __restrict__ b, T* __restrict__ x, int color) {
-    int jj = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
-    int j = 2 * jj + ((i + color) & 1);
-    if (i >= n1 || j >= n2) return;
-    T s = b[IX(i, j, n2)];
-    if (i > 0) s += tx[IX(i, j, n2)] * x[IX(i - 1, j, n2)];
-    if (i < n1 - 1) s += tx[IX(i + 1, j, n2)] * x[IX(i + 1, j, n2)];
-    if (j > 0) s += ty[IX(i, j, n2 + 1)] * x[IX(i, j - 1, n2)];
-    if (j < n2 - 1) s += ty[IX(i, j + 1, n2 + 1)] * x[IX(i, j + 1, n2)];
-    x[IX(i, j, n2)] = s * idiag[IX(i, j, n2)];
+    pdl_enter();
+    const int jj = blockIdx.x * BX + threadIdx.x, i0 = blockIdx.y * (RB_ROWS * BY) + threadIdx.y;
+    T v[RB_ROWS];
+#pragma unroll
+    for (int r = 0; r < RB_ROWS; ++r) {
+        const int i = i0 + r * BY, j = 2 * jj + ((i + color) & 1);
+        if (i >= n1 || j >= n2) continue;
+        T s = b[IX(i, j, n2)];
+        if (i > 0) s += tx[IX(i, j, n2)] * x[IX(i - 1, j, n2)];
+        if (i < n1 - 1) s += tx[IX(i + 1, j, n2)] * x[IX(i + 1, j, n2)];
+        if (j > 0) s += ty[IX(i, j, n2 + 1)] * x[IX(i, j - 1, n2)];
+        if (j < n2 - 1) s += ty[IX(i, j + 1, n2 + 1)] * x[IX(i, j + 1, n2)];
+        v[r] = s * idiag[IX(i, j, n2)];
+    }
+#pragma unroll
+    for (int r = 0; r < RB_ROWS; ++r) {
+        const int i = i0 + r * BY, j = 2 * jj + ((i + color) & 1);
+        if (i < n1 && j < n2) x[IX(i, j, n2)] = v[r];
+    }
 }
 
 template <class T>
 __global__ void k_gs4_exp9(int n1, int n2, const T* __restrict__ a9, const T* __restrict__ idiag,
                            const T* __restrict__ b, T* __restrict__ x, int ci, int cj) {
+    pdl_enter();
     int j = 2 * (blockIdx.x * BX + threadIdx.x) + cj, i = 2 * (blockIdx.y * BY + threadIdx.y) + ci;
     if (i >= n1 || j >= n2) return;
     T s = b[IX(i, j, n2)] - offsum_exp9<T>(i, j, n1, n2, a9, x);
@@ -271,28 +305,45 @@ __global__ void k_gs4_exp9(int n1, int n2, const T* __restrict__ a9, const T* __
 }
 
 // ---------------------------------------------------------------- transfers
+// r = b - A x at (i, j) as one accumulation: s = b + sum t * x_nb (FACE5) or
+// b - sum a_e * x_nb (EXP9), then r = s - diag * x.
 template <class T>
-__device__ __forceinline__ T resid(const Level& Lv, int i, int j, const T* tx, const T* ty, const T* a9,
-                                   const T* b, const T* x) {
+__device__ __forceinline__ T resid(const Level& Lv, int i, int j, const T* __restrict__ tx, const T* __restrict__ ty,
+                                   const T* __restrict__ a9, const T* __restrict__ dg, const T* __restrict__ b,
+                                   const T* __restrict__ x) {
+    const int n1 = Lv.n1, n2 = Lv.n2;
+    const size_t k = IX(i, j, n2);
+    T s = b[k];
     if (Lv.kind == FACE5) {
-        T d, o;
-        return b[IX(i, j, Lv.n2)] - apply_face5<T>(i, j, Lv.n1, Lv.n2, tx, ty, x, d, o);
+        if (i > 0) s += tx[k] * x[k - n2];
+        if (i < n1 - 1) s += tx[k + n2] * x[k + n2];
+        if (j > 0) s += ty[IX(i, j, n2 + 1)] * x[k - 1];
+        if (j < n2 - 1) s += ty[IX(i, j + 1, n2 + 1)] * x[k + 1];
+    } else {
+        const size_t n = (size_t)n1 * n2;
+#pragma unroll
+        for (int e = 1; e < 9; ++e) {
+            const int ii = i + c_off[e][0], jj = j + c_off[e][1];
+            if (ii < 0 || ii >= n1 || jj < 0 || jj >= n2) continue;
+            s -= a9[e * n + k] * x[IX(ii, jj, n2)];
+        }
     }
-    return b[IX(i, j, Lv.n2)] - (a9[IX(i, j, Lv.n2)] * x[IX(i, j, Lv.n2)] + offsum_exp9<T>(i, j, Lv.n1, Lv.n2, a9, x));
+    return s - dg[k] * x[k];
 }
 
 // Residual of the fine level summed over each 2x2 aggregate -> coarse rhs; coarse x := 0.
 template <class T>
 __global__ void k_restrict(Level F, const T* __restrict__ tx, const T* __restrict__ ty, const T* __restrict__ a9,
-                           const T* __restrict__ b, const T* __restrict__ x, int n1c, int n2c, T* __restrict__ bc,
-                           T* __restrict__ xc) {
+                           const T* __restrict__ dg, const T* __restrict__ b, const T* __restrict__ x, int n1c,
+                           int n2c, T* __restrict__ bc, T* __restrict__ xc) {
+    pdl_enter();
     int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
     if (I >= n1c || J >= n2c) return;
     T s = 0;
     for (int a = 0; a < 2; ++a)
         for (int bb = 0; bb < 2; ++bb) {
             int i = 2 * I + a, j = 2 * J + bb;
-            if (i < F.n1 && j < F.n2) s += resid<T>(F, i, j, tx, ty, a9, b, x);
+            if (i < F.n1 && j < F.n2) s += resid<T>(F, i, j, tx, ty, a9, dg, b, x);
         }
     bc[IX(I, J, n2c)] = s;
     xc[IX(I, J, n2c)] = 0;
@@ -302,20 +353,25 @@ __global__ void k_restrict(Level F, const T* __restrict__ tx, const T* __restric
 // neighbour is replaced by the cell itself), added to the fine iterate.
 template <class T>
 __global__ void k_prolong(int n1, int n2, T* __restrict__ x, int n1c, int n2c, const T* __restrict__ xc) {
+    pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i >= n1 || j >= n2) return;
     int I = i >> 1, J = j >> 1;
     int I2 = (i & 1) ? I + 1 : I - 1, J2 = (j & 1) ? J + 1 : J - 1;
     if (I2 < 0 || I2 >= n1c) I2 = I;
     if (J2 < 0 || J2 >= n2c) J2 = J;
-    T e = T(0.5625) * xc[IX(I, J, n2c)] + T(0.1875) * xc[IX(I2, J, n2c)] + T(0.1875) * xc[IX(I, J2, n2c)] +
-          T(0.0625) * xc[IX(I2, J2, n2c)];
-    x[IX(i, j, n2)] += e;
+    T v = x[IX(i, j, n2)];
+    v += T(0.5625) * xc[IX(I, J, n2c)];
+    v += T(0.1875) * xc[IX(I2, J, n2c)];
+    v += T(0.1875) * xc[IX(I, J2, n2c)];
+    v += T(0.0625) * xc[IX(I2, J2, n2c)];
+    x[IX(i, j, n2)] = v;
 }
 
 // ---------------------------------------------------------------- coarsest level (dense)
 __global__ void k_dense_build(Level C, const double* __restrict__ tx, const double* __restrict__ ty,
                               const double* __restrict__ a9, int singular, double* __restrict__ D) {
+    pdl_enter();
     const int n1 = C.n1, n2 = C.n2, n = n1 * n2;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         for (int cc = 0; cc < n; ++cc) D[(size_t)r * n + cc] = 0.0;
@@ -344,6 +400,7 @@ __global__ void k_dense_build(Level C, const double* __restrict__ tx, const doub
 
 // Gauss-Jordan inversion of an n x n (n <= 64) diagonally dominant matrix in shared memory.
 __global__ void k_dense_invert(int n, const double* __restrict__ D, double* __restrict__ Dinv) {
+    pdl_enter();
     extern __shared__ double sm[];
     double* A = sm;          // n x n
     double* B = sm + n * n;  // n x n
@@ -379,6 +436,7 @@ __global__ void k_dense_invert(int n, const double* __restrict__ D, double* __re
 template <class T>
 __global__ void k_dense_solve(int n, const double* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x,
                               int singular) {
+    pdl_enter();
     __shared__ double sb[64];
     __shared__ double sx[64];
     for (int k = threadIdx.x; k < n; k += blockDim.x) sb[k] = (singular && k == 0) ? 0.0 : (double)b[k];
@@ -410,15 +468,14 @@ __global__ void __launch_bounds__(RED_THREADS) k_fine_resid(Level F, const doubl
                                                             const double* __restrict__ x, int pin,
                                                             float* __restrict__ r32, double* partials, int mb,
                                                             unsigned* counter, double* out) {
+    pdl_enter();
     double acc[1] = {0.0};
-    const size_t n = F.n();
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-        int i = (int)(k / F.n2), j = (int)(k % F.n2);
-        double r = resid<double>(F, i, j, F.tx, F.ty, F.a9, f, x);
+    for_cells(F.n1, F.n2, [&](int i, int j, size_t k) {
+        double r = resid<double>(F, i, j, F.tx, F.ty, F.a9, F.diag, f, x);
         if (r32) r32[k] = (float)r;  // consistent rhs of the singular correction equation
         if ((int)k == pin) r = 0.0;  // the pinned row of the reference system has zero residual
         acc[0] += r * r;
-    }
+    });
     grid_reduce<1>(acc, 0u, partials, mb, counter, out);
 }
 
@@ -426,6 +483,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_fine_resid(Level F, const doubl
 __global__ void __launch_bounds__(RED_THREADS) k_rhs(size_t n, const double* __restrict__ q, double dA,
                                                      double* __restrict__ f, double* partials, int mb,
                                                      unsigned* counter, double* out) {
+    pdl_enter();
     double acc[2] = {0.0, 0.0};
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
         double v = dA * q[k];
@@ -439,17 +497,20 @@ __global__ void __launch_bounds__(RED_THREADS) k_rhs(size_t n, const double* __r
 // Consistent right-hand side and pinned value: f(pin) := -(sum f - f(pin));
 // p_pin = -q_pin dA / kappa  (pinned row kappa/dA p = -q, src/MGSolver.cpp:553-565).
 __global__ void k_fix_pin(double* f, const double* q, int pin, double dA, double kappa, DevScalars* S) {
+    pdl_enter();
     double fp = f[pin];
     S->pin_value = -q[pin] * dA / kappa;
     f[pin] = -(S->fsum - fp);
 }
 
 __global__ void k_add_f32(size_t n, double* __restrict__ x, const float* __restrict__ e) {
+    pdl_enter();
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
         x[k] += (double)e[k];
 }
 
 __global__ void k_shift(size_t n, double* __restrict__ x, int pin, const DevScalars* S) {
+    pdl_enter();
     double s = S->pin_value - x[pin];
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
         x[k] += s;
@@ -458,6 +519,7 @@ __global__ void k_shift(size_t n, double* __restrict__ x, int pin, const DevScal
 // y = A_ref x (reference pinned matrix) from the device operator.
 __global__ void k_apply_ref(Level F, const double* __restrict__ x, int pin, double dA, double kappa,
                             double* __restrict__ y) {
+    pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i >= F.n1 || j >= F.n2) return;
     size_t k = IX(i, j, F.n2);
@@ -473,11 +535,35 @@ __global__ void k_apply_ref(Level F, const double* __restrict__ x, int pin, doub
 }
 
 #include "mgfused.cuh"
+#include "mgcluster.cuh"
 
 constexpr size_t MG_COARSE_SMEM = 160 * 1024;
+constexpr size_t MG_CLUSTER_SMEM = 160 * 1024;
+
+// CTAs per cluster for k_cluster_vcycle: 16 where the device can co-schedule such a cluster
+// with the kernel's shared memory, else 8, else 0 (the per-level path is used).
+template <class T>
+static int cluster_size_for(int want) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(want);
+    cfg.blockDim = dim3(CL_THREADS);
+    cfg.dynamicSmemBytes = MG_CLUSTER_SMEM;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = want;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int num = 0;
+    if (cudaOccupancyMaxActiveClusters(&num, k_cluster_vcycle<T>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return num > 0 ? want : 0;
+}
 
 // ---------------------------------------------------------------- host orchestration
-static int red_blocks(impec_ctx* ctx) { return ctx->num_sms * 2 < ctx->max_blocks ? ctx->num_sms * 2 : ctx->max_blocks; }
 
 impec_status pressure_alloc(impec_ctx* ctx) {
     const impec_params& P = ctx->P;
@@ -507,12 +593,15 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         }
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.idiag, n * 8));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.idiag32, n * 4));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.diag, n * 8));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.diag32, n * 4));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.x, n * 8));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.b, n * 8));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.x32, n * 4));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.b32, n * 4));
         ctx->L.push_back(Lv);
-        if (n1 <= 8 && n2 <= 8) break;
+        const int cmax = (int)env_long("IMPEC_MG_COARSEST", 4);  // coarsest level: both sides <= cmax
+        if (n1 <= cmax && n2 <= cmax) break;
         n1 = (n1 + 1) / 2;
         n2 = (n2 + 1) / 2;
     }
@@ -524,6 +613,17 @@ impec_status pressure_alloc(impec_ctx* ctx) {
     IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_coarse_vcycle<double, EXP9>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs));
     IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_coarse_vcycle<float, FACE5>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs));
     IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_coarse_vcycle<float, EXP9>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs));
+    const int cls = (int)MG_CLUSTER_SMEM;
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_cluster_vcycle<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, cls));
+    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_cluster_vcycle<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, cls));
+    ctx->cl_size = 0;
+    if (cudaFuncSetAttribute(k_cluster_vcycle<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+        cudaFuncSetAttribute(k_cluster_vcycle<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+        const int want = (int)env_long("IMPEC_MG_CL_CTAS", CL_MAX_CTAS);
+        for (int cs = want < CL_MAX_CTAS ? want : CL_MAX_CTAS; cs >= 2 && !ctx->cl_size; cs /= 2)
+            if (cluster_size_for<double>(cs) && cluster_size_for<float>(cs)) ctx->cl_size = cs;
+    }
+    cudaGetLastError();
     IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_pre<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<double, TBH_PRE>()));
     IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_post<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<double, TBH_POST>()));
     IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_pre<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<float, TBH_PRE>()));
@@ -533,7 +633,8 @@ impec_status pressure_alloc(impec_ctx* ctx) {
 
 void pressure_free(impec_ctx* ctx) {
     for (Level& Lv : ctx->L) {
-        void* ps[] = {Lv.tx, Lv.ty, Lv.a9, Lv.idiag, Lv.x, Lv.b, Lv.tx32, Lv.ty32, Lv.a932, Lv.idiag32, Lv.x32, Lv.b32};
+        void* ps[] = {Lv.tx,   Lv.ty,   Lv.a9,   Lv.idiag,   Lv.diag,   Lv.x,   Lv.b,
+                      Lv.tx32, Lv.ty32, Lv.a932, Lv.idiag32, Lv.diag32, Lv.x32, Lv.b32};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
@@ -548,15 +649,15 @@ impec_status face_mobility(impec_ctx* ctx, const double* c) {
     const int n1 = P.N1, n2 = P.N2;
     const int harm = P.avgproc == IMPEC_HARMONIC;
     double* w2 = ctx->K22 ? ctx->muK22 : nullptr;
-    ++ctx->nlaunch, k_cell_w<<<grid2(n1, n2), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, c, ctx->K11, ctx->K22, ctx->G.mob1over4,
+    ++ctx->nlaunch, launch_k(ctx->stream, k_cell_w, grid2(n1, n2), dim3(BX, BY), 0, n1, n2, c, ctx->K11, ctx->K22, ctx->G.mob1over4,
                                                                P.mu_res, harm, ctx->muK11, w2);
     IMPEC_LAUNCH_CHECK();
     const double* W2 = w2 ? w2 : ctx->muK11;
-    ++ctx->nlaunch, k_face_lam<<<grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, ctx->muK11, W2, harm, ctx->lamx,
+    ++ctx->nlaunch, launch_k(ctx->stream, k_face_lam, grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, n1, n2, ctx->muK11, W2, harm, ctx->lamx,
                                                                           ctx->lamy);
     IMPEC_LAUNCH_CHECK();
     if (P.nu < 1.0) {
-        ++ctx->nlaunch, k_corner<<<grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(n1, n2, ctx->muK11, W2, harm, ctx->G,
+        ++ctx->nlaunch, launch_k(ctx->stream, k_corner, grid2(n1 + 1, n2 + 1), dim3(BX, BY), 0, n1, n2, ctx->muK11, W2, harm, ctx->G,
                                                                             ctx->cm11, ctx->cm22, ctx->cm12);
         IMPEC_LAUNCH_CHECK();
     }
@@ -570,44 +671,45 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
     const Geo& G = ctx->G;
     if (F.kind == FACE5) {
         double sx = G.dA * (1. / (G.dx * G.dx)), sy = G.dA * (1. / (G.dy * G.dy));
-        ++ctx->nlaunch, k_face5_fine<<<grid2(F.n1 + 1, F.n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, ctx->lamx, ctx->lamy,
+        ++ctx->nlaunch, launch_k(ctx->stream, k_face5_fine, grid2(F.n1 + 1, F.n2 + 1), dim3(BX, BY), 0, F.n1, F.n2, ctx->lamx, ctx->lamy,
                                                                                   sx, sy, F.tx, F.ty);
     } else {
-        ++ctx->nlaunch, k_exp9_fine<<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, ctx->lamx, ctx->lamy, ctx->cm11,
+        ++ctx->nlaunch, launch_k(ctx->stream, k_exp9_fine, grid2(F.n1, F.n2), dim3(BX, BY), 0, F.n1, F.n2, ctx->lamx, ctx->lamy, ctx->cm11,
                                                                          ctx->cm22, ctx->cm12, P.nu, G, F.a9);
     }
     IMPEC_LAUNCH_CHECK();
     for (size_t l = 0; l + 1 < ctx->L.size(); ++l) {
         Level &A = ctx->L[l], &B = ctx->L[l + 1];
         if (A.kind == FACE5)
-            ++ctx->nlaunch, k_face5_coarsen<<<grid2(B.n1 + 1, B.n2 + 1), dim3(BX, BY), 0, ctx->stream>>>(A.n1, A.n2, A.tx, A.ty, B.n1,
+            ++ctx->nlaunch, launch_k(ctx->stream, k_face5_coarsen, grid2(B.n1 + 1, B.n2 + 1), dim3(BX, BY), 0, A.n1, A.n2, A.tx, A.ty, B.n1,
                                                                                         B.n2, B.tx, B.ty);
         else
-            ++ctx->nlaunch, k_exp9_coarsen<<<grid2(B.n1, B.n2), dim3(BX, BY), 0, ctx->stream>>>(A.n1, A.n2, A.a9, B.n1, B.n2, B.a9);
+            ++ctx->nlaunch, launch_k(ctx->stream, k_exp9_coarsen, grid2(B.n1, B.n2), dim3(BX, BY), 0, A.n1, A.n2, A.a9, B.n1, B.n2, B.a9);
         IMPEC_LAUNCH_CHECK();
     }
     const bool mixed = P.precision == IMPEC_PREC_MIXED;
     for (Level& Lv : ctx->L) {
-        ++ctx->nlaunch, k_idiag<<<grid2(Lv.n1, Lv.n2), dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, Lv.kind, Lv.tx, Lv.ty, Lv.a9,
-                                                                        Lv.idiag);
+        ++ctx->nlaunch, launch_k(ctx->stream, k_idiag, grid2(Lv.n1, Lv.n2), dim3(BX, BY), 0, Lv.n1, Lv.n2, Lv.kind, Lv.tx,
+                                 Lv.ty, Lv.a9, Lv.diag, Lv.idiag);
         IMPEC_LAUNCH_CHECK();
         if (mixed) {
             const size_t n = Lv.n();
             int nb = ctx->num_sms * 4;
-            ++ctx->nlaunch, k_to_float<<<nb, 256, 0, ctx->stream>>>(n, Lv.idiag, Lv.idiag32);
+            ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, n, Lv.idiag, Lv.idiag32);
+            ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, n, Lv.diag, Lv.diag32);
             if (Lv.kind == FACE5) {
-                ++ctx->nlaunch, k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)(Lv.n1 + 1) * Lv.n2, Lv.tx, Lv.tx32);
-                ++ctx->nlaunch, k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)Lv.n1 * (Lv.n2 + 1), Lv.ty, Lv.ty32);
+                ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)(Lv.n1 + 1) * Lv.n2, Lv.tx, Lv.tx32);
+                ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)Lv.n1 * (Lv.n2 + 1), Lv.ty, Lv.ty32);
             } else {
-                ++ctx->nlaunch, k_to_float<<<nb, 256, 0, ctx->stream>>>(n * 9, Lv.a9, Lv.a932);
+                ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, n * 9, Lv.a9, Lv.a932);
             }
             IMPEC_LAUNCH_CHECK();
         }
     }
     Level& C = ctx->L.back();
-    ++ctx->nlaunch, k_dense_build<<<1, 256, 0, ctx->stream>>>(C, C.tx, C.ty, C.a9, 1, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n);
+    ++ctx->nlaunch, launch_k(ctx->stream, k_dense_build, 1, 256, 0, C, C.tx, C.ty, C.a9, 1, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n);
     IMPEC_LAUNCH_CHECK();
-    ++ctx->nlaunch, k_dense_invert<<<1, 256, 2 * ctx->dense_n * ctx->dense_n * 8, ctx->stream>>>(
+    ++ctx->nlaunch, launch_k(ctx->stream, k_dense_invert, 1, 256, 2 * ctx->dense_n * ctx->dense_n * 8,
         ctx->dense_n, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n, ctx->dense_inv);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
@@ -627,20 +729,27 @@ void level_ptrs<float>(Level& Lv, const float*& tx, const float*& ty, const floa
 }
 
 template <class T>
+static const T* level_diag(const Level& Lv);
+template <>
+const double* level_diag<double>(const Level& Lv) { return Lv.diag; }
+template <>
+const float* level_diag<float>(const Level& Lv) { return Lv.diag32; }
+
+template <class T>
 static void smooth(impec_ctx* ctx, Level& Lv, int sweeps, bool reverse) {
     const T *tx, *ty, *a9, *id;
     T *x, *b;
     level_ptrs<T>(Lv, tx, ty, a9, id, x, b);
     for (int s = 0; s < sweeps; ++s) {
         if (Lv.kind == FACE5) {
-            dim3 g((Lv.n2 / 2 + 1 + BX - 1) / BX, (Lv.n1 + BY - 1) / BY);
+            dim3 g((Lv.n2 / 2 + 1 + BX - 1) / BX, (Lv.n1 + RB_ROWS * BY - 1) / (RB_ROWS * BY));
             for (int cc = 0; cc < 2; ++cc)
-                ++ctx->nlaunch, k_rb_face5<T><<<g, dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, tx, ty, id, b, x, reverse ? 1 - cc : cc);
+                ++ctx->nlaunch, launch_k(ctx->stream, k_rb_face5<T>, g, dim3(BX, BY), 0, Lv.n1, Lv.n2, tx, ty, id, b, x, reverse ? 1 - cc : cc);
         } else {
             dim3 g(((Lv.n2 + 1) / 2 + BX - 1) / BX, ((Lv.n1 + 1) / 2 + BY - 1) / BY);
             for (int cc = 0; cc < 4; ++cc) {
                 int col = reverse ? 3 - cc : cc;
-                ++ctx->nlaunch, k_gs4_exp9<T><<<g, dim3(BX, BY), 0, ctx->stream>>>(Lv.n1, Lv.n2, a9, id, b, x, col >> 1, col & 1);
+                ++ctx->nlaunch, launch_k(ctx->stream, k_gs4_exp9<T>, g, dim3(BX, BY), 0, Lv.n1, Lv.n2, a9, id, b, x, col >> 1, col & 1);
             }
         }
     }
@@ -653,14 +762,9 @@ static size_t coarse_bytes(const impec_ctx* ctx, size_t l) {
     for (size_t k = l; k < ctx->L.size(); ++k) {
         const Level& Lv = ctx->L[k];
         const size_t n = Lv.n();
-        b += Lv.kind == FACE5 ? (size_t)(Lv.n1 + 1) * Lv.n2 + (size_t)Lv.n1 * (Lv.n2 + 1) + 3 * n : 12 * n;
+        b += Lv.kind == FACE5 ? (size_t)(Lv.n1 + 1) * Lv.n2 + (size_t)Lv.n1 * (Lv.n2 + 1) + 4 * n : 12 * n;
     }
     return b * sizeof(T);
-}
-
-static long env_long(const char* name, long dflt) {
-    const char* e = getenv(name);
-    return e && *e ? strtol(e, nullptr, 10) : dflt;
 }
 
 // First level handled by the single-CTA coarse V-cycle: the largest level whose cell count is
@@ -668,7 +772,7 @@ static long env_long(const char* name, long dflt) {
 template <class T>
 static size_t coarse_start(const impec_ctx* ctx) {
     const size_t cells = (size_t)(sizeof(T) == 8 ? env_long("IMPEC_MG_COARSE_CELLS64", 256)
-                                                 : env_long("IMPEC_MG_COARSE_CELLS32", 4096));
+                                                 : env_long("IMPEC_MG_COARSE_CELLS32", 1024));
     for (size_t l = 0; l < ctx->L.size(); ++l)
         if (ctx->L[l].n() <= cells && coarse_bytes<T>(ctx, l) <= MG_COARSE_SMEM) return l;
     return ctx->L.size() - 1;
@@ -688,22 +792,111 @@ static void launch_coarse(impec_ctx* ctx, size_t lc) {
         level_ptrs<T>(Lv, tx, ty, a9, id, x, b);
         A.n1[k] = Lv.n1;
         A.n2[k] = Lv.n2;
-        A.tx[k] = tx; A.ty[k] = ty; A.a9[k] = a9; A.id[k] = id;
+        A.tx[k] = tx; A.ty[k] = ty; A.a9[k] = a9; A.id[k] = id; A.dg[k] = level_diag<T>(Lv);
         if (k == 0) { A.x0 = x; A.b0 = b; }
     }
     const size_t smem = coarse_bytes<T>(ctx, lc);
     ++ctx->nlaunch;
     if (ctx->L[lc].kind == FACE5)
-        k_coarse_vcycle<T, FACE5><<<1, 1024, smem, ctx->stream>>>(A);
+        launch_k(ctx->stream, k_coarse_vcycle<T, FACE5>, 1, 1024, smem, A);
     else
-        k_coarse_vcycle<T, EXP9><<<1, 1024, smem, ctx->stream>>>(A);
+        launch_k(ctx->stream, k_coarse_vcycle<T, EXP9>, 1, 1024, smem, A);
 }
 
-// Temporally blocked level kernels: used for FP32 levels (all), FP64 levels only on request
-// (each CTA's FP64 work is latency-bound on one SM).
+// Layout of the cluster V-cycle over levels ls .. L-1: which levels are spread over the cluster
+// (a prefix of at least one level above the CTA-0 threshold), each CTA's band height and the
+// shared-memory offsets.  False when the levels do not fit the kernel (nine-point operators,
+// too many levels, too much shared memory, a coarsest level above CL_THREADS cells).
+template <class T>
+static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& smem) {
+    const int CS = ctx->cl_size;
+    const size_t nl = ctx->L.size() - ls;
+    if (CS < 2 || nl < 2 || nl > (size_t)CL_MAXL || ctx->dense_n > CL_THREADS) return false;
+    const long cta0 = env_long("IMPEC_MG_CL_CTA0", 256);
+    A = ClusterArgs<T>{};
+    A.nl = (int)nl;
+    A.singular = 1;
+    A.dn = ctx->dense_n;
+    A.dinv = ctx->dense_inv;
+    size_t off = 0;
+    int nd = 0;
+    for (size_t k = 0; k < nl; ++k) {
+        Level& Lv = ctx->L[ls + k];
+        if (Lv.kind != FACE5) return false;
+        int R = Lv.n1;
+        if (k + 1 < nl && nd == (int)k && (long)Lv.n() > cta0) {
+            R = (Lv.n1 + CS - 1) / CS;
+            R += R & 1;
+            ++nd;
+        }
+        A.n1[k] = Lv.n1;
+        A.n2[k] = Lv.n2;
+        A.rows[k] = R;
+        const size_t n2 = (size_t)Lv.n2, r = (size_t)R;
+        const size_t sz[6] = {(r + 1) * n2, r * (n2 + 1), r * n2, r * n2, r * n2, r * n2};
+        for (int a = 0; a < 6; ++a) {
+            A.off[k][a] = (unsigned)off;
+            off += sz[a];
+        }
+        const T *tx, *ty, *a9, *id;
+        T *x, *b;
+        level_ptrs<T>(Lv, tx, ty, a9, id, x, b);
+        A.tx[k] = tx;
+        A.ty[k] = ty;
+        A.id[k] = id;
+        A.dg[k] = level_diag<T>(Lv);
+        if (k == 0) {
+            A.x0 = x;
+            A.b0 = b;
+        }
+    }
+    A.nd = nd;
+    smem = off * sizeof(T);
+    return nd > 0 && smem <= MG_CLUSTER_SMEM;
+}
+
+// First level handled by the cluster V-cycle (the largest level within IMPEC_MG_CL_CELLS cells
+// whose plan fits), or SIZE_MAX for the per-level path.
+template <class T>
+static size_t cluster_start(impec_ctx* ctx) {
+    if (ctx->cl_size < 2 || env_long("IMPEC_MG_CLUSTER", 1) == 0) return SIZE_MAX;
+    const long cells = env_long("IMPEC_MG_CL_CELLS", 16384);
+    ClusterArgs<T> A;
+    size_t smem;
+    for (size_t l = 0; l < ctx->L.size(); ++l)
+        if ((long)ctx->L[l].n() <= cells && cluster_plan<T>(ctx, l, A, smem)) return l;
+    return SIZE_MAX;
+}
+
+template <class T>
+static void launch_cluster(impec_ctx* ctx, size_t ls) {
+    ClusterArgs<T> A;
+    size_t smem = 0;
+    cluster_plan<T>(ctx, ls, A, smem);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctx->cl_size);
+    cfg.blockDim = dim3(CL_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = ctx->cl_size;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 2 : 1;
+    ++ctx->nlaunch;
+    cudaLaunchKernelEx(&cfg, k_cluster_vcycle<T>, A);
+}
+
+// Temporally blocked level kernels (two launches per level and cycle), only on request: on
+// GB300 they are slower than full-sweep launches in both precisions, because the halo cells
+// they recompute cost FP64 issue slots and their per-CTA phases serialise.
 template <class T>
 static bool use_fused_level(size_t l) {
-    if (sizeof(T) == 4) return env_long("IMPEC_MG_FUSED32", 1) != 0;
+    if (sizeof(T) == 4) return env_long("IMPEC_MG_FUSED32", 0) != 0;
     return env_long("IMPEC_MG_FUSED64", 0) != 0 && (l > 0 || env_long("IMPEC_MG_FUSE_FINE", 0) != 0);
 }
 
@@ -713,6 +906,10 @@ static void vcycle(impec_ctx* ctx, size_t l) {
     const T *tx, *ty, *a9, *id;
     T *x, *b;
     level_ptrs<T>(F, tx, ty, a9, id, x, b);
+    if (l == cluster_start<T>(ctx)) {
+        launch_cluster<T>(ctx, l);
+        return;
+    }
     const size_t lc = coarse_start<T>(ctx);
     if (l == lc) {
         launch_coarse<T>(ctx, lc);
@@ -726,18 +923,19 @@ static void vcycle(impec_ctx* ctx, size_t l) {
     if (fused) {  // two launches for this level: smooth+residual+restrict, prolong+smooth
         dim3 g((F.n2 + TB - 1) / TB, (F.n1 + TB - 1) / TB);
         ++ctx->nlaunch;
-        k_level_pre<T><<<g, TBT, tb_smem<T, TBH_PRE>(), ctx->stream>>>(F.n1, F.n2, tx, ty, id, b, x, C.n2, cb, cx, C.n1);
+        launch_k(ctx->stream, k_level_pre<T>, g, TBT, tb_smem<T, TBH_PRE>(), F.n1, F.n2, tx, ty, id, b, x, C.n2, cb, cx, C.n1);
         vcycle<T>(ctx, l + 1);
         ++ctx->nlaunch;
-        k_level_post<T><<<g, TBT, tb_smem<T, TBH_POST>(), ctx->stream>>>(F.n1, F.n2, tx, ty, id, b, x, C.n1, C.n2, cx);
+        launch_k(ctx->stream, k_level_post<T>, g, TBT, tb_smem<T, TBH_POST>(), F.n1, F.n2, tx, ty, id, b, x, C.n1, C.n2, cx);
         return;
     }
     smooth<T>(ctx, F, 2, false);
     ++ctx->nlaunch;
-    k_restrict<T><<<grid2(C.n1, C.n2), dim3(BX, BY), 0, ctx->stream>>>(F, tx, ty, a9, b, x, C.n1, C.n2, cb, cx);
+    launch_k(ctx->stream, k_restrict<T>, grid2(C.n1, C.n2), dim3(BX, BY), 0, F, tx, ty, a9, level_diag<T>(F), b, x,
+             C.n1, C.n2, cb, cx);
     vcycle<T>(ctx, l + 1);
     ++ctx->nlaunch;
-    k_prolong<T><<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F.n1, F.n2, x, C.n1, C.n2, cx);
+    launch_k(ctx->stream, k_prolong<T>, grid2(F.n1, F.n2), dim3(BX, BY), 0, F.n1, F.n2, x, C.n1, C.n2, cx);
     smooth<T>(ctx, F, 2, true);
 }
 
@@ -745,6 +943,7 @@ static void vcycle(impec_ctx* ctx, size_t l) {
 // another cycle runs and, inside a graph, sets the WHILE node's condition.
 __global__ void k_mg_check(DevScalars* S, double tol, int max_cycles, int inc, cudaGraphConditionalHandle h,
                            int use_h) {
+    pdl_enter();
     if (inc) S->mg_cycles++;
     double fn = S->fnorm2, rn = S->rnorm2;
     double rr = fn > 0 ? sqrt(rn / fn) : sqrt(rn);
@@ -766,13 +965,12 @@ impec_status pressure_prepare(impec_ctx* ctx, const double* c, const double* p) 
     Level& F = ctx->L[0];
     const size_t n = F.n();
     const int pin = pin_index(ctx);
-    const int rb = red_blocks(ctx);
     DevScalars* S = ctx->dscal;
     ++ctx->nlaunch;
-    k_rhs<<<rb, RED_THREADS, 0, ctx->stream>>>(n, ctx->q, ctx->G.dA, ctx->f, ctx->partials, ctx->max_blocks,
+    launch_k(ctx->stream, k_rhs, flat_blocks(n, red_cap(ctx->num_sms, ctx->max_blocks)), RED_THREADS, 0, n, ctx->q, ctx->G.dA, ctx->f, ctx->partials, ctx->max_blocks,
                                                 ctx->counter, &S->fsum);
     ++ctx->nlaunch;
-    k_fix_pin<<<1, 1, 0, ctx->stream>>>(ctx->f, ctx->q, pin, ctx->G.dA, ctx->pin_kappa, S);
+    launch_k(ctx->stream, k_fix_pin, 1, 1, 0, ctx->f, ctx->q, pin, ctx->G.dA, ctx->pin_kappa, S);
     IMPEC_LAUNCH_CHECK();
     if (P.warm_start)
         IMPEC_CUDA_TRY(cudaMemcpyAsync(F.x, p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -788,7 +986,9 @@ impec_status pressure_residual(impec_ctx* ctx) {
     Level& F = ctx->L[0];
     const bool mixed = ctx->P.precision == IMPEC_PREC_MIXED;
     ++ctx->nlaunch;
-    k_fine_resid<<<red_blocks(ctx), RED_THREADS, 0, ctx->stream>>>(F, ctx->f, F.x, pin_index(ctx),
+    // about seven cells per thread: the FP64 warp sums of the reduction stay small beside the residual
+    const int blocks = seg_blocks(F.n1, F.n2, red_cap(ctx->num_sms, ctx->max_blocks));
+    launch_k(ctx->stream, k_fine_resid, blocks, RED_THREADS, 0, F, ctx->f, F.x, pin_index(ctx),
                                                                   mixed ? F.b32 : nullptr, ctx->partials,
                                                                   ctx->max_blocks, ctx->counter, &ctx->dscal->rnorm2);
     IMPEC_LAUNCH_CHECK();
@@ -797,7 +997,7 @@ impec_status pressure_residual(impec_ctx* ctx) {
 
 impec_status pressure_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h) {
     ++ctx->nlaunch;
-    k_mg_check<<<1, 1, 0, ctx->stream>>>(ctx->dscal, tol, ctx->P.max_cycles, inc, h, use_h);
+    launch_k(ctx->stream, k_mg_check, 1, 1, 0, ctx->dscal, tol, ctx->P.max_cycles, inc, h, use_h);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -810,7 +1010,7 @@ impec_status pressure_iteration(impec_ctx* ctx) {
         IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
         vcycle<float>(ctx, 0);
         ++ctx->nlaunch;
-        k_add_f32<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, F.x, F.x32);
+        launch_k(ctx->stream, k_add_f32, ctx->num_sms * 4, 256, 0, n, F.x, F.x32);
     } else {
         vcycle<double>(ctx, 0);
     }
@@ -823,7 +1023,7 @@ impec_status pressure_finish(impec_ctx* ctx, double* p) {
     Level& F = ctx->L[0];
     const size_t n = F.n();
     ++ctx->nlaunch;
-    k_shift<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, F.x, pin_index(ctx), ctx->dscal);
+    launch_k(ctx->stream, k_shift, ctx->num_sms * 4, 256, 0, n, F.x, pin_index(ctx), ctx->dscal);
     IMPEC_LAUNCH_CHECK();
     IMPEC_CUDA_TRY(cudaMemcpyAsync(p, F.x, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     return IMPEC_OK;
@@ -855,7 +1055,7 @@ impec_status pressure_solve(impec_ctx* ctx, const double* c, double* p, double t
 impec_status pressure_apply_ref(impec_ctx* ctx, const double* x, double* y) {
     Level& F = ctx->L[0];
     const int pin = (int)IX(ctx->pin_i, ctx->pin_j, F.n2);
-    ++ctx->nlaunch, k_apply_ref<<<grid2(F.n1, F.n2), dim3(BX, BY), 0, ctx->stream>>>(F, x, pin, ctx->G.dA, ctx->pin_kappa, y);
+    ++ctx->nlaunch, launch_k(ctx->stream, k_apply_ref, grid2(F.n1, F.n2), dim3(BX, BY), 0, F, x, pin, ctx->G.dA, ctx->pin_kappa, y);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -888,6 +1088,7 @@ __global__ void k_velocity(VelArgs A, const double* __restrict__ p, const double
                            const double* __restrict__ lamy, const double* __restrict__ m11,
                            const double* __restrict__ m22, const double* __restrict__ m12, double* __restrict__ u,
                            double* __restrict__ v) {
+    pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     const int n1 = A.n1, n2 = A.n2;
     const bool diag = A.nu < 1.0;
@@ -922,7 +1123,7 @@ impec_status velocity(impec_ctx* ctx, const double* p, const double* c, double* 
     const impec_params& P = ctx->P;
     const Geo& G = ctx->G;
     VelArgs A{P.N1, P.N2, P.nu, 1.0 / G.dx, 1.0 / G.dy, 1.0 / G.dxi, 1.0 / G.deta, G.cost, G.sina, G.sint, G.cosa};
-    ++ctx->nlaunch, k_velocity<<<grid2(P.N1 + 1, P.N2 + 1), dim3(BX, BY), 0, ctx->stream>>>(A, p, ctx->lamx, ctx->lamy, ctx->cm11,
+    ++ctx->nlaunch, launch_k(ctx->stream, k_velocity, grid2(P.N1 + 1, P.N2 + 1), dim3(BX, BY), 0, A, p, ctx->lamx, ctx->lamy, ctx->cm11,
                                                                             ctx->cm22, ctx->cm12, u, v);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
@@ -933,11 +1134,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_maxvel(int n1, int n2, const do
                                                         const double* __restrict__ v, int diffusion, double al,
                                                         double at, double dx, double* partials, int mb,
                                                         unsigned* counter, double* out) {
+    pdl_enter();
     double acc[2] = {0.0, -1.0e10};  // max velocity, max of -dt_diff
-    const size_t n = (size_t)n1 * n2;
     const double tiny = 2.2250738585072014e-308;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-        int i = (int)(k / n2), j = (int)(k % n2);
+    for_cells(n1, n2, [&](int i, int j, size_t) {
         double uij = 0.5 * (u[IX(i, j, n2)] + u[IX(i + 1, j, n2)]);
         double vij = 0.5 * (v[IX(i, j, n2 + 1)] + v[IX(i, j + 1, n2 + 1)]);
         double uc = fabs(uij), vc = fabs(vij);
@@ -952,11 +1152,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_maxvel(int n1, int n2, const do
             double dt = 1. / 2 * dx * dx / (d11 + d22);
             acc[1] = fmax(acc[1], -dt);
         }
-    }
+    });
     grid_reduce<2>(acc, 3u, partials, mb, counter, out);
 }
 
 __global__ void k_finish_dt(DevScalars* S, double dx, double dy, double cfl, int use_diff, double limit) {
+    pdl_enter();
     double mv = S->red[0];
     S->maxvel = mv;
     double dt = fmin(dx / mv, dy / mv) * cfl;
@@ -970,12 +1171,13 @@ __global__ void k_finish_dt(DevScalars* S, double dx, double dy, double cfl, int
 impec_status max_stable_dt_dev(impec_ctx* ctx, const double* u, const double* v) {
     const impec_params& P = ctx->P;
     const Geo& G = ctx->G;
-    const int rb = red_blocks(ctx);
-    ++ctx->nlaunch, k_maxvel<<<rb, RED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, u, v, P.diffusion, P.alpha_l, P.alpha_t, G.dx,
-                                                   ctx->partials, ctx->max_blocks, ctx->counter, ctx->dscal->red);
-    double cfl = P.cfl_porosity ? P.cfl * P.porosity : P.cfl;
+    // the diffusive limit (sqrt and two FP64 divisions per cell) only when it enters dt
     const int use_diff = P.diffusion && P.ptype != IMPEC_CRANKNICOLSON;
-    ++ctx->nlaunch, k_finish_dt<<<1, 1, 0, ctx->stream>>>(ctx->dscal, G.dx, G.dy, cfl, use_diff, P.dt_diff_limit);
+    ++ctx->nlaunch, launch_k(ctx->stream, k_maxvel, seg_blocks(P.N1, P.N2, red_cap(ctx->num_sms, ctx->max_blocks)), RED_THREADS, 0,
+        P.N1, P.N2, u, v, use_diff, P.alpha_l, P.alpha_t, G.dx, ctx->partials, ctx->max_blocks, ctx->counter,
+        ctx->dscal->red);
+    double cfl = P.cfl_porosity ? P.cfl * P.porosity : P.cfl;
+    ++ctx->nlaunch, launch_k(ctx->stream, k_finish_dt, 1, 1, 0, ctx->dscal, G.dx, G.dy, cfl, use_diff, P.dt_diff_limit);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -991,14 +1193,14 @@ extern "C" impec_status impec_time_kernel(impec_ctx* ctx, int which, int reps, d
     if (which == 1 && ctx->P.precision != IMPEC_PREC_MIXED) {  // FP32 copies of the fine level
         const int nb = ctx->num_sms * 4;
         if (F.kind == FACE5) {
-            k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)(F.n1 + 1) * F.n2, F.tx, F.tx32);
-            k_to_float<<<nb, 256, 0, ctx->stream>>>((size_t)F.n1 * (F.n2 + 1), F.ty, F.ty32);
+            launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)(F.n1 + 1) * F.n2, F.tx, F.tx32);
+            launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)F.n1 * (F.n2 + 1), F.ty, F.ty32);
         } else {
-            k_to_float<<<nb, 256, 0, ctx->stream>>>(F.n() * 9, F.a9, F.a932);
+            launch_k(ctx->stream, k_to_float, nb, 256, 0, F.n() * 9, F.a9, F.a932);
         }
-        k_to_float<<<nb, 256, 0, ctx->stream>>>(F.n(), F.idiag, F.idiag32);
-        k_to_float<<<nb, 256, 0, ctx->stream>>>(F.n(), F.b, F.b32);
-        k_to_float<<<nb, 256, 0, ctx->stream>>>(F.n(), F.x, F.x32);
+        launch_k(ctx->stream, k_to_float, nb, 256, 0, F.n(), F.idiag, F.idiag32);
+        launch_k(ctx->stream, k_to_float, nb, 256, 0, F.n(), F.b, F.b32);
+        launch_k(ctx->stream, k_to_float, nb, 256, 0, F.n(), F.x, F.x32);
         IMPEC_LAUNCH_CHECK();
     }
     cudaEvent_t e0, e1;

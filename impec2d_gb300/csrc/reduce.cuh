@@ -39,6 +39,35 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], unsigned maxmask) {
     }
 }
 
+// Blocks for a row-segment walk over an n1 x n2 grid: one block per segment of RED_THREADS
+// cells of a row, at most max_blocks (larger grids loop).
+static inline int seg_blocks(int n1, int n2, int max_blocks) {
+    const long units = (long)n1 * ((n2 + RED_THREADS - 1) / RED_THREADS);
+    return (int)(units < max_blocks ? units : max_blocks);
+}
+
+// Block limit for the reductions: four blocks per SM, so that each thread folds several cells
+// before the FP64 warp sums (five additions per reduced value and thread) are paid.
+static inline int red_cap(int num_sms, int max_blocks) { return num_sms * 4 < max_blocks ? num_sms * 4 : max_blocks; }
+
+// Blocks for a flat walk over n values: one value per thread, at most max_blocks.
+static inline int flat_blocks(size_t n, int max_blocks) {
+    const size_t b = (n + RED_THREADS - 1) / RED_THREADS;
+    return (int)(b < (size_t)max_blocks ? (b > 0 ? b : 1) : (size_t)max_blocks);
+}
+
+// Row-segment walk (grid of seg_blocks blocks of RED_THREADS): f(i, j, k) for every cell,
+// k = i*n2 + j.  A block issues the loads of a whole segment at once and no thread divides
+// per cell, which keeps the walk bandwidth- rather than latency-bound.
+template <class F>
+__device__ __forceinline__ void for_cells(int n1, int n2, F&& f) {
+    const int segs = (n2 + RED_THREADS - 1) / RED_THREADS, units = n1 * segs;
+    for (int u = blockIdx.x; u < units; u += gridDim.x) {
+        const int i = u / segs, j = (u - i * segs) * RED_THREADS + (int)threadIdx.x;
+        if (j < n2) f(i, j, (size_t)i * n2 + j);
+    }
+}
+
 // Grid-level reduction with last-block finalisation.  Requires blockDim.x == RED_THREADS,
 // 1-D grid with gridDim.x <= max_blocks.  out[k] receives the reduced values.
 template <int K>

@@ -52,10 +52,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_diag(int n1, int n2, const doub
                                                       const double* __restrict__ u, const double* __restrict__ v,
                                                       const double* __restrict__ q, double inv_dx, double inv_dy,
                                                       double* partials, int mb, unsigned* counter, double* out) {
+    pdl_enter();
     double acc[5] = {0.0, 0.0, 0.0, -INFINITY, -INFINITY};
-    const size_t n = (size_t)n1 * n2;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-        int i = (int)(k / n2), j = (int)(k % n2);
+    for_cells(n1, n2, [&](int i, int j, size_t k) {
         double cc = c[k];
         acc[0] += cc;
         double div = (v[IX(i, j + 1, n2 + 1)] - v[IX(i, j, n2 + 1)]) * inv_dy + (u[IX(i + 1, j, n2)] - u[IX(i, j, n2)]) * inv_dx;
@@ -68,13 +67,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_diag(int n1, int n2, const doub
         acc[2] += be;
         acc[3] = fmax(acc[3], cc);
         acc[4] = fmax(acc[4], -cc);
-    }
+    });
     grid_reduce<5>(acc, (1u << 3) | (1u << 4), partials, mb, counter, out);
 }
 
 static impec_status diagnostics_dev(impec_ctx* ctx, const double* c, const double* u, const double* v) {
     const impec_params& P = ctx->P;
-    ++ctx->nlaunch, k_diag<<<ctx->num_sms * 2, RED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, u, v, ctx->have_source ? ctx->q : nullptr,
+    ++ctx->nlaunch, launch_k(ctx->stream, k_diag, seg_blocks(P.N1, P.N2, red_cap(ctx->num_sms, ctx->max_blocks)), RED_THREADS, 0, P.N1, P.N2, c, u, v, ctx->have_source ? ctx->q : nullptr,
                                                               1.0 / ctx->G.dx, 1.0 / ctx->G.dy, ctx->partials,
                                                               ctx->max_blocks, ctx->counter, ctx->dscal->red);
     IMPEC_LAUNCH_CHECK();

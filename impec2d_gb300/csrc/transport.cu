@@ -23,6 +23,7 @@ constexpr int TBX = 32, TBY = 8;
 __global__ void __launch_bounds__(RED_THREADS) k_tr(int nw, const int* __restrict__ idx, const double* __restrict__ qv,
                                                     double* __restrict__ c, const double* __restrict__ dt_dev,
                                                     double scale, double cinj, DevScalars* S, int slot) {
+    pdl_enter();
     const double dt = scale * dt_dev[0];
     double acc[1] = {0.0};
     for (int w = threadIdx.x; w < nw; w += blockDim.x) {
@@ -46,7 +47,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_tr(int nw, const int* __restric
 
 impec_status tr_integrate_dev(impec_ctx* ctx, double* c, double dt_scale, const double* dt_dev, int slot) {
     if (!ctx->have_source || ctx->nwells == 0) return IMPEC_OK;
-    ++ctx->nlaunch, k_tr<<<1, RED_THREADS, 0, ctx->stream>>>(ctx->nwells, ctx->well_idx, ctx->well_q, c, dt_dev, dt_scale,
+    ++ctx->nlaunch, launch_k(ctx->stream, k_tr, 1, RED_THREADS, 0, ctx->nwells, ctx->well_idx, ctx->well_q, c, dt_dev, dt_scale,
                                              ctx->P.inj_fluid_conc, ctx->dscal, slot);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
@@ -129,6 +130,7 @@ template <int SCHEME, int BC>
 __global__ void k_sweep_x(int n1, int n2, const double* __restrict__ cin, const double* __restrict__ cghost,
                           double* __restrict__ cout, const double* __restrict__ u, const double* __restrict__ dt_dev,
                           double dt_scale, double inv_dx_phi) {
+    pdl_enter();
     int j = blockIdx.x * TBX + threadIdx.x, i = blockIdx.y * TBY + threadIdx.y;
     if (i >= n1 || j >= n2) return;
     const double dt = dt_scale * dt_dev[0];
@@ -141,6 +143,7 @@ template <int SCHEME, int BC>
 __global__ void k_sweep_y(int n1, int n2, const double* __restrict__ cin, double* __restrict__ cout,
                           const double* __restrict__ v, const double* __restrict__ dt_dev, double dt_scale,
                           double inv_dy_phi) {
+    pdl_enter();
     int j = blockIdx.x * TBX + threadIdx.x, i = blockIdx.y * TBY + threadIdx.y;
     if (i >= n1 || j >= n2) return;
     const double dt = dt_scale * dt_dev[0];
@@ -149,6 +152,7 @@ __global__ void k_sweep_y(int n1, int n2, const double* __restrict__ cin, double
 }
 
 __global__ void k_average(size_t n, double* __restrict__ c, const double* __restrict__ a, const double* __restrict__ b) {
+    pdl_enter();
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
         c[k] = 0.5 * (a[k] + b[k]);
 }
@@ -179,6 +183,7 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_advect_symmetric(int n1, int 
                                                                      const double* __restrict__ v,
                                                                      const double* __restrict__ dt_dev, double inv_dx_phi,
                                                                      double inv_dy_phi) {
+    pdl_enter();
     __shared__ double sc[(TI + 4) * CW];   // c, rows i0-2 .. i0+TI+1
     __shared__ double su[(TI + 3) * CW];   // u faces fi in [i0-1, i0+TI+1], cols j0-2 ..
     __shared__ double sv[(TI + 4) * VW];   // v faces, rows i0-2 .., fj in [j0-1, j0+TJ+1]
@@ -283,11 +288,11 @@ impec_status advect_x_dev(impec_ctx* ctx, const double* cin, double* cout, const
     ++ctx->nlaunch;
     const bool per = P.bc == IMPEC_BC_PERIODIC;
     if (P.hmtype == IMPEC_MUSCL) {
-        if (per) k_sweep_x<IMPEC_MUSCL, IMPEC_BC_PERIODIC><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
-        else k_sweep_x<IMPEC_MUSCL, IMPEC_BC_NEUMANN><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
+        if (per) launch_k(ctx->stream, k_sweep_x<IMPEC_MUSCL, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
+        else launch_k(ctx->stream, k_sweep_x<IMPEC_MUSCL, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
     } else {
-        if (per) k_sweep_x<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
-        else k_sweep_x<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
+        if (per) launch_k(ctx->stream, k_sweep_x<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
+        else launch_k(ctx->stream, k_sweep_x<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
     }
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
@@ -301,11 +306,11 @@ impec_status advect_y_dev(impec_ctx* ctx, const double* cin, double* cout, const
     ++ctx->nlaunch;
     const bool per = P.bc == IMPEC_BC_PERIODIC;
     if (P.hmtype == IMPEC_MUSCL) {
-        if (per) k_sweep_y<IMPEC_MUSCL, IMPEC_BC_PERIODIC><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
-        else k_sweep_y<IMPEC_MUSCL, IMPEC_BC_NEUMANN><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
+        if (per) launch_k(ctx->stream, k_sweep_y<IMPEC_MUSCL, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
+        else launch_k(ctx->stream, k_sweep_y<IMPEC_MUSCL, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
     } else {
-        if (per) k_sweep_y<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
-        else k_sweep_y<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN><<<g, b, 0, ctx->stream>>>(P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
+        if (per) launch_k(ctx->stream, k_sweep_y<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
+        else launch_k(ctx->stream, k_sweep_y<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
     }
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
@@ -313,7 +318,7 @@ impec_status advect_y_dev(impec_ctx* ctx, const double* cin, double* cout, const
 
 impec_status average_dev(impec_ctx* ctx, double* c, const double* a, const double* b) {
     const size_t n = (size_t)ctx->P.N1 * ctx->P.N2;
-    ++ctx->nlaunch, k_average<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(n, c, a, b);
+    ++ctx->nlaunch, launch_k(ctx->stream, k_average, ctx->num_sms * 4, 256, 0, n, c, a, b);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -362,11 +367,11 @@ impec_status advect_split_dev(impec_ctx* ctx, double* c, const double* u, const 
             const bool per = P.bc == IMPEC_BC_PERIODIC;
             ++ctx->nlaunch;
             if (P.hmtype == IMPEC_MUSCL) {
-                if (per) k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_PERIODIC><<<g, FUSED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
-                else k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_NEUMANN><<<g, FUSED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+                if (per) launch_k(ctx->stream, k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_PERIODIC>, g, FUSED_THREADS, 0, P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+                else launch_k(ctx->stream, k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_NEUMANN>, g, FUSED_THREADS, 0, P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
             } else {
-                if (per) k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC><<<g, FUSED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
-                else k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN><<<g, FUSED_THREADS, 0, ctx->stream>>>(P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+                if (per) launch_k(ctx->stream, k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC>, g, FUSED_THREADS, 0, P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+                else launch_k(ctx->stream, k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN>, g, FUSED_THREADS, 0, P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
             }
             IMPEC_LAUNCH_CHECK();
             IMPEC_CUDA_TRY(cudaMemcpyAsync(c, t1, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -440,11 +445,11 @@ extern "C" impec_status impec_advect_symmetric_noalloc(const impec_params* P, do
     dim3 g((N2 + TJ - 1) / TJ, (N1 + TI - 1) / TI);
     const bool per = P->bc == IMPEC_BC_PERIODIC;
     if (P->hmtype == IMPEC_MUSCL) {
-        if (per) k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_PERIODIC><<<g, FUSED_THREADS, 0, s>>>(N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
-        else k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_NEUMANN><<<g, FUSED_THREADS, 0, s>>>(N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
+        if (per) launch_k(s, k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_PERIODIC>, g, FUSED_THREADS, 0, N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
+        else launch_k(s, k_advect_symmetric<IMPEC_MUSCL, IMPEC_BC_NEUMANN>, g, FUSED_THREADS, 0, N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
     } else {
-        if (per) k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC><<<g, FUSED_THREADS, 0, s>>>(N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
-        else k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN><<<g, FUSED_THREADS, 0, s>>>(N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
+        if (per) launch_k(s, k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC>, g, FUSED_THREADS, 0, N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
+        else launch_k(s, k_advect_symmetric<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN>, g, FUSED_THREADS, 0, N1, N2, c_dev, cnew, u_dev, v_dev, scratch, fx, fy);
     }
     IMPEC_LAUNCH_CHECK();
     IMPEC_CUDA_TRY(cudaMemcpyAsync(c_dev, cnew, (size_t)N1 * N2 * sizeof(double), cudaMemcpyDeviceToDevice, s));

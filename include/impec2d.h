@@ -172,6 +172,11 @@ impec_status impec_launch_count(impec_ctx* ctx, long long* n);
 impec_status impec_time_kernel(impec_ctx* ctx, int which, int reps, double* ms_per_launch,
                                double* bytes_per_launch);
 
+/* FP64 fused multiply-adds per second that the current device sustains (eight independent
+ * chains per thread on every SM): the denominator of the FP64-pipe fractions reported beside
+ * the HBM roofline.  No counterpart in the reference. */
+impec_status impec_measure_fp64(double* fma_per_second);
+
 /* Allocation-free transport step.  No counterpart in the reference: it exists for callers
  * that may not allocate device memory themselves or through this library -- code running
  * under a host framework that owns every device allocation (a fixed pool or budget), or that
