@@ -40,11 +40,16 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--n", type=int, default=None, help="grid side (default 1024; 4096 for --study pressure)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch each kernel on the stream instead of replaying the step graph (for ncu)")
+    ap.add_argument("--study", default=None, choices=["pressure", "warmstart"],
+                    help="pressure: FP64 vs mixed-precision solves on re-seeded heterogeneous fields; "
+                         "warmstart: V-cycles and ms per solve along the IMPES run for zero and previous-step "
+                         "initial guesses")
+    ap.add_argument("--solves", type=int, default=20, help="re-seeded solves of the pressure study")
     return ap.parse_args()
 
 
@@ -153,7 +158,7 @@ def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    n = args.n
+    n = args.n or N_DEFAULT
     cps, cores, secs = cpu_baseline(n, max(1, args.steps // 4) + 1)
     line = {"impl": "reference", "metric": METRIC, "value": cps, "unit": "cell-steps/s", "n_gpus": args.gpus,
             "steps": max(1, args.steps // 4) + 1, "warmup": 0, "ms_per_step": 1e3 / cps * n * n,
@@ -165,10 +170,118 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def grf(N, ell, seed):
+    """Seeded Gaussian random field on the GPU: white noise (Philox, seeded) filtered in Fourier
+    space to the covariance exp(-r^2 / ell^2) (ell in cells, periodic), zero mean, unit variance."""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    w = torch.randn((N, N), generator=g, device="cuda", dtype=torch.float64)
+    f = torch.fft.fftfreq(N, device="cuda", dtype=torch.float64)
+    H = torch.exp(-(math.pi * ell) ** 2 * (f[:, None] ** 2 + f[None, :] ** 2) / 2)
+    x = torch.fft.ifft2(torch.fft.fft2(w) * H).real
+    return ((x - x.mean()) / x.std()).contiguous()
+
+
+def study_pressure(args):
+    """FP64 vs mixed-precision pressure solves to 1e-10 on re-seeded heterogeneous fields:
+    N^2 diagonal quarter-five-spot on the unit square, c = logistic(4 g_c) with g_c a GRF of
+    correlation length 32 cells, ln K = GRF(sigma 1, correlation length 16), M = 41
+    quarter-power mobility.  Reports ms per solve, V-cycles, and the mixed-precision solution's
+    deviation from the FP64 one."""
+    import torch
+
+    import impec2d_gb300 as E
+    from impec2d_gb300 import build as B
+    B.build()
+    N = args.n or 4096
+    ctxs = {}
+    for prec in ("fp64", "mixed"):
+        P = E.default_params(N, N, stype=E.DIAGONAL, hmtype=E.MUSCL, nu=1.0, eps=1e-10, max_cycles=200,
+                             precision=E.PREC_MIXED if prec == "mixed" else E.PREC_FP64)
+        ctxs[prec] = E.Context(P)
+    dx = 1.0 / N
+    q = torch.zeros(N * N, dtype=torch.float64, device="cuda")
+    q[0], q[-1] = 1.0 / (dx * dx), -1.0 / (dx * dx)
+    for cx in ctxs.values():
+        cx.set_source(q)
+    res = {k: {"ms": [], "cycles": [], "relres": []} for k in ctxs}
+    errs = []
+    p = {k: torch.zeros((N, N), dtype=torch.float64, device="cuda") for k in ctxs}
+    for s in range(args.solves):
+        c = torch.sigmoid(4.0 * grf(N, 32.0, 1000 + 2 * s)).contiguous()
+        K = torch.exp(grf(N, 16.0, 1001 + 2 * s)).contiguous()
+        for k, cx in ctxs.items():
+            cx.set_permeability(K, K)
+            p[k].zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            cyc, rr, _ = cx.pressure_solve(c, p[k], 1e-10)
+            e1.record()
+            torch.cuda.synchronize()
+            res[k]["ms"].append(e0.elapsed_time(e1))
+            res[k]["cycles"].append(cyc)
+            res[k]["relres"].append(rr)
+        errs.append(float(torch.linalg.vector_norm(p["mixed"] - p["fp64"]) / torch.linalg.vector_norm(p["fp64"])))
+    out = {"study": "pressure", "workload": f"{N}x{N} diagonal quarter-five-spot, c = logistic(4 GRF(l=32)), "
+                                            f"ln K = GRF(sigma=1, l=16), M=41, tol 1e-10",
+           "solves": args.solves, "data": "synthetic (seeded GRFs on the GPU)"}
+    for k, r in res.items():
+        out[k] = {"ms_per_solve_median": statistics.median(r["ms"]), "ms_per_solve_mean": statistics.mean(r["ms"]),
+                  "cycles_mean": statistics.mean(r["cycles"]), "relres_max": max(r["relres"])}
+    out["mixed_vs_fp64"] = {"speedup": out["fp64"]["ms_per_solve_median"] / out["mixed"]["ms_per_solve_median"],
+                            "rel_l2_diff_max": max(errs)}
+    print(json.dumps(out))
+    for cx in ctxs.values():
+        cx.close()
+
+
+def study_warmstart(args):
+    """V-cycles and ms per pressure solve along the 1024^2 IMPES run, zero initial guess (the
+    reference's choice) against the previous step's pressure."""
+    import numpy as np
+    import torch
+
+    import impec2d_gb300 as E
+    from impec2d_gb300 import build as B
+    B.build()
+    N = args.n or N_DEFAULT
+    out = {"study": "warmstart", "workload": f"parallel quarter-five-spot {N}x{N} (IMPES steps as in the bench)",
+           "steps": args.steps}
+    for warm in (0, 1):
+        P = workload_params(E, N, args.precision)
+        P.warm_start = warm
+        ctx = E.Context(P)
+        c0, q = initial_state(N)
+        g = 2
+        cg = np.zeros((N + 2 * g, N + 2 * g))
+        cg[g:g + N, g:g + N] = c0
+        ctx.upload(cg, q, ghost=g)
+        ctx.set_time(0.0)
+        cyc, ms = [], []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            info = ctx.step()
+            e1.record()
+            torch.cuda.synchronize()
+            cyc.append(info.its)
+            ms.append(e0.elapsed_time(e1))
+        out["previous_step" if warm else "zero"] = {"cycles_mean": statistics.mean(cyc[1:] or cyc),
+                                                    "ms_per_step_median": statistics.median(ms[1:] or ms)}
+        ctx.close()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.study == "pressure":
+        return study_pressure(args)
+    if args.study == "warmstart":
+        return study_warmstart(args)
     if args.no_graph:
         os.environ["IMPEC_NO_GRAPH"] = "1"  # read by the engine at each step
     import numpy as np
@@ -183,7 +296,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     B.build()
-    N = args.n
+    N = args.n or N_DEFAULT
     P = workload_params(E, N, args.precision)
     ctx = E.Context(P)
     c0, q = initial_state(N)
