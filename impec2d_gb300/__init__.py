@@ -103,6 +103,8 @@ _SIGS = {
     "impec_advect_symmetric_noalloc": (C.c_int, [C.POINTER(Params), _VP, _VP, _VP, C.c_double, _VP]),
     "impec_time_kernel": (C.c_int, [_VP, C.c_int, C.c_int, _PD, _PD]),
     "impec_measure_fp64": (C.c_int, [_PD]),
+    "impec_project_diagonal": (C.c_int, [_VP, C.c_int, _VP, C.c_int, C.c_int]),
+    "impec_project_diagonal_download": (C.c_int, [_VP, C.c_int, _PD, C.c_int, C.c_int]),
 }
 
 KERNELS = {0: "k_rb_face5<double> (fine RB-GS sweep, FP64)", 1: "k_rb_face5<float> (fine RB-GS sweep, FP32)",
@@ -319,6 +321,11 @@ class Context:
         ps = [C.c_void_p() for _ in range(5)]
         _chk(lib().impec_state(self.h, *[C.byref(x) for x in ps]), "state")
         return [x.value for x in ps]
+
+    def project_diagonal(self, field: int, out, dN1: int, dN2: int):
+        """Project the resident c (field 0) or p (field 1) of a parallel run onto the dN1 x dN2
+        diagonal grid (out: float64 CUDA tensor of dN1*dN2)."""
+        _chk(lib().impec_project_diagonal(self.h, field, _p(out), dN1, dN2), "project_diagonal")
 
     def pressure_solve_resident(self, sync=True):
         cyc, rr = C.c_int(), C.c_double()

@@ -75,6 +75,15 @@ void Engine::put_q(const double* qh) {
     check(impec_state_upload(ctx_, nullptr, qh, g), "upload q");
 }
 
+void Engine::project_diagonal(int field, int dN1, int dN2, Array2d& a, int bounds) {
+    std::vector<double> h((size_t)dN1 * dN2);
+    check(impec_project_diagonal_download(ctx_, field, h.data(), dN1, dN2), "project_diagonal");
+    a.resize(dN1 + 2 * bounds, dN2 + 2 * bounds, -bounds, -bounds);
+    std::fill(a.data(), a.data() + (size_t)(dN1 + 2 * bounds) * (dN2 + 2 * bounds), 0.0);
+    for (int i = 0; i < dN1; ++i)
+        for (int j = 0; j < dN2; ++j) a(i, j) = h[(size_t)i * dN2 + j];
+}
+
 // ---------------------------------------------------------------- elliptic
 EllipticSolver::EllipticSolver(SimParams* sp, Engine* eng) : sp(sp), eng(eng) { SetNu(sp->nu); }
 
@@ -401,15 +410,28 @@ void Impec2DSolver::LogResults(const std::string& postfix) {  // LogResultsMatch
     const bool final = postfix.empty();
     const std::string dir = final ? sp->results_dir : sp->log_dir;
     const std::string sfx = final ? ".dat" : postfix + ".dat";
+    if (sp->stype == PARALLEL) {
+        // parallel runs are written on the diagonal grid (Project, src/Impec2DSolver.cpp:645-666, 690-716)
+        const int dN1 = (int)std::lround(sp->N1 / std::sqrt(2.)), dN2 = (int)std::lround(sp->N2 / std::sqrt(2.));
+        const double d_dx = (sp->x_ub - sp->x_lb) / (std::sqrt(2.) * dN1);
+        const double d_dy = (sp->y_ub - sp->y_lb) / (std::sqrt(2.) * dN2);
+        Array2d diag;
+        eng->project_diagonal(0, dN1, dN2, diag, sp->c_bounds);
+        PrintDToPlotFile(dir + "/concentration" + sfx, diag, sp->x_lb, sp->y_lb, d_dx, d_dy, sp->c_bounds);
+        if (final) {
+            eng->project_diagonal(1, dN1, dN2, diag, sp->p_bounds);
+            PrintDToPlotFile(dir + "/pressure" + sfx, diag, sp->x_lb, sp->y_lb, d_dx, d_dy, sp->p_bounds);
+        }
+        return;
+    }
     eng->get_c(c);
     PrintDToPlotFile(dir + "/concentration" + sfx, c, sp->x_lb, sp->y_lb, sp->dx, sp->dy, sp->c_bounds);
     if (final) {
         eng->get_p(p);
         eng->get_v(v);
         PrintDToPlotFile(dir + "/pressure" + sfx, p, sp->x_lb, sp->y_lb, sp->dx, sp->dy, sp->p_bounds);
-        if (sp->stype != PARALLEL)
-            PrintVelToPlotFile(dir + "/velocity_u" + sfx, dir + "/velocity_v" + sfx, v, sp->x_lb, sp->y_lb, sp->dx, sp->dy,
-                               sp->v_bounds);
+        PrintVelToPlotFile(dir + "/velocity_u" + sfx, dir + "/velocity_v" + sfx, v, sp->x_lb, sp->y_lb, sp->dx, sp->dy,
+                           sp->v_bounds);
     }
 }
 

@@ -38,6 +38,9 @@ public:
     void put_v(const Array3d& v_host);
     void get_v(Array3d& v_host);
     void put_q(const double* q_host);
+    // Impec2DSolver::Project on the device: c (field 0) or p (field 1) of a parallel run onto the
+    // dN1 x dN2 diagonal grid, into `a` with a zero ghost ring of `bounds`
+    void project_diagonal(int field, int dN1, int dN2, Array2d& a, int bounds);
     int N1, N2, g;
 
 private:

@@ -106,6 +106,8 @@ struct DevScalars {
     double fsum, fnorm2, rnorm2, pin_value;  // fsum,fnorm2 adjacent: written as a pair
     double red[8];
     double relres, cn_relres, t_clip;
+    double pcg_rz, pcg_zq;  // (r, z) and (z, q_old) of the current CG iteration (written as a pair)
+    double pcg_pq, pcg_alpha, pcg_rz_old;
     int mg_cycles, cn_cycles, cn_cycles_total, flags, go, clipped, steps;
     long long graph_launches;  // kernels executed by step-graph replays
 };
@@ -128,6 +130,10 @@ struct impec_ctx {
     double *f = nullptr, *r = nullptr;            // integrated rhs, FP64 residual
     std::vector<impec::Level> L;
     double* dense_inv = nullptr;                  // coarsest-level inverse (n x n)
+    // V-cycle preconditioned conjugate gradients: iterate, search direction, A p
+    double *cg_x = nullptr, *cg_p = nullptr, *cg_q = nullptr;
+    int krylov = 1;  // 1: CG with one V-cycle as preconditioner; 0: stationary V-cycles
+    double solve_tol = 1e-10;  // tolerance of the pressure solve being launched or captured
     int dense_n = 0;
     int pin_i = 1, pin_j = 1;
     double pin_kappa = 1.0;

@@ -466,12 +466,14 @@ __global__ void k_dense_solve(int n, const double* __restrict__ Dinv, const T* _
 // one; optionally stores r as FP32 for the mixed-precision correction cycle.
 __global__ void __launch_bounds__(RED_THREADS) k_fine_resid(Level F, const double* __restrict__ f,
                                                             const double* __restrict__ x, int pin,
-                                                            float* __restrict__ r32, double* partials, int mb,
-                                                            unsigned* counter, double* out) {
+                                                            float* __restrict__ r32, double* __restrict__ r64,
+                                                            double* partials, int mb, unsigned* counter,
+                                                            double* out) {
     pdl_enter();
     double acc[1] = {0.0};
     for_cells(F.n1, F.n2, [&](int i, int j, size_t k) {
         double r = resid<double>(F, i, j, F.tx, F.ty, F.a9, F.diag, f, x);
+        if (r64) r64[k] = r;
         if (r32) r32[k] = (float)r;  // consistent rhs of the singular correction equation
         if ((int)k == pin) r = 0.0;  // the pinned row of the reference system has zero residual
         acc[0] += r * r;
@@ -606,6 +608,14 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         n2 = (n2 + 1) / 2;
     }
     ctx->dense_n = ctx->L.back().n1 * ctx->L.back().n2;
+    {
+        const size_t nf = ctx->L[0].n();
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->cg_x, nf * 8));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->cg_p, nf * 8));
+        IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->cg_q, nf * 8));
+        IMPEC_CUDA_TRY(cudaMemset(ctx->cg_q, 0, nf * 8));
+        ctx->krylov = (int)env_long("IMPEC_MG_KRYLOV", 1) != 0;
+    }
     IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dense_inv, (size_t)ctx->dense_n * ctx->dense_n * 8 * 2));
     IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_dense_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 64 * 8));
     const int cs = (int)MG_COARSE_SMEM;
@@ -639,7 +649,7 @@ void pressure_free(impec_ctx* ctx) {
             if (p) cudaFree(p);
     }
     ctx->L.clear();
-    void* ps[] = {ctx->cm11, ctx->cm22, ctx->cm12, ctx->dense_inv};
+    void* ps[] = {ctx->cm11, ctx->cm22, ctx->cm12, ctx->dense_inv, ctx->cg_x, ctx->cg_p, ctx->cg_q};
     for (void* p : ps)
         if (p) cudaFree(p);
 }
@@ -941,22 +951,149 @@ static void vcycle(impec_ctx* ctx, size_t l) {
 
 // Convergence check of the multigrid loop (one thread): relres = ||r||/||f||; decides whether
 // another cycle runs and, inside a graph, sets the WHILE node's condition.
+// Convergence check of the solve loop (one thread): relres = ||r||/||f||; decides whether
+// another cycle runs and, inside a graph, sets the WHILE node's condition.  With CG
+// (krylov) and after an iteration, it also keeps the iteration's alpha and (r, z) for the
+// next search direction, and stops on a breakdown ((p, Ap) <= 0).
 __global__ void k_mg_check(DevScalars* S, double tol, int max_cycles, int inc, cudaGraphConditionalHandle h,
-                           int use_h) {
+                           int use_h, int krylov) {
     pdl_enter();
-    if (inc) S->mg_cycles++;
+    bool breakdown = false;
+    if (inc) {
+        S->mg_cycles++;
+        if (krylov) {
+            breakdown = !(S->pcg_pq > 0.0);
+            S->pcg_alpha = breakdown ? 0.0 : S->pcg_rz / S->pcg_pq;
+            S->pcg_rz_old = S->pcg_rz;
+        }
+    }
     double fn = S->fnorm2, rn = S->rnorm2;
     double rr = fn > 0 ? sqrt(rn / fn) : sqrt(rn);
     S->relres = rr;
     const bool bad = !(rr == rr) || isinf(rr);
-    const bool go = !bad && rr > tol && S->mg_cycles < max_cycles;
+    const bool go = !bad && !breakdown && rr > tol && S->mg_cycles < max_cycles;
     if (bad) S->flags |= FLAG_MG_NAN;
     else if (!go && rr > tol) S->flags |= FLAG_MG_NOT_CONVERGED;
     S->go = go ? 1 : 0;
     if (use_h) cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
+// ---------------------------------------------------------------- V-cycle preconditioned CG
+// The reference solves the pressure system with CG preconditioned by HYPRE's SMG
+// (src/MGSolver.cpp:594-629); here the preconditioner is one V(2,2) cycle of the engine's own
+// multigrid, z = M^-1 r, in FP64 or (mixed precision) in FP32 on the FP32 copy of r.  CG runs
+// in FP64 on the consistent singular system.  Because the FP32 cycle is not an exactly
+// symmetric operator, the direction uses the flexible (Polak-Ribiere) coefficient
+//   beta = (z_k, r_k - r_{k-1}) / (z_{k-1}, r_{k-1}) = -alpha_{k-1} (z_k, A p_{k-1}) / (z_{k-1}, r_{k-1}),
+// which needs only (z, r) and (z, q) with q = A p still holding the previous direction.
+
+// z: the V-cycle's finest iterate, FP64 or FP32.
+__device__ __forceinline__ double cg_z(const double* __restrict__ z, const float* __restrict__ z32, size_t k) {
+    return z32 ? (double)z32[k] : z[k];
+}
+
+// (r, z) and (z, q) into out[0], out[1].
+__global__ void __launch_bounds__(RED_THREADS) k_cg_dots(int n1, int n2, const double* __restrict__ r,
+                                                         const double* __restrict__ z, const float* __restrict__ z32,
+                                                         const double* __restrict__ q, double* partials, int mb,
+                                                         unsigned* counter, double* out) {
+    pdl_enter();
+    double acc[2] = {0.0, 0.0};
+    for_cells(n1, n2, [&](int, int, size_t k) {
+        const double zz = cg_z(z, z32, k);
+        acc[0] += r[k] * zz;
+        acc[1] += zz * q[k];
+    });
+    grid_reduce<2>(acc, 0u, partials, mb, counter, out);
+}
+
+// p = z + beta p (p = z on the first iteration, whatever p held).
+__global__ void k_cg_direction(size_t n, const double* __restrict__ z, const float* __restrict__ z32,
+                               double* __restrict__ p, const DevScalars* __restrict__ S) {
+    pdl_enter();
+    const bool first = S->mg_cycles == 0 || S->pcg_rz_old == 0.0;
+    const double beta = first ? 0.0 : -S->pcg_alpha * S->pcg_zq / S->pcg_rz_old;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        p[k] = first ? cg_z(z, z32, k) : cg_z(z, z32, k) + beta * p[k];
+}
+
+// q = A p with the integrated operator (diag p - sum t p_nb) and (p, q) into out[0].
+__global__ void __launch_bounds__(RED_THREADS) k_cg_apply(Level F, const double* __restrict__ p,
+                                                          double* __restrict__ q, double* partials, int mb,
+                                                          unsigned* counter, double* out) {
+    pdl_enter();
+    double acc[1] = {0.0};
+    for_cells(F.n1, F.n2, [&](int i, int j, size_t k) {
+        const int n1 = F.n1, n2 = F.n2;
+        double s = F.diag[k] * p[k];
+        if (F.kind == FACE5) {
+            if (i > 0) s -= F.tx[k] * p[k - n2];
+            if (i < n1 - 1) s -= F.tx[k + n2] * p[k + n2];
+            if (j > 0) s -= F.ty[IX(i, j, n2 + 1)] * p[k - 1];
+            if (j < n2 - 1) s -= F.ty[IX(i, j + 1, n2 + 1)] * p[k + 1];
+        } else {
+            const size_t n = (size_t)n1 * n2;
+            for (int e = 1; e < 9; ++e) {
+                const int ii = i + c_off[e][0], jj = j + c_off[e][1];
+                if (ii < 0 || ii >= n1 || jj < 0 || jj >= n2) continue;
+                s += F.a9[e * n + k] * p[IX(ii, jj, n2)];
+            }
+        }
+        q[k] = s;
+        acc[0] += p[k] * s;
+    });
+    grid_reduce<1>(acc, 0u, partials, mb, counter, out);
+}
+
+// alpha = (r, z) / (p, Ap); x += alpha p; r -= alpha Ap (and its FP32 copy); ||r||^2 over the
+// cells other than the pinned one.
+__global__ void __launch_bounds__(RED_THREADS) k_cg_update(int n1, int n2, double* __restrict__ x,
+                                                           double* __restrict__ r, float* __restrict__ r32,
+                                                           const double* __restrict__ p, const double* __restrict__ q,
+                                                           int pin, const DevScalars* __restrict__ S,
+                                                           double* partials, int mb, unsigned* counter, double* out) {
+    pdl_enter();
+    const double pq = S->pcg_pq;
+    const double alpha = pq > 0.0 ? S->pcg_rz / pq : 0.0;
+    double acc[1] = {0.0};
+    for_cells(n1, n2, [&](int, int, size_t k) {
+        x[k] += alpha * p[k];
+        const double rr = r[k] - alpha * q[k];
+        r[k] = rr;
+        if (r32) r32[k] = (float)rr;
+        if ((int)k != pin) acc[0] += rr * rr;
+    });
+    grid_reduce<1>(acc, 0u, partials, mb, counter, out);
+}
+
+// Relative residual of the returned iterate (true residual, recomputed after the loop).
+__global__ void k_true_relres(DevScalars* S, double tol) {
+    pdl_enter();
+    const double fn = S->fnorm2, rn = S->rnorm2;
+    const double rr = fn > 0 ? sqrt(rn / fn) : sqrt(rn);
+    S->relres = rr;
+    if (!(rr == rr) || isinf(rr)) S->flags |= FLAG_MG_NAN;
+    else if (rr > 2.0 * tol && !(S->flags & FLAG_MG_NOT_CONVERGED)) S->flags |= FLAG_MG_NOT_CONVERGED;
+}
+
 static int pin_index(impec_ctx* ctx) { return (int)IX(ctx->pin_i, ctx->pin_j, ctx->L[0].n2); }
+
+// The iterate the loop updates: CG keeps it in its own buffer (the finest level's iterate is
+// the preconditioner's output), stationary cycles update the finest iterate itself.
+static double* solve_iterate(impec_ctx* ctx) { return ctx->krylov ? ctx->cg_x : ctx->L[0].x; }
+
+// FP64 residual r = f - A x of the iterate and ||r||^2, optionally stored in FP32 (r32: the
+// rhs of the mixed-precision cycle) and in FP64 (r64: the CG residual).
+static impec_status fine_residual(impec_ctx* ctx, const double* x, float* r32, double* r64) {
+    Level& F = ctx->L[0];
+    ++ctx->nlaunch;
+    // about seven cells per thread: the FP64 warp sums of the reduction stay small beside the residual
+    const int blocks = seg_blocks(F.n1, F.n2, red_cap(ctx->num_sms, ctx->max_blocks));
+    launch_k(ctx->stream, k_fine_resid, blocks, RED_THREADS, 0, F, ctx->f, x, pin_index(ctx), r32, r64,
+             ctx->partials, ctx->max_blocks, ctx->counter, &ctx->dscal->rnorm2);
+    IMPEC_LAUNCH_CHECK();
+    return IMPEC_OK;
+}
 
 // Operator, hierarchy, consistent rhs, initial iterate and initial residual (launch only).
 impec_status pressure_prepare(impec_ctx* ctx, const double* c, const double* p) {
@@ -967,65 +1104,98 @@ impec_status pressure_prepare(impec_ctx* ctx, const double* c, const double* p) 
     const int pin = pin_index(ctx);
     DevScalars* S = ctx->dscal;
     ++ctx->nlaunch;
-    launch_k(ctx->stream, k_rhs, flat_blocks(n, red_cap(ctx->num_sms, ctx->max_blocks)), RED_THREADS, 0, n, ctx->q, ctx->G.dA, ctx->f, ctx->partials, ctx->max_blocks,
-                                                ctx->counter, &S->fsum);
+    launch_k(ctx->stream, k_rhs, flat_blocks(n, red_cap(ctx->num_sms, ctx->max_blocks)), RED_THREADS, 0, n, ctx->q,
+             ctx->G.dA, ctx->f, ctx->partials, ctx->max_blocks, ctx->counter, &S->fsum);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_fix_pin, 1, 1, 0, ctx->f, ctx->q, pin, ctx->G.dA, ctx->pin_kappa, S);
     IMPEC_LAUNCH_CHECK();
+    double* x = solve_iterate(ctx);
     if (P.warm_start)
-        IMPEC_CUDA_TRY(cudaMemcpyAsync(F.x, p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(x, p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     else
-        IMPEC_CUDA_TRY(cudaMemsetAsync(F.x, 0, n * 8, ctx->stream));
-    IMPEC_CUDA_TRY(cudaMemcpyAsync(F.b, ctx->f, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        IMPEC_CUDA_TRY(cudaMemsetAsync(x, 0, n * 8, ctx->stream));
+    if (!ctx->krylov) IMPEC_CUDA_TRY(cudaMemcpyAsync(F.b, ctx->f, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     IMPEC_CUDA_TRY(cudaMemsetAsync(&S->mg_cycles, 0, sizeof(int), ctx->stream));
+    const bool mixed = P.precision == IMPEC_PREC_MIXED;
+    if (ctx->krylov) return fine_residual(ctx, x, mixed ? F.b32 : nullptr, mixed ? ctx->r : F.b);
     return pressure_residual(ctx);
 }
 
-// FP64 fine residual and its norm (r32 for the mixed-precision correction).
+// FP64 fine residual and its norm of the stationary iteration (r32 for the mixed correction).
 impec_status pressure_residual(impec_ctx* ctx) {
     Level& F = ctx->L[0];
-    const bool mixed = ctx->P.precision == IMPEC_PREC_MIXED;
-    ++ctx->nlaunch;
-    // about seven cells per thread: the FP64 warp sums of the reduction stay small beside the residual
-    const int blocks = seg_blocks(F.n1, F.n2, red_cap(ctx->num_sms, ctx->max_blocks));
-    launch_k(ctx->stream, k_fine_resid, blocks, RED_THREADS, 0, F, ctx->f, F.x, pin_index(ctx),
-                                                                  mixed ? F.b32 : nullptr, ctx->partials,
-                                                                  ctx->max_blocks, ctx->counter, &ctx->dscal->rnorm2);
-    IMPEC_LAUNCH_CHECK();
-    return IMPEC_OK;
+    return fine_residual(ctx, F.x, ctx->P.precision == IMPEC_PREC_MIXED ? F.b32 : nullptr, nullptr);
 }
 
 impec_status pressure_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h) {
+    ctx->solve_tol = tol;
     ++ctx->nlaunch;
-    launch_k(ctx->stream, k_mg_check, 1, 1, 0, ctx->dscal, tol, ctx->P.max_cycles, inc, h, use_h);
+    launch_k(ctx->stream, k_mg_check, 1, 1, 0, ctx->dscal, tol, ctx->P.max_cycles, inc, h, use_h, ctx->krylov);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
 
-// One multigrid cycle on the current iterate followed by the new residual (launch only).
+// One iteration on the current iterate followed by the new residual (launch only): a
+// stationary V-cycle, or a CG step preconditioned by one V-cycle.
 impec_status pressure_iteration(impec_ctx* ctx) {
     Level& F = ctx->L[0];
     const size_t n = F.n();
-    if (ctx->P.precision == IMPEC_PREC_MIXED) {
+    const bool mixed = ctx->P.precision == IMPEC_PREC_MIXED;
+    if (!ctx->krylov) {
+        if (mixed) {
+            IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
+            vcycle<float>(ctx, 0);
+            ++ctx->nlaunch;
+            launch_k(ctx->stream, k_add_f32, ctx->num_sms * 4, 256, 0, n, F.x, F.x32);
+            IMPEC_LAUNCH_CHECK();
+            return pressure_residual(ctx);
+        }
+        vcycle<double>(ctx, 0);
+        IMPEC_LAUNCH_CHECK();
+        return pressure_residual(ctx);
+    }
+    DevScalars* S = ctx->dscal;
+    double* r = mixed ? ctx->r : F.b;
+    const double* z = mixed ? nullptr : F.x;
+    const float* z32 = mixed ? F.x32 : nullptr;
+    if (mixed) {
         IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
         vcycle<float>(ctx, 0);
-        ++ctx->nlaunch;
-        launch_k(ctx->stream, k_add_f32, ctx->num_sms * 4, 256, 0, n, F.x, F.x32);
     } else {
+        IMPEC_CUDA_TRY(cudaMemsetAsync(F.x, 0, n * 8, ctx->stream));
         vcycle<double>(ctx, 0);
     }
+    const int cap = red_cap(ctx->num_sms, ctx->max_blocks), blocks = seg_blocks(F.n1, F.n2, cap);
+    ++ctx->nlaunch;
+    launch_k(ctx->stream, k_cg_dots, blocks, RED_THREADS, 0, F.n1, F.n2, r, z, z32, ctx->cg_q, ctx->partials,
+             ctx->max_blocks, ctx->counter, &S->pcg_rz);
+    ++ctx->nlaunch;
+    launch_k(ctx->stream, k_cg_direction, ctx->num_sms * 4, 256, 0, n, z, z32, ctx->cg_p, S);
+    ++ctx->nlaunch;
+    launch_k(ctx->stream, k_cg_apply, blocks, RED_THREADS, 0, F, ctx->cg_p, ctx->cg_q, ctx->partials,
+             ctx->max_blocks, ctx->counter, &S->pcg_pq);
+    ++ctx->nlaunch;
+    launch_k(ctx->stream, k_cg_update, blocks, RED_THREADS, 0, F.n1, F.n2, ctx->cg_x, r, mixed ? F.b32 : nullptr,
+             ctx->cg_p, ctx->cg_q, pin_index(ctx), S, ctx->partials, ctx->max_blocks, ctx->counter, &S->rnorm2);
     IMPEC_LAUNCH_CHECK();
-    return pressure_residual(ctx);
+    return IMPEC_OK;
 }
 
-// Constant shift to the pinned value and copy to p (launch only).
+// Constant shift to the pinned value and copy to p (launch only).  After CG the residual of
+// the returned iterate is recomputed, so the reported relres is the true one.
 impec_status pressure_finish(impec_ctx* ctx, double* p) {
     Level& F = ctx->L[0];
     const size_t n = F.n();
+    double* x = solve_iterate(ctx);
+    if (ctx->krylov) {
+        IMPEC_TRY(fine_residual(ctx, x, nullptr, nullptr));
+        ++ctx->nlaunch;
+        launch_k(ctx->stream, k_true_relres, 1, 1, 0, ctx->dscal, ctx->solve_tol);
+    }
     ++ctx->nlaunch;
-    launch_k(ctx->stream, k_shift, ctx->num_sms * 4, 256, 0, n, F.x, pin_index(ctx), ctx->dscal);
+    launch_k(ctx->stream, k_shift, ctx->num_sms * 4, 256, 0, n, x, pin_index(ctx), ctx->dscal);
     IMPEC_LAUNCH_CHECK();
-    IMPEC_CUDA_TRY(cudaMemcpyAsync(p, F.x, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(p, x, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     return IMPEC_OK;
 }
 
@@ -1041,6 +1211,7 @@ impec_status pressure_solve(impec_ctx* ctx, const double* c, double* p, double t
         IMPEC_TRY(pressure_check(ctx, tol, 1, 0, 0));
     }
     IMPEC_TRY(pressure_finish(ctx, p));
+    IMPEC_TRY(sync_scalars(ctx));
     const int k = ctx->hscal->mg_cycles;
     const double rr = ctx->hscal->relres;
     if (cycles) *cycles = k;

@@ -172,6 +172,15 @@ impec_status impec_launch_count(impec_ctx* ctx, long long* n);
 impec_status impec_time_kernel(impec_ctx* ctx, int which, int reps, double* ms_per_launch,
                                double* bytes_per_launch);
 
+/* Output projection of a parallel-orientation run onto the diagonal grid: Impec2DSolver::Project
+ * + ParallelProjector::FillDiagonal (src/Impec2DSolver.cpp:690-716,
+ * src/ParallelProjector.cpp:95-199).  field 0 = the resident c, 1 = the resident p; out_dev
+ * receives d_N1*d_N2 FP64 values, row-major (the reference uses d_N = round(N / sqrt 2)).  The
+ * parallel field's ghost ring is its Neumann mirror.  Enqueued on the context's stream. */
+impec_status impec_project_diagonal(impec_ctx* ctx, int field, double* out_dev, int d_N1, int d_N2);
+/* The same into a host buffer of d_N1*d_N2 values (d_N1*d_N2 <= N1*N2); returns when it is filled. */
+impec_status impec_project_diagonal_download(impec_ctx* ctx, int field, double* out_host, int d_N1, int d_N2);
+
 /* FP64 fused multiply-adds per second that the current device sustains (eight independent
  * chains per thread on every SM): the denominator of the FP64-pipe fractions reported beside
  * the HBM roofline.  No counterpart in the reference. */

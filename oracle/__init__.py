@@ -93,6 +93,7 @@ def _declare(L):
     d("or_pressure_matrix_neumann", None, _PP, _D, _D)
     d("or_pressure_rhs", None, _PP, _D, _D)
     d("or_face_mobility", None, _PP, _D, _D, _D)
+    d("or_project_diagonal", None, _PP, _D, C.c_int, C.c_int, _D)
     d("or_matvec9", None, _PP, _D, _D, _D)
     d("or_relres9", C.c_double, _PP, _D, _D, _D)
     d("or_solve_banded", C.c_int, _PP, _D, _D, _D)

@@ -130,6 +130,10 @@ double or_exact_vol_frac_circle(double x1, double y1, double r, double dx, doubl
 /* profile: 0 sine, 1 tophat, 2 gaussbell, 3 vertical sine, 4 diagonal sine */
 double or_profile(const or_params* P, int profile, double x, double y);
 double or_advection_norm(const or_params* P, const double* c, int profile, int norm);
+/* ParallelProjector (src/ParallelProjector.cpp:51-199, src/Impec2DSolver.cpp:690-716):
+ * bilinear projection of a parallel-orientation field f (Blitz layout with ghosts, ghost ring
+ * already filled) onto the dN1 x dN2 diagonal grid; out is dN1*dN2, row-major. */
+void or_project_diagonal(const or_params* P, const double* f, int dN1, int dN2, double* out);
 /* Elliptic manufactured test (src/EllipticSolver.cpp:155-311) at the grid in P. */
 int or_elliptic_test(const or_params* P, double* errs3);
 

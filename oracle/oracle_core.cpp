@@ -1066,4 +1066,33 @@ double or_advection_norm(const or_params* P, const double* cflat, int profile, i
     return s * G.dx * G.dy;
 }
 
+// ParallelProjector::FillDiagonal + GetFromParallel (src/ParallelProjector.cpp:95-199), with
+// the projector set up as in Impec2DSolver::Project (src/Impec2DSolver.cpp:690-716): angle
+// -pi/4, parallel resolution N1 x N2, diagonal spacing L / (sqrt 2 dN).
+void or_project_diagonal(const or_params* P, const double* f, int dN1, int dN2, double* out) {
+    const int g = P->g, N2g = P->N2 + 2 * g;
+    auto at = [&](int i, int j) { return f[(size_t)(i + g) * N2g + (j + g)]; };
+    const double angle = -M_PI / 4.;
+    const double pN1 = P->N1, pN2 = P->N2;
+    const double p_dx = (P->x_ub - P->x_lb) / pN1, p_dy = (P->y_ub - P->y_lb) / pN2;
+    const double d_dx = (P->x_ub - P->x_lb) / (sqrt(2.) * dN1), d_dy = (P->y_ub - P->y_lb) / (sqrt(2.) * dN2);
+    auto centred = [](double lb, double dx, int idx) { return lb + (idx + 0.5) * dx; };
+    for (int i = 0; i < dN1; ++i)
+        for (int j = 0; j < dN2; ++j) {
+            const double xd = centred(P->x_lb, d_dx, i), yd = centred(P->y_lb, d_dy, j);
+            const double x = cos(angle) * xd - sin(angle) * yd;
+            double y = sin(angle) * xd + cos(angle) * yd;
+            y = fabs(y);
+            const int x00 = (int)floor(x / (P->x_ub - P->x_lb) * pN1);
+            const int y00 = (int)floor(y / (P->y_ub - P->y_lb) * pN2);
+            const int x11 = x00 + 1, y11 = y00 + 1;
+            const double x_00 = centred(P->x_lb, p_dx, x00), x_11 = centred(P->x_lb, p_dx, x11);
+            const double y_00 = centred(P->y_lb, p_dy, y00), y_11 = centred(P->y_lb, p_dy, y11);
+            out[(size_t)i * dN2 + j] = 1. / ((x_11 - x_00) * (y_11 - y_00)) * (x_11 - x) * (y_11 - y) * at(x00, y00) +
+                                       1. / ((x_11 - x_00) * (y_11 - y_00)) * (x - x_00) * (y_11 - y) * at(x11, y00) +
+                                       1. / ((x_11 - x_00) * (y_11 - y_00)) * (x_11 - x) * (y - y_00) * at(x00, y11) +
+                                       1. / ((x_11 - x_00) * (y_11 - y_00)) * (x - x_00) * (y - y_00) * at(x11, y11);
+        }
+}
+
 }  // extern "C"

@@ -184,3 +184,48 @@ def test_quarter_circle_wells_balance(oracle_lib):
         nwell = 1 if stype == O.DIAGONAL else 2
         dA = (1.0 / 64) ** 2
         assert q[q > 0].sum() * dA == pytest.approx(nwell * P.I, rel=1e-12)
+
+
+def _project(L, P, interior, dN1, dN2):
+    f = cell_ghost(P, interior)
+    out = np.zeros(dN1 * dN2)
+    L.or_project_diagonal(C.byref(P), O.ptr(f), dN1, dN2, O.ptr(out))
+    return out.reshape(dN1, dN2)
+
+
+@pytest.mark.parametrize("N", [64, 101])
+def test_parallel_projection_reproduces_constant_and_linear_fields(oracle_lib, N):
+    """ParallelProjector (src/ParallelProjector.cpp:95-199): bilinear interpolation keeps a
+    constant, and reproduces a field linear in the parallel coordinates at every diagonal
+    cell whose four source cells are interior."""
+    math_sqrt2 = np.sqrt(2.0)
+    P = O.make_params(N1=N, N2=N, x_ub=math_sqrt2, y_ub=math_sqrt2, stype=O.PARALLEL)
+    dN = int(round(N / np.sqrt(2.0)))
+    out = _project(oracle_lib, P, np.full((N, N), 0.37), dN, dN)
+    assert np.allclose(out, 0.37, rtol=0, atol=1e-15)
+    h = math_sqrt2 / N
+    xc = (np.arange(N) + 0.5) * h
+    lin = 2.0 * xc[:, None] - 3.0 * xc[None, :] + 1.0
+    out = _project(oracle_lib, P, lin, dN, dN)
+    dd = math_sqrt2 / (np.sqrt(2.0) * dN)
+    xd = (np.arange(dN) + 0.5) * dd
+    X = (xd[:, None] + xd[None, :]) / np.sqrt(2.0)
+    Y = np.abs(xd[None, :] - xd[:, None]) / np.sqrt(2.0)
+    inside = (np.floor(X / math_sqrt2 * N) + 1 < N) & (np.floor(Y / math_sqrt2 * N) + 1 < N)
+    exact = 2.0 * X - 3.0 * Y + 1.0
+    assert inside.mean() > 0.95
+    assert np.max(np.abs(out - exact)[inside]) < 1e-12
+
+
+def test_parallel_projection_uses_the_mirror_symmetry(oracle_lib):
+    """The projector folds negative y onto |y| (GetFromParallel, src/ParallelProjector.cpp:95-97),
+    so the diagonal image of a parallel field is symmetric about i = j -- up to the
+    reference's rounding: cos(-pi/4) and -sin(-pi/4) differ in the last bit, and where the
+    rotated coordinate lands on a cell boundary, floor() picks a different bilinear stencil
+    for (i, j) and (j, i).  That happens in under 2 % of the cells."""
+    N = 80
+    P = O.make_params(N1=N, N2=N, x_ub=np.sqrt(2.0), y_ub=np.sqrt(2.0), stype=O.PARALLEL)
+    dN = int(round(N / np.sqrt(2.0)))
+    out = _project(oracle_lib, P, smooth_field(N, N, 5), dN, dN)
+    d = np.abs(out - out.T)
+    assert (d > 1e-12).mean() < 0.02 and d.max() < 1e-2
