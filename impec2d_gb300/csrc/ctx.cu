@@ -131,7 +131,10 @@ static impec_status validate(const impec_params* P) {
         return IMPEC_ERR_ARG;
     }
     if (P->dim_splitting < 0 || P->dim_splitting > 4) { set_error("unknown dimensional_splitting"); return IMPEC_ERR_ARG; }
-    if (P->stype == IMPEC_HORIZONTAL) { set_error("source_type horizontal is not supported by the device path"); return IMPEC_ERR_ARG; }
+    if (P->stype == IMPEC_HORIZONTAL && (P->N1 < 4 || P->bc != IMPEC_BC_NEUMANN)) {
+        set_error("source_type horizontal needs N1 >= 4 and Neumann boundaries");
+        return IMPEC_ERR_ARG;
+    }
     if (P->precision != IMPEC_PREC_FP64 && P->precision != IMPEC_PREC_MIXED) { set_error("unknown precision"); return IMPEC_ERR_ARG; }
     return IMPEC_OK;
 }
@@ -190,6 +193,11 @@ impec_status impec_ctx_create(const impec_params* P, void* stream, impec_ctx** o
     cudaMemsetAsync(ctx->v, 0, nv * 8, ctx->stream);
     ctx->pin_i = 1;
     ctx->pin_j = 1;
+    if (P->stype == IMPEC_HORIZONTAL) {
+        ctx->dir_row = 1;
+        ctx->cn_dir_row = P->N1 - 2;
+        ctx->singular = 0;
+    }
     impec_status s = pressure_alloc(ctx);
     if (s != IMPEC_OK) return fail(s);
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
@@ -264,7 +272,15 @@ impec_status impec_set_source(impec_ctx* ctx, const double* q_dev) {
             idx.push_back((int)k);
             val.push_back(hq[k]);
         }
+    if (ctx->have_source && idx == ctx->well_idx_host) {
+        // same wells, new rates (e.g. the pulsing or linear horizontal front, src/Impec2DSolver.cpp:437-439):
+        // the step graph reads q and the rates from device memory, so it stays valid
+        if (ctx->nwells)
+            IMPEC_CUDA_TRY(cudaMemcpy(ctx->well_q, val.data(), val.size() * 8, cudaMemcpyHostToDevice));
+        return IMPEC_OK;
+    }
     invalidate_step_graph(ctx);
+    ctx->well_idx_host = idx;
     if (ctx->well_idx) cudaFree(ctx->well_idx);
     if (ctx->well_q) cudaFree(ctx->well_q);
     ctx->well_idx = nullptr;

@@ -73,6 +73,8 @@ struct CNArgs {
     double kxy;    // 1 / (dx dy)
     double k2xx;   // 1 / (2 dx dx)
     double k2yy;   // 1 / (2 dy dy)
+    double dA;     // dx dy
+    int dir_row;   // horizontal source: row N1-2 is Dirichlet, c = 0 (src/MGSolver.cpp:1295-1317, 1361-1367); else -1
 };
 
 // GetCoefficients_Parabolic (src/MGSolver.cpp:923-948) with the Neumann folding of
@@ -111,6 +113,7 @@ __global__ void k_cn_matrix(CNArgs A, const double* __restrict__ dfx, const doub
     if (k == 0 && l == n2 - 1) set(C + W + N + NW, 0, 0, S + SW, SE, E + NE, 0, 0, 0);
     if (k == n1 - 1 && l == n2 - 1) set(C + N + NE + E, W + NW, SW, S + SE, 0, 0, 0, 0, 0);
     if (k == n1 - 1 && l == 0) set(C + S + E + SE, W + SW, 0, 0, 0, 0, 0, N + NE, NW);
+    if (i == A.dir_row) set(1. / A.dA, 0, 0, 0, 0, 0, 0, 0, 0);
     const size_t n = (size_t)n1 * n2, kk = IX(i, j, n2);
     for (int e = 0; e < 9; ++e) a9[e * n + kk] = o[e];
     idiag[kk] = 1.0 / o[0];
@@ -137,7 +140,7 @@ __global__ void k_cn_rhs(CNArgs A, const double* __restrict__ dfx, const double*
     double t3 = A.kxy * (d21_jp * (cc(ip, j) + cc(ip, jp) - cc(im, jp) - cc(im, j)) -
                          d21_jm * (cc(ip, j) + cc(ip, jm) - cc(im, j) - cc(im, jm)));
     double t4 = A.k4yy * (d22_jp * (cc(i, jp) - c0) - d22_jm * (c0 - cc(i, jm)));
-    rhs[IX(i, j, n2)] = c0 + dt * 0.125 * (t1 + t2 + t3 + t4);
+    rhs[IX(i, j, n2)] = i == A.dir_row ? 0.0 : c0 + dt * 0.125 * (t1 + t2 + t3 + t4);
 }
 
 __device__ __forceinline__ double cn_off(int i, int j, int n1, int n2, const double* __restrict__ a9,
@@ -204,7 +207,7 @@ __global__ void k_cn_check(DevScalars* S, double tol, int max_its, int inc, cuda
 static CNArgs cn_args(impec_ctx* ctx) {
     const Geo& G = ctx->G;
     return CNArgs{ctx->P.N1, ctx->P.N2, 1. / (8. * G.dx * G.dy), 4. / (G.dx * G.dx), 4. / (G.dy * G.dy),
-                  1. / (G.dx * G.dy), 1. / (2. * G.dx * G.dx), 1. / (2. * G.dy * G.dy)};
+                  1. / (G.dx * G.dy), 1. / (2. * G.dx * G.dx), 1. / (2. * G.dy * G.dy), G.dx * G.dy, ctx->cn_dir_row};
 }
 
 // Peaceman face tensors and the CN matrix for the half step dt = scale * dt_dev (launch only).

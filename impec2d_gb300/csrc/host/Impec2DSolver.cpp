@@ -500,6 +500,10 @@ bool Impec2DSolver::Solve(bool quiet) {  // src/Impec2DSolver.cpp:293-466, resid
             if (is_step || (sp->log_skip_steps != 0 && (counter == 1 || counter % sp->log_skip_steps == 0)))
                 LogResults("_" + std::to_string(counter));
         }
+        if (sp->stype == HORIZONTAL && sp->im != CONSTANT) {  // src/Impec2DSolver.cpp:437-439
+            InitializeSourceTerm(*sp, q.data(), t);
+            eng->put_q(q.data());  // same well cells: the step graph is kept, only the rates change
+        }
     }
     if (counter > 0) avg_fill /= counter;
     if (myid == 0) {

@@ -61,7 +61,8 @@ struct Level {
     double* ty = nullptr;    // FACE5: n1*(n2+1)
     double* a9 = nullptr;    // EXP9: 9 planes of n1*n2, folded (no coupling outside the grid)
     double* idiag = nullptr; // 1 / diagonal
-    double* diag = nullptr;  // diagonal (FACE5: sum of the four faces; EXP9: plane 0)
+    double* diag = nullptr;  // diagonal (FACE5: sum of the four faces + ed; EXP9: plane 0)
+    double* ed = nullptr;    // FACE5 with a Dirichlet row: couplings to known cells, moved to the diagonal
     double *x = nullptr, *b = nullptr;
     // FP32 copies for the mixed-precision cycle
     float *tx32 = nullptr, *ty32 = nullptr, *a932 = nullptr, *idiag32 = nullptr, *diag32 = nullptr;
@@ -137,10 +138,18 @@ struct impec_ctx {
     int dense_n = 0;
     int pin_i = 1, pin_j = 1;
     double pin_kappa = 1.0;
+    // source_type horizontal: Dirichlet row dir_row of the pressure system (cells (1, j),
+    // src/MGSolver.cpp:119-140) and of the CN system (cells (N1-2, j), :133-139); -1 otherwise
+    int dir_row = -1, cn_dir_row = -1;
+    int singular = 1;            // the pressure system is the singular Neumann one (no Dirichlet row)
+    int eliminate = 1;           // remove the known cells from the operator (off only to apply the reference matrix)
+    unsigned char* dmask = nullptr;  // finest level: 1 at known (Dirichlet) cells
+    double* dfd = nullptr;           // finest level: rhs additions from known neighbours; the value at known cells
     // transport scratch
     double *t1 = nullptr, *t2 = nullptr, *t3 = nullptr;
     // wells (TR integrator)
     int nwells = 0;
+    std::vector<int> well_idx_host;  // host copy of the well cells (a source with the same cells keeps the graph)
     int* well_idx = nullptr;
     double* well_q = nullptr;
     // dispersion

@@ -189,8 +189,8 @@ __global__ void k_face5_coarsen(int n1f, int n2f, const double* __restrict__ txf
     }
 }
 
-__global__ void k_exp9_coarsen(int n1f, int n2f, const double* __restrict__ af, int n1c, int n2c,
-                               double* __restrict__ ac) {
+__global__ void k_exp9_coarsen(int n1f, int n2f, const double* __restrict__ af, const unsigned char* __restrict__ maskf,
+                               int n1c, int n2c, double* __restrict__ ac) {
     pdl_enter();
     int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
     if (I >= n1c || J >= n2c) return;
@@ -200,6 +200,7 @@ __global__ void k_exp9_coarsen(int n1f, int n2f, const double* __restrict__ af, 
         for (int b = 0; b < 2; ++b) {
             int i = 2 * I + a, j = 2 * J + b;
             if (i >= n1f || j >= n2f) continue;
+            if (maskf && maskf[IX(i, j, n2f)]) continue;  // known cells are not unknowns of the coarse problem
             for (int e = 0; e < 9; ++e) {
                 int ii = i + c_off[e][0], jj = j + c_off[e][1];
                 if (ii < 0 || ii >= n1f || jj < 0 || jj >= n2f) continue;
@@ -215,16 +216,106 @@ __global__ void k_exp9_coarsen(int n1f, int n2f, const double* __restrict__ af, 
     for (int e = 0; e < 9; ++e) ac[e * nc + IX(I, J, n2c)] = 0.5 * acc[e];
 }
 
+// Coarse extra diagonal: half the sum over the 2x2 children (Galerkin product with piecewise
+// constant transfer, scaled by 1/2, of the couplings moved to the diagonal).
+__global__ void k_ed_coarsen(int n1f, int n2f, const double* __restrict__ edf, int n1c, int n2c,
+                             double* __restrict__ edc) {
+    pdl_enter();
+    int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
+    if (I >= n1c || J >= n2c) return;
+    double s = 0.0;
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) {
+            const int i = 2 * I + a, j = 2 * J + b;
+            if (i < n1f && j < n2f) s += edf[IX(i, j, n2f)];
+        }
+    edc[IX(I, J, n2c)] = 0.5 * s;
+}
+
+// Dirichlet row of the horizontal source (cells (dr, j), row kappa/dA p = -q,
+// src/MGSolver.cpp:119-140, 518-567): the known values x_d = -q_d dA / kappa are moved to the
+// right-hand sides of their neighbours and the couplings to them removed, which leaves an SPD
+// system in the unknowns.  Five-point operator: each removed face joins the neighbour's
+// diagonal (ed); one thread per column j.
+__global__ void k_dirichlet_face5(int n1, int n2, int dr, const double* __restrict__ q, double dA, double kappa,
+                                  double* __restrict__ tx, double* __restrict__ ty, double* __restrict__ ed,
+                                  double* __restrict__ fd, unsigned char* __restrict__ mask) {
+    pdl_enter();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n2) return;
+    const size_t kd = IX(dr, j, n2);
+    const double xd = -q[kd] * dA / kappa;
+    mask[kd] = 1;
+    fd[kd] = xd;
+    if (dr > 0) {
+        const double t = tx[IX(dr, j, n2)];
+        ed[IX(dr - 1, j, n2)] += t;
+        fd[IX(dr - 1, j, n2)] += t * xd;
+        tx[IX(dr, j, n2)] = 0.0;
+    }
+    if (dr < n1 - 1) {
+        const double t = tx[IX(dr + 1, j, n2)];
+        ed[IX(dr + 1, j, n2)] += t;
+        fd[IX(dr + 1, j, n2)] += t * xd;
+        tx[IX(dr + 1, j, n2)] = 0.0;
+    }
+    ty[IX(dr, j, n2 + 1)] = 0.0;
+    if (j == n2 - 1) ty[IX(dr, n2, n2 + 1)] = 0.0;
+}
+
+// Nine-point operator: rows dr-1 and dr+1 drop their entries towards row dr (the value moves to
+// fd); the known row becomes x = fd.  One thread per cell of rows dr-1 .. dr+1.
+__global__ void k_dirichlet_exp9(int n1, int n2, int dr, const double* __restrict__ q, double dA, double kappa,
+                                 double* __restrict__ a9, double* __restrict__ fd, unsigned char* __restrict__ mask) {
+    pdl_enter();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = dr - 1 + (int)blockIdx.y;
+    if (j >= n2 || i < 0 || i >= n1) return;
+    const size_t n = (size_t)n1 * n2, k = IX(i, j, n2);
+    if (i == dr) {
+        mask[k] = 1;
+        fd[k] = -q[k] * dA / kappa;
+        a9[k] = 1.0;
+        for (int e = 1; e < 9; ++e) a9[e * n + k] = 0.0;
+        return;
+    }
+    double add = 0.0;
+    for (int e = 1; e < 9; ++e) {
+        const int ii = i + c_off[e][0], jj = j + c_off[e][1];
+        if (ii != dr || jj < 0 || jj >= n2) continue;
+        add -= a9[e * n + k] * (-q[IX(dr, jj, n2)] * dA / kappa);
+        a9[e * n + k] = 0.0;
+    }
+    fd[k] = add;
+}
+
+// f := f + fd on unknown cells, f := the known value on known cells; x := the known value there.
+__global__ void k_dirichlet_rhs(size_t n, double* __restrict__ f, double* __restrict__ x,
+                                const double* __restrict__ fd, const unsigned char* __restrict__ mask) {
+    pdl_enter();
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        if (mask[k]) {
+            f[k] = fd[k];
+            x[k] = fd[k];
+        } else {
+            f[k] += fd[k];
+        }
+    }
+}
+
 __global__ void k_idiag(int n1, int n2, int kind, const double* __restrict__ tx, const double* __restrict__ ty,
-                        const double* __restrict__ a9, double* __restrict__ diag, double* __restrict__ idiag) {
+                        const double* __restrict__ a9, const double* __restrict__ ed,
+                        const unsigned char* __restrict__ mask, double* __restrict__ diag, double* __restrict__ idiag) {
     pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i >= n1 || j >= n2) return;
     double d;
-    if (kind == FACE5)
+    if (kind == FACE5) {
         d = tx[IX(i, j, n2)] + tx[IX(i + 1, j, n2)] + ty[IX(i, j, n2 + 1)] + ty[IX(i, j + 1, n2 + 1)];
-    else
+        if (ed) d += ed[IX(i, j, n2)];
+    } else {
         d = a9[IX(i, j, n2)];
+    }
+    if (mask && mask[IX(i, j, n2)]) d = 1.0;  // known cell: x = rhs
     diag[IX(i, j, n2)] = d;
     idiag[IX(i, j, n2)] = d != 0.0 ? 1.0 / d : 0.0;
 }
@@ -352,10 +443,12 @@ __global__ void k_restrict(Level F, const T* __restrict__ tx, const T* __restric
 // Bilinear cell-centred prolongation (weights 9/16, 3/16, 3/16, 1/16; the outside
 // neighbour is replaced by the cell itself), added to the fine iterate.
 template <class T>
-__global__ void k_prolong(int n1, int n2, T* __restrict__ x, int n1c, int n2c, const T* __restrict__ xc) {
+__global__ void k_prolong(int n1, int n2, T* __restrict__ x, int n1c, int n2c, const T* __restrict__ xc,
+                          const unsigned char* __restrict__ mask) {
     pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i >= n1 || j >= n2) return;
+    if (mask && mask[IX(i, j, n2)]) return;  // known cells take no correction
     int I = i >> 1, J = j >> 1;
     int I2 = (i & 1) ? I + 1 : I - 1, J2 = (j & 1) ? J + 1 : J - 1;
     if (I2 < 0 || I2 >= n1c) I2 = I;
@@ -378,7 +471,7 @@ __global__ void k_dense_build(Level C, const double* __restrict__ tx, const doub
         int i = r / n2, j = r % n2;
         if (C.kind == FACE5) {
             double tw = tx[IX(i, j, n2)], te = tx[IX(i + 1, j, n2)], ts = ty[IX(i, j, n2 + 1)], tn = ty[IX(i, j + 1, n2 + 1)];
-            D[(size_t)r * n + r] = tw + te + ts + tn;
+            D[(size_t)r * n + r] = C.diag[r];  // the faces' sum (+ couplings moved to the diagonal)
             if (i > 0) D[(size_t)r * n + IX(i - 1, j, n2)] = -tw;
             if (i < n1 - 1) D[(size_t)r * n + IX(i + 1, j, n2)] = -te;
             if (j > 0) D[(size_t)r * n + IX(i, j - 1, n2)] = -ts;
@@ -519,13 +612,13 @@ __global__ void k_shift(size_t n, double* __restrict__ x, int pin, const DevScal
 }
 
 // y = A_ref x (reference pinned matrix) from the device operator.
-__global__ void k_apply_ref(Level F, const double* __restrict__ x, int pin, double dA, double kappa,
+__global__ void k_apply_ref(Level F, const double* __restrict__ x, int pin, int dir_row, double dA, double kappa,
                             double* __restrict__ y) {
     pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i >= F.n1 || j >= F.n2) return;
     size_t k = IX(i, j, F.n2);
-    if ((int)k == pin) { y[k] = kappa / dA * x[k]; return; }
+    if ((int)k == pin || i == dir_row) { y[k] = kappa / dA * x[k]; return; }
     double v;
     if (F.kind == FACE5) {
         double d, o;
@@ -596,6 +689,7 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.idiag, n * 8));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.idiag32, n * 4));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.diag, n * 8));
+        if (ctx->dir_row >= 0 && Lv.kind == FACE5) IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.ed, n * 8));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.diag32, n * 4));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.x, n * 8));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.b, n * 8));
@@ -615,6 +709,10 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->cg_q, nf * 8));
         IMPEC_CUDA_TRY(cudaMemset(ctx->cg_q, 0, nf * 8));
         ctx->krylov = (int)env_long("IMPEC_MG_KRYLOV", 1) != 0;
+        if (ctx->dir_row >= 0) {
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dmask, nf));
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dfd, nf * 8));
+        }
     }
     IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dense_inv, (size_t)ctx->dense_n * ctx->dense_n * 8 * 2));
     IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_dense_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 64 * 8));
@@ -643,13 +741,13 @@ impec_status pressure_alloc(impec_ctx* ctx) {
 
 void pressure_free(impec_ctx* ctx) {
     for (Level& Lv : ctx->L) {
-        void* ps[] = {Lv.tx,   Lv.ty,   Lv.a9,   Lv.idiag,   Lv.diag,   Lv.x,   Lv.b,
+        void* ps[] = {Lv.tx,   Lv.ty,   Lv.a9,   Lv.idiag,   Lv.diag,   Lv.ed,  Lv.x,   Lv.b,
                       Lv.tx32, Lv.ty32, Lv.a932, Lv.idiag32, Lv.diag32, Lv.x32, Lv.b32};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
     ctx->L.clear();
-    void* ps[] = {ctx->cm11, ctx->cm22, ctx->cm12, ctx->dense_inv, ctx->cg_x, ctx->cg_p, ctx->cg_q};
+    void* ps[] = {ctx->cm11, ctx->cm22, ctx->cm12, ctx->dense_inv, ctx->cg_x, ctx->cg_p, ctx->cg_q, ctx->dmask, ctx->dfd};
     for (void* p : ps)
         if (p) cudaFree(p);
 }
@@ -688,19 +786,43 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
                                                                          ctx->cm22, ctx->cm12, P.nu, G, F.a9);
     }
     IMPEC_LAUNCH_CHECK();
+    // Dirichlet row (horizontal source): known cells out of the operator, their values into fd
+    const bool dir = ctx->dir_row >= 0 && ctx->eliminate;
+    const unsigned char* mask0 = dir ? ctx->dmask : nullptr;
+    if (dir) {
+        const size_t n = F.n();
+        IMPEC_CUDA_TRY(cudaMemsetAsync(ctx->dmask, 0, n, ctx->stream));
+        IMPEC_CUDA_TRY(cudaMemsetAsync(ctx->dfd, 0, n * 8, ctx->stream));
+        if (F.kind == FACE5) {
+            IMPEC_CUDA_TRY(cudaMemsetAsync(F.ed, 0, n * 8, ctx->stream));
+            ++ctx->nlaunch, launch_k(ctx->stream, k_dirichlet_face5, (F.n2 + 127) / 128, 128, 0, F.n1, F.n2, ctx->dir_row,
+                                     ctx->q, G.dA, ctx->pin_kappa, F.tx, F.ty, F.ed, ctx->dfd, ctx->dmask);
+        } else {
+            ++ctx->nlaunch, launch_k(ctx->stream, k_dirichlet_exp9, dim3((F.n2 + 127) / 128, 3), 128, 0, F.n1, F.n2,
+                                     ctx->dir_row, ctx->q, G.dA, ctx->pin_kappa, F.a9, ctx->dfd, ctx->dmask);
+        }
+        IMPEC_LAUNCH_CHECK();
+    }
     for (size_t l = 0; l + 1 < ctx->L.size(); ++l) {
         Level &A = ctx->L[l], &B = ctx->L[l + 1];
-        if (A.kind == FACE5)
+        if (A.kind == FACE5) {
             ++ctx->nlaunch, launch_k(ctx->stream, k_face5_coarsen, grid2(B.n1 + 1, B.n2 + 1), dim3(BX, BY), 0, A.n1, A.n2, A.tx, A.ty, B.n1,
                                                                                         B.n2, B.tx, B.ty);
-        else
-            ++ctx->nlaunch, launch_k(ctx->stream, k_exp9_coarsen, grid2(B.n1, B.n2), dim3(BX, BY), 0, A.n1, A.n2, A.a9, B.n1, B.n2, B.a9);
+            if (dir)
+                ++ctx->nlaunch, launch_k(ctx->stream, k_ed_coarsen, grid2(B.n1, B.n2), dim3(BX, BY), 0, A.n1, A.n2, A.ed,
+                                         B.n1, B.n2, B.ed);
+        } else {
+            ++ctx->nlaunch, launch_k(ctx->stream, k_exp9_coarsen, grid2(B.n1, B.n2), dim3(BX, BY), 0, A.n1, A.n2, A.a9,
+                                     l == 0 ? mask0 : nullptr, B.n1, B.n2, B.a9);
+        }
         IMPEC_LAUNCH_CHECK();
     }
     const bool mixed = P.precision == IMPEC_PREC_MIXED;
-    for (Level& Lv : ctx->L) {
+    for (size_t l = 0; l < ctx->L.size(); ++l) {
+        Level& Lv = ctx->L[l];
         ++ctx->nlaunch, launch_k(ctx->stream, k_idiag, grid2(Lv.n1, Lv.n2), dim3(BX, BY), 0, Lv.n1, Lv.n2, Lv.kind, Lv.tx,
-                                 Lv.ty, Lv.a9, Lv.diag, Lv.idiag);
+                                 Lv.ty, Lv.a9, dir && Lv.kind == FACE5 ? Lv.ed : nullptr, l == 0 ? mask0 : nullptr,
+                                 Lv.diag, Lv.idiag);
         IMPEC_LAUNCH_CHECK();
         if (mixed) {
             const size_t n = Lv.n();
@@ -717,7 +839,8 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
         }
     }
     Level& C = ctx->L.back();
-    ++ctx->nlaunch, launch_k(ctx->stream, k_dense_build, 1, 256, 0, C, C.tx, C.ty, C.a9, 1, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n);
+    ++ctx->nlaunch, launch_k(ctx->stream, k_dense_build, 1, 256, 0, C, C.tx, C.ty, C.a9, ctx->singular,
+                             ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n);
     IMPEC_LAUNCH_CHECK();
     ++ctx->nlaunch, launch_k(ctx->stream, k_dense_invert, 1, 256, 2 * ctx->dense_n * ctx->dense_n * 8,
         ctx->dense_n, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n, ctx->dense_inv);
@@ -783,7 +906,9 @@ template <class T>
 static size_t coarse_start(const impec_ctx* ctx) {
     const size_t cells = (size_t)(sizeof(T) == 8 ? env_long("IMPEC_MG_COARSE_CELLS64", 256)
                                                  : env_long("IMPEC_MG_COARSE_CELLS32", 1024));
-    for (size_t l = 0; l < ctx->L.size(); ++l)
+    // with a Dirichlet row the finest level keeps its own kernels (its prolongation is masked)
+    const size_t l0 = ctx->dir_row >= 0 && ctx->L.size() > 1 ? 1 : 0;
+    for (size_t l = l0; l < ctx->L.size(); ++l)
         if (ctx->L[l].n() <= cells && coarse_bytes<T>(ctx, l) <= MG_COARSE_SMEM) return l;
     return ctx->L.size() - 1;
 }
@@ -792,7 +917,7 @@ template <class T>
 static void launch_coarse(impec_ctx* ctx, size_t lc) {
     CoarseArgs<T> A{};
     A.nl = (int)(ctx->L.size() - lc);
-    A.singular = 1;
+    A.singular = ctx->singular;
     A.dn = ctx->dense_n;
     A.dinv = ctx->dense_inv;
     for (int k = 0; k < A.nl; ++k) {
@@ -825,7 +950,7 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
     const long cta0 = env_long("IMPEC_MG_CL_CTA0", 256);
     A = ClusterArgs<T>{};
     A.nl = (int)nl;
-    A.singular = 1;
+    A.singular = ctx->singular;
     A.dn = ctx->dense_n;
     A.dinv = ctx->dense_inv;
     size_t off = 0;
@@ -873,7 +998,8 @@ static size_t cluster_start(impec_ctx* ctx) {
     const long cells = env_long("IMPEC_MG_CL_CELLS", 16384);
     ClusterArgs<T> A;
     size_t smem;
-    for (size_t l = 0; l < ctx->L.size(); ++l)
+    const size_t l0 = ctx->dir_row >= 0 ? 1 : 0;  // the finest level's prolongation is masked there
+    for (size_t l = l0; l < ctx->L.size(); ++l)
         if ((long)ctx->L[l].n() <= cells && cluster_plan<T>(ctx, l, A, smem)) return l;
     return SIZE_MAX;
 }
@@ -906,7 +1032,7 @@ static void launch_cluster(impec_ctx* ctx, size_t ls) {
 // they recompute cost FP64 issue slots and their per-CTA phases serialise.
 template <class T>
 static bool use_fused_level(size_t l) {
-    if (sizeof(T) == 4) return env_long("IMPEC_MG_FUSED32", 0) != 0;
+    if (sizeof(T) == 4) return env_long("IMPEC_MG_FUSED32", 0) != 0 && (l > 0 || env_long("IMPEC_MG_FUSE_FINE", 0) != 0);
     return env_long("IMPEC_MG_FUSED64", 0) != 0 && (l > 0 || env_long("IMPEC_MG_FUSE_FINE", 0) != 0);
 }
 
@@ -945,7 +1071,8 @@ static void vcycle(impec_ctx* ctx, size_t l) {
              C.n1, C.n2, cb, cx);
     vcycle<T>(ctx, l + 1);
     ++ctx->nlaunch;
-    launch_k(ctx->stream, k_prolong<T>, grid2(F.n1, F.n2), dim3(BX, BY), 0, F.n1, F.n2, x, C.n1, C.n2, cx);
+    launch_k(ctx->stream, k_prolong<T>, grid2(F.n1, F.n2), dim3(BX, BY), 0, F.n1, F.n2, x, C.n1, C.n2, cx,
+             l == 0 && ctx->dir_row >= 0 ? ctx->dmask : nullptr);
     smooth<T>(ctx, F, 2, true);
 }
 
@@ -1076,7 +1203,8 @@ __global__ void k_true_relres(DevScalars* S, double tol) {
     else if (rr > 2.0 * tol && !(S->flags & FLAG_MG_NOT_CONVERGED)) S->flags |= FLAG_MG_NOT_CONVERGED;
 }
 
-static int pin_index(impec_ctx* ctx) { return (int)IX(ctx->pin_i, ctx->pin_j, ctx->L[0].n2); }
+// The pinned cell of the singular system (-1 with a Dirichlet row: nothing is pinned).
+static int pin_index(impec_ctx* ctx) { return ctx->singular ? (int)IX(ctx->pin_i, ctx->pin_j, ctx->L[0].n2) : -1; }
 
 // The iterate the loop updates: CG keeps it in its own buffer (the finest level's iterate is
 // the preconditioner's output), stationary cycles update the finest iterate itself.
@@ -1106,14 +1234,21 @@ impec_status pressure_prepare(impec_ctx* ctx, const double* c, const double* p) 
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_rhs, flat_blocks(n, red_cap(ctx->num_sms, ctx->max_blocks)), RED_THREADS, 0, n, ctx->q,
              ctx->G.dA, ctx->f, ctx->partials, ctx->max_blocks, ctx->counter, &S->fsum);
-    ++ctx->nlaunch;
-    launch_k(ctx->stream, k_fix_pin, 1, 1, 0, ctx->f, ctx->q, pin, ctx->G.dA, ctx->pin_kappa, S);
+    if (ctx->singular) {
+        ++ctx->nlaunch;
+        launch_k(ctx->stream, k_fix_pin, 1, 1, 0, ctx->f, ctx->q, pin, ctx->G.dA, ctx->pin_kappa, S);
+    }
     IMPEC_LAUNCH_CHECK();
     double* x = solve_iterate(ctx);
     if (P.warm_start)
         IMPEC_CUDA_TRY(cudaMemcpyAsync(x, p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     else
         IMPEC_CUDA_TRY(cudaMemsetAsync(x, 0, n * 8, ctx->stream));
+    if (!ctx->singular) {  // Dirichlet row: known values into f and x, their couplings into f
+        ++ctx->nlaunch;
+        launch_k(ctx->stream, k_dirichlet_rhs, ctx->num_sms * 4, 256, 0, n, ctx->f, x, ctx->dfd, ctx->dmask);
+        IMPEC_LAUNCH_CHECK();
+    }
     if (!ctx->krylov) IMPEC_CUDA_TRY(cudaMemcpyAsync(F.b, ctx->f, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     IMPEC_CUDA_TRY(cudaMemsetAsync(&S->mg_cycles, 0, sizeof(int), ctx->stream));
     const bool mixed = P.precision == IMPEC_PREC_MIXED;
@@ -1192,8 +1327,10 @@ impec_status pressure_finish(impec_ctx* ctx, double* p) {
         ++ctx->nlaunch;
         launch_k(ctx->stream, k_true_relres, 1, 1, 0, ctx->dscal, ctx->solve_tol);
     }
-    ++ctx->nlaunch;
-    launch_k(ctx->stream, k_shift, ctx->num_sms * 4, 256, 0, n, x, pin_index(ctx), ctx->dscal);
+    if (ctx->singular) {  // the constant that puts the pinned cell at its value
+        ++ctx->nlaunch;
+        launch_k(ctx->stream, k_shift, ctx->num_sms * 4, 256, 0, n, x, pin_index(ctx), ctx->dscal);
+    }
     IMPEC_LAUNCH_CHECK();
     IMPEC_CUDA_TRY(cudaMemcpyAsync(p, x, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     return IMPEC_OK;
@@ -1225,8 +1362,9 @@ impec_status pressure_solve(impec_ctx* ctx, const double* c, double* p, double t
 
 impec_status pressure_apply_ref(impec_ctx* ctx, const double* x, double* y) {
     Level& F = ctx->L[0];
-    const int pin = (int)IX(ctx->pin_i, ctx->pin_j, F.n2);
-    ++ctx->nlaunch, launch_k(ctx->stream, k_apply_ref, grid2(F.n1, F.n2), dim3(BX, BY), 0, F, x, pin, ctx->G.dA, ctx->pin_kappa, y);
+    const int pin = ctx->singular ? (int)IX(ctx->pin_i, ctx->pin_j, F.n2) : -1;
+    ++ctx->nlaunch, launch_k(ctx->stream, k_apply_ref, grid2(F.n1, F.n2), dim3(BX, BY), 0, F, x, pin, ctx->dir_row,
+                             ctx->G.dA, ctx->pin_kappa, y);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }

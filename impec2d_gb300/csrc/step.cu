@@ -145,7 +145,10 @@ impec_status impec_face_mobility(impec_ctx* ctx, const double* c, double* lamx, 
 
 impec_status impec_pressure_apply(impec_ctx* ctx, const double* c, const double* x, double* y) {
     if (!ctx || !c || !x || !y) return IMPEC_ERR_ARG;
-    IMPEC_TRY(pressure_setup(ctx, c));
+    ctx->eliminate = 0;  // the reference's matrix, Dirichlet rows included, not the reduced system
+    impec_status s = pressure_setup(ctx, c);
+    ctx->eliminate = 1;
+    IMPEC_TRY(s);
     IMPEC_TRY(pressure_apply_ref(ctx, x, y));
     IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return IMPEC_OK;

@@ -34,6 +34,34 @@ def test_fixture_config2():
     assert P.eps == 1e-10 and P.precision == E.PREC_FP64 and P.bc == E.BC_NEUMANN
 
 
+def test_fixture_horizontal_front():
+    """source_type horizontal: injection over the first and production over the last
+    round(well_width L / dx) rows (InitHorizontalFront, src/Util.cpp:607-639)."""
+    path = os.path.join(HERE, "golden", "horizontal_pulsing_64x48.cfg")
+    P, t0, t1 = E.load_cfg(path)
+    assert (P.N1, P.N2) == (64, 48) and P.stype == E.HORIZONTAL and P.diffusion == 1
+    q = E.cfg_source(path, 64, 48)
+    rows = 3  # round(0.05 * 1 / (1 / 64))
+    val = 1.0 / (48 * (1 / 64) * (1 / 48) * rows)
+    assert q[:48 * rows] == pytest.approx(val) and q[-48 * rows:] == pytest.approx(-val)
+    assert (q != 0).sum() == 2 * 48 * rows
+
+
+@pytest.mark.gpu
+def test_run_horizontal_pulsing_cfg():
+    """The whole .cfg through the executable's entry point: Dirichlet rows in the pressure and
+    CN systems and the pulsing rate updated every step."""
+    path = os.path.join(HERE, "golden", "horizontal_pulsing_64x48.cfg")
+    assert E.lib().impec_run_cfg(path.encode(), 1) == 0, E.last_error()
+    rows = [list(map(float, l.split())) for l in open("/tmp/impec2d_horizontal/concentration.dat") if l.strip()]
+    c = [r[2] for r in rows]
+    assert len(c) == 64 * 48 and min(c) > -1e-6 and max(c) < 1.0 + 1e-6
+    # after t = 0.004 the three injection rows hold about q t = 64 / 3 * 0.004 (less what has moved on)
+    first = sum(c[:3 * 48]) / (3 * 48)
+    rest = sum(c[10 * 48:]) / (54 * 48)
+    assert 0.05 < first < 0.0854 and rest < 1e-3
+
+
 @pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not mounted")
 def test_reference_examples_parse_unchanged():
     files = sorted(glob.glob(os.path.join(REF_EXAMPLES, "*.cfg")))

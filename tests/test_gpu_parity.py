@@ -367,3 +367,138 @@ def test_cg_and_stationary_cycles_agree_on_heterogeneous_coefficients(engine, or
         out[kry] = (cyc, host(p))
     assert out["1"][0] < out["0"][0]
     assert rel_err(out["1"][1], out["0"][1]) <= 1e-7
+
+
+# ---------------------------------------------------------------- horizontal-front source
+# source_type "horizontal": injection over the first and production over the last well_width
+# rows (InitHorizontalFront, src/Util.cpp:607-639), a Dirichlet row (1, j) in the pressure
+# system (src/MGSolver.cpp:119-140, 518-567) and (N1-2, j) in the CN system (:1295-1317).
+
+@pytest.mark.parametrize("nu", [1.0, 2.0 / 3.0])
+def test_horizontal_pressure_apply(engine, oracle_lib, nu):
+    E = engine
+    N1, N2 = 40, 32
+    P, ctx = _ctx(E, N1, N2, nu=nu, stype=2)
+    OP = oparams(P)
+    ctx.set_source(dev(source(OP)))
+    c = _rand_c(N1, N2, 2)
+    x = np.random.default_rng(3).normal(size=(N1, N2))
+    A = np.zeros(N1 * N2 * 9)
+    oracle_lib.or_pressure_matrix(C.byref(OP), O.ptr(cell_ghost(OP, c)), O.ptr(A))
+    y_or = np.zeros(N1 * N2)
+    oracle_lib.or_matvec9(C.byref(OP), O.ptr(A), O.ptr(x.ravel().copy()), O.ptr(y_or))
+    import torch
+    y = torch.zeros((N1, N2), dtype=torch.float64, device="cuda")
+    ctx.pressure_apply(dev(c), dev(x), y)
+    scale = np.abs(A.reshape(-1, 9)).sum(1).max() * np.abs(x).max()
+    assert np.abs(host(y).ravel() - y_or).max() <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("N1,N2", [(64, 48), (97, 70)])
+@pytest.mark.parametrize("nu", [1.0, 2.0 / 3.0])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_horizontal_pressure_solve(engine, oracle_lib, N1, N2, nu, prec):
+    """The Dirichlet-row system (known cells eliminated, SPD) solved by V-cycle CG reaches the
+    tolerance under the oracle's matrix and matches the oracle's banded LU solve."""
+    E = engine
+    import torch
+    P, ctx = _ctx(E, N1, N2, nu=nu, stype=2, precision=prec, max_cycles=200)
+    OP = oparams(P)
+    c = _rand_c(N1, N2, 4)
+    q = source(OP)
+    ctx.set_source(dev(q))
+    p = torch.zeros((N1, N2), dtype=torch.float64, device="cuda")
+    tol = 1e-12
+    cyc, rr, _ = ctx.pressure_solve(dev(c), p, tol)
+    assert rr <= tol and cyc < 200
+    A = np.zeros(N1 * N2 * 9)
+    b = np.zeros(N1 * N2)
+    oracle_lib.or_pressure_matrix(C.byref(OP), O.ptr(cell_ghost(OP, c)), O.ptr(A))
+    oracle_lib.or_pressure_rhs(C.byref(OP), O.ptr(q), O.ptr(b))
+    ph = host(p).ravel().copy()
+    assert oracle_lib.or_relres9(C.byref(OP), O.ptr(A), O.ptr(ph), O.ptr(b)) <= 2 * tol
+    p_or = _oracle_pressure(oracle_lib, OP, c, q)
+    assert rel_err(host(p), p_or) <= 1e-8
+
+
+def test_horizontal_dispersion_cn(engine, oracle_lib):
+    """CN with the Dirichlet row c = 0 at i = N1-2."""
+    E = engine
+    N1, N2 = 48, 40
+    P, ctx = _ctx(E, N1, N2, stype=2, diffusion=1, alpha_l=1.0, alpha_t=0.1, para_eps=1e-13, max_cycles=400)
+    OP = oparams(P)
+    vg = _vel_field(OP, 10)
+    u, v = vel_split(OP, vg)
+    c = _rand_c(N1, N2, 11)
+    cg = cell_ghost(OP, c)
+    dt = 0.5 * oracle_lib.or_max_stable_dt(C.byref(OP), O.ptr(vg))
+    its, rr = C.c_int(), C.c_double()
+    assert oracle_lib.or_cn_solve(C.byref(OP), O.ptr(cg), O.ptr(vg), dt, 0, 1e-14, C.byref(its), C.byref(rr)) == 0
+    dc = dev(c)
+    its_d, rr_d = ctx.dispersion_cn(dc, dev(u), dev(v), dt, 1e-13)
+    assert rr_d <= 1e-13
+    out = host(dc)
+    assert np.all(out[N1 - 2] == 0.0)
+    assert rel_err(out, O.interior(OP, cg)) <= 1e-11
+
+
+@pytest.mark.parametrize("nu,disp,pulsing", [(1.0, 0, False), (2.0 / 3.0, 1, False), (2.0 / 3.0, 1, True)])
+def test_horizontal_impes_steps_short_horizon(engine, oracle_lib, nu, disp, pulsing):
+    """Whole IMPES steps with the horizontal front against the oracle; with pulsing injection
+    (InitHorizontalFront at the current time before every step, src/Impec2DSolver.cpp:437-439)
+    the rates change in place between steps."""
+    E = engine
+    N1, N2 = 48, 40
+    kw = dict(stype=2, hmtype=4, nu=nu, diffusion=disp, alpha_l=1e-2, alpha_t=1e-3)
+    P, ctx = _ctx(E, N1, N2, eps=1e-13, para_eps=1e-13, max_cycles=200, **kw)
+    OP = oparams(P, inj_mode=0, q_freq=400.0) if pulsing else oparams(P)
+    q = source(OP)
+    rates = set()
+    c0 = np.zeros((N1, N2))
+    ctx.upload(cell_ghost(OP, c0), q, ghost=2)
+    c = cell_ghost(OP, c0)
+    p = np.zeros(O.scalar_shape(OP))
+    vv = np.zeros(O.vel_shape(OP))
+    S = O.State()
+    S.prev_first_sweep = 1
+    tidx = C.c_int(0)
+    for k in range(8):
+        if pulsing:
+            oracle_lib.or_init_source(C.byref(OP), O.ptr(q), S.t)
+            ctx.set_source(dev(q))
+            rates.add(float(q[0]))
+        oracle_lib.or_impes_step(C.byref(OP), C.byref(S), O.ptr(c), O.ptr(p), O.ptr(vv), O.ptr(q), None, 0,
+                                 C.byref(tidx), 0, 1e-14)
+        info = ctx.step()
+        assert info.dt == pytest.approx(S.dt, rel=1e-9)
+    if pulsing:
+        assert len(rates) == 2  # both phases of the pulse were used
+    ch, ph, vh = np.zeros_like(c), np.zeros_like(p), np.zeros_like(vv)
+    ctx.download(ch, ph, vh, ghost=2)
+    assert rel_err(O.interior(OP, ch), O.interior(OP, c)) <= 1e-9
+    assert rel_err(O.interior(OP, ph), O.interior(OP, p)) <= 1e-8
+
+
+def test_horizontal_source_rate_update_in_place(engine):
+    """A source with the same well cells and new rates (the pulsing / linear front,
+    src/Impec2DSolver.cpp:437-439) updates the rates in place; the next steps equal those of a
+    context built with the new rates from the start."""
+    E = engine
+    N1, N2 = 40, 32
+    P, ctx = _ctx(E, N1, N2, stype=2)
+    q = source(oparams(P))
+    z = np.zeros((N1 + 4, N2 + 4))
+    P2, ref = _ctx(E, N1, N2, stype=2)
+    for cx in (ctx, ref):
+        cx.upload(z, q, ghost=2)
+        cx.step()  # captures the step graph
+    ctx.set_source(dev(q * 50.0))  # same cells: rates updated under the existing graph
+    ref.set_source(dev(np.zeros_like(q)))  # different cells: well list rebuilt, graph captured again
+    ref.set_source(dev(q * 50.0))
+    for _ in range(3):
+        a, b = ctx.step(), ref.step()
+        assert a.dt == b.dt
+    ca, cb = np.zeros_like(z), np.zeros_like(z)
+    ctx.download(ca, None, None, ghost=2)
+    ref.download(cb, None, None, ghost=2)
+    assert np.array_equal(ca, cb)
