@@ -45,11 +45,14 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch each kernel on the stream instead of replaying the step graph (for ncu)")
-    ap.add_argument("--study", default=None, choices=["pressure", "warmstart"],
+    ap.add_argument("--study", default=None, choices=["pressure", "warmstart", "ensemble"],
                     help="pressure: FP64 vs mixed-precision solves on re-seeded heterogeneous fields; "
                          "warmstart: V-cycles and ms per solve along the IMPES run for zero and previous-step "
                          "initial guesses")
     ap.add_argument("--solves", type=int, default=20, help="re-seeded solves of the pressure study")
+    ap.add_argument("--members-per-size", type=int, default=64,
+                    help="ensemble study: realisations at each of 128^2, 256^2, 384^2, 512^2")
+    ap.add_argument("--no-autotune", action="store_true", help="ensemble study: keep the default schedules")
     return ap.parse_args()
 
 
@@ -274,6 +277,98 @@ def study_warmstart(args):
     print(json.dumps(out))
 
 
+def ensemble_member(E, N, seed, precision="mixed"):
+    """One realisation of the batched-ensemble workload: lognormal K (sigma 0.5, correlation
+    16 cells), M from {5, 20, 41, 100} and diagonal or parallel orientation chosen by the seed,
+    MUSCL + Peaceman dispersion (alpha_l 1e-3, alpha_t 1e-4), FP64 transport and
+    mixed-precision pressure."""
+    import numpy as np
+    import torch
+    M = (5.0, 20.0, 41.0, 100.0)[seed % 4]
+    parallel = (seed // 4) % 2 == 1
+    L = math.sqrt(2.0) if parallel else 1.0
+    P = E.default_params(N, N, x_ub=L, y_ub=L, stype=E.PARALLEL if parallel else E.DIAGONAL, hmtype=E.MUSCL,
+                         nu=1.0, diffusion=1, alpha_l=1e-3, alpha_t=1e-4, cfl=0.5, porosity=1.0, eps=1e-10,
+                         para_eps=1e-10, mu_res=M, mu_inj=1.0, max_cycles=200,
+                         precision=E.PREC_MIXED if precision == "mixed" else E.PREC_FP64)
+    ctx = E.Context(P)
+    dx = L / N
+    qv = 1.0 / (dx * dx)
+    q = np.zeros(N * N)
+    q[0] = qv
+    if parallel:
+        q[-1], q[N - 1], q[(N - 1) * N] = qv, -qv, -qv
+    else:
+        q[-1] = -qv
+    K = torch.exp(0.5 * grf(N, 16.0, 5000 + seed)).contiguous()
+    ctx.upload(np.zeros((N + 4, N + 4)), q, ghost=2)
+    ctx.set_permeability(K, K)
+    ctx.set_time(0.0)
+    return ctx
+
+
+def study_ensemble(args):
+    """Batched ensemble: members of four sizes advanced by one graph launch per IMPES step,
+    against the same members stepped one after another."""
+    import torch
+
+    import impec2d_gb300 as E
+    from impec2d_gb300 import build as B
+    B.build()
+    sizes = (128, 256, 384, 512)
+    k = args.members_per_size
+    tuned = {}
+    if not args.no_autotune:  # one probe per size, on its own state after a few steps
+        for N in sizes:
+            probe = ensemble_member(E, N, 0)
+            probe.run_steps(3)
+            probe.step()
+            rep = probe.autotune(reps=3)
+            tuned[N] = {n: probe.get_tuning(n) for n in ("mg_pre", "mg_post", "cluster")}
+            tuned[N]["report"] = rep.strip().splitlines()[-1]
+            probe.close()
+    members = []
+    for N in sizes:
+        for i in range(k):
+            ctx = ensemble_member(E, N, i)
+            for name, v in tuned.get(N, {}).items():
+                if name != "report":
+                    ctx.set_tuning(name, v)
+            members.append((N, ctx))
+    cells = sum(N * N for N, _ in members)
+    t0 = time.perf_counter()
+    ens = E.Ensemble([c for _, c in members])
+    t_capture = time.perf_counter() - t0
+    ens.step(args.warmup)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ens.step(args.steps)
+    t_ens = time.perf_counter() - t0
+    # the same members one after another (each its own graph launch per step)
+    for _, c in members:
+        c.run_steps(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for _, c in members:
+            c.run_steps(1)
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    out = {"study": "ensemble",
+           "workload": f"{len(members)} realisations, {k} each at 128^2, 256^2, 384^2, 512^2; lognormal K "
+                       f"(sigma 0.5), M in {{5,20,41,100}}, diagonal/parallel by seed; MUSCL + Peaceman; "
+                       f"mixed-precision pressure",
+           "cells": cells, "steps": args.steps, "warmup": args.warmup,
+           "ensemble": {"cell_steps_per_s": cells * args.steps / t_ens, "ms_per_step": 1e3 * t_ens / args.steps,
+                        "capture_s": t_capture},
+           "one_after_another": {"cell_steps_per_s": cells * args.steps / t_seq, "ms_per_step": 1e3 * t_seq / args.steps},
+           "speedup": t_seq / t_ens, "autotune": tuned or None, "data": "synthetic (seeded GRF permeability)"}
+    print(json.dumps(out))
+    ens.close()
+    for _, c in members:
+        c.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -282,6 +377,8 @@ def main():
         return study_pressure(args)
     if args.study == "warmstart":
         return study_warmstart(args)
+    if args.study == "ensemble":
+        return study_ensemble(args)
     if args.no_graph:
         os.environ["IMPEC_NO_GRAPH"] = "1"  # read by the engine at each step
     import numpy as np

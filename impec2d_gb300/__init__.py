@@ -103,6 +103,12 @@ _SIGS = {
     "impec_advect_symmetric_noalloc": (C.c_int, [C.POINTER(Params), _VP, _VP, _VP, C.c_double, _VP]),
     "impec_time_kernel": (C.c_int, [_VP, C.c_int, C.c_int, _PD, _PD]),
     "impec_measure_fp64": (C.c_int, [_PD]),
+    "impec_set_tuning": (C.c_int, [_VP, C.c_char_p, C.c_long]),
+    "impec_get_tuning": (C.c_int, [_VP, C.c_char_p, C.POINTER(C.c_long)]),
+    "impec_autotune": (C.c_int, [_VP, C.c_int, C.c_char_p, C.c_int]),
+    "impec_ensemble_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
+    "impec_ensemble_step": (C.c_int, [_VP, C.c_int, C.c_int]),
+    "impec_ensemble_destroy": (C.c_int, [_VP]),
     "impec_project_diagonal": (C.c_int, [_VP, C.c_int, _VP, C.c_int, C.c_int]),
     "impec_project_diagonal_download": (C.c_int, [_VP, C.c_int, _PD, C.c_int, C.c_int]),
 }
@@ -170,6 +176,32 @@ def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None, traffi
                        "frac": ops / (ms * 1e-3) / fma, "ops_per_launch": ops,
                        "peak_source": "measured (impec_measure_fp64: DFMA lanes per second)"}
     return out
+
+
+class Ensemble:
+    """Independent contexts advanced together by one graph launch per IMPES step."""
+
+    def __init__(self, members):
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.h.value if isinstance(m.h, C.c_void_p) else m.h
+                                                   for m in self.members])
+        h = C.c_void_p()
+        _chk(lib().impec_ensemble_create(arr, len(self.members), C.byref(h)), "ensemble_create")
+        self.h = h
+
+    def step(self, n: int = 1, sync: bool = True):
+        _chk(lib().impec_ensemble_step(self.h, n, 1 if sync else 0), "ensemble_step")
+
+    def close(self):
+        if self.h:
+            lib().impec_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
 
 
 def load_cfg(path: str):
@@ -326,6 +358,20 @@ class Context:
         """Project the resident c (field 0) or p (field 1) of a parallel run onto the dN1 x dN2
         diagonal grid (out: float64 CUDA tensor of dN1*dN2)."""
         _chk(lib().impec_project_diagonal(self.h, field, _p(out), dN1, dN2), "project_diagonal")
+
+    def set_tuning(self, name: str, value: int):
+        _chk(lib().impec_set_tuning(self.h, name.encode(), value), f"set_tuning({name})")
+
+    def get_tuning(self, name: str) -> int:
+        v = C.c_long()
+        _chk(lib().impec_get_tuning(self.h, name.encode(), C.byref(v)), f"get_tuning({name})")
+        return v.value
+
+    def autotune(self, reps: int = 3) -> str:
+        """Pick the fastest smoother schedule / cluster choice for this context's pressure solve."""
+        buf = C.create_string_buffer(4096)
+        _chk(lib().impec_autotune(self.h, reps, buf, len(buf)), "autotune")
+        return buf.value.decode()
 
     def pressure_solve_resident(self, sync=True):
         cyc, rr = C.c_int(), C.c_double()

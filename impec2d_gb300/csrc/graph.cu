@@ -7,6 +7,8 @@
 // whose condition is set on the device by the convergence-check kernel, so a step needs no
 // host round trip and steps can be queued back to back.
 #include <cmath>
+#include <string>
+#include <vector>
 
 #include "internal.cuh"
 #include "reduce.cuh"
@@ -98,12 +100,12 @@ static impec_status capture_cn_solve(impec_ctx* ctx, double* c) {
     return IMPEC_OK;
 }
 
-// Captures the step for the given alternating-sweep parity (0: X first, 1: Y first).
-static impec_status capture_step(impec_ctx* ctx, int pfs_in, cudaGraph_t* out) {
+// Captures one step, for the given alternating-sweep parity (0: X first, 1: Y first), into
+// the capture that is active on ctx->cap_stream (its own, or an ensemble's joined by an event).
+static impec_status capture_step_into(impec_ctx* ctx, int pfs_in) {
     const impec_params& P = ctx->P;
     DevScalars* S = ctx->dscal;
     const double* dt = &S->dt;
-    IMPEC_CUDA_TRY(cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeRelaxed));
     cudaStream_t saved = ctx->stream;
     ctx->stream = ctx->cap_stream;
     const long long n0 = ctx->nlaunch;
@@ -143,15 +145,29 @@ static impec_status capture_step(impec_ctx* ctx, int pfs_in, cudaGraph_t* out) {
     };
     impec_status s = body();
     ctx->stream = saved;
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
-    IMPEC_TRY(s);
-    IMPEC_CUDA_TRY(e);
     const long long loops = mg_body + (P.diffusion ? 2 * ctx->step_cn_body_launches : 0);
     ctx->step_outer_launches = ctx->nlaunch - n0 - loops;
     ctx->step_mg_body_launches = mg_body;
     ctx->nlaunch = n0;  // captured launches run (and are counted) on the device at each replay
+    return s;
+}
+
+static impec_status capture_step(impec_ctx* ctx, int pfs_in, cudaGraph_t* out) {
+    IMPEC_CUDA_TRY(cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeRelaxed));
+    impec_status s = capture_step_into(ctx, pfs_in);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
+    IMPEC_TRY(s);
+    IMPEC_CUDA_TRY(e);
     *out = g;
+    return IMPEC_OK;
+}
+
+static impec_status ensure_capture_streams(impec_ctx* ctx) {
+    if (!ctx->cap_stream) {
+        IMPEC_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+        IMPEC_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->body_stream, cudaStreamNonBlocking));
+    }
     return IMPEC_OK;
 }
 
@@ -264,3 +280,125 @@ impec_status launch_step_graph(impec_ctx* ctx, double t_clip) {
 }
 
 }  // namespace impec
+
+// ---------------------------------------------------------------- ensembles
+// Independent realisations advanced together: one CUDA graph holds every member's whole IMPES
+// step (its WHILE loops included) as a parallel branch, so one graph launch advances all
+// members and the GPU overlaps their kernels.  Members keep their own buffers, scalars and
+// reduction scratch, so the branches share nothing.
+struct impec_ensemble {
+    std::vector<impec_ctx*> m;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t fork = nullptr, done = nullptr;
+    std::vector<cudaEvent_t> join;
+};
+
+using namespace impec;
+
+static void ensemble_free(impec_ensemble* e) {
+    if (!e) return;
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    for (cudaEvent_t ev : e->join)
+        if (ev) cudaEventDestroy(ev);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->done) cudaEventDestroy(e->done);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+extern "C" impec_status impec_ensemble_create(impec_ctx* const* members, int n, impec_ensemble** out) {
+    if (!members || n < 1 || !out) return IMPEC_ERR_ARG;
+    for (int i = 0; i < n; ++i) {
+        if (!members[i]) return IMPEC_ERR_ARG;
+        if (members[i]->P.dim_splitting == IMPEC_ALTERNATING) {
+            set_error("impec_ensemble_create: members with alternating sweeps need two step variants; not supported");
+            return IMPEC_ERR_ARG;
+        }
+        for (int k = 0; k < i; ++k)
+            if (members[k] == members[i]) {
+                set_error("impec_ensemble_create: a context appears twice");
+                return IMPEC_ERR_ARG;
+            }
+    }
+    impec_ensemble* e = new impec_ensemble;
+    e->m.assign(members, members + n);
+    e->join.assign(n, nullptr);
+    auto fail = [&](impec_status s) {
+        ensemble_free(e);
+        return s;
+    };
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming) != cudaSuccess) {
+        set_error("impec_ensemble_create: stream or event creation failed");
+        return fail(IMPEC_ERR_CUDA);
+    }
+    const double no_clip = -1.0;
+    for (int i = 0; i < n; ++i) {
+        impec_ctx* c = e->m[i];
+        if (cudaEventCreateWithFlags(&e->join[i], cudaEventDisableTiming) != cudaSuccess) return fail(IMPEC_ERR_CUDA);
+        impec_status s = ensure_capture_streams(c);
+        if (s != IMPEC_OK) return fail(s);
+        if (cudaMemcpyAsync(&c->dscal->t_clip, &no_clip, sizeof(double), cudaMemcpyHostToDevice, c->stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(c->stream) != cudaSuccess) {
+            set_error("impec_ensemble_create: member stream failed");
+            return fail(IMPEC_ERR_CUDA);
+        }
+    }
+    if (cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        set_error("impec_ensemble_create: capture failed to start");
+        return fail(IMPEC_ERR_CUDA);
+    }
+    impec_status s = IMPEC_OK;
+    cudaError_t ce = cudaEventRecord(e->fork, e->stream);
+    for (int i = 0; i < n && s == IMPEC_OK && ce == cudaSuccess; ++i) {
+        impec_ctx* c = e->m[i];
+        ce = cudaStreamWaitEvent(c->cap_stream, e->fork, 0);
+        if (ce != cudaSuccess) break;
+        s = capture_step_into(c, 0);  // the variant a single context replays (non-alternating splitting)
+        if (s != IMPEC_OK) break;
+        ce = cudaEventRecord(e->join[i], c->cap_stream);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(e->stream, e->join[i], 0);
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(e->stream, &g);
+    if (s != IMPEC_OK) {
+        if (g) cudaGraphDestroy(g);
+        return fail(s);
+    }
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+        set_error(std::string("impec_ensemble_create: capture failed: ") + cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+        if (g) cudaGraphDestroy(g);
+        return fail(IMPEC_ERR_CUDA);
+    }
+    ce = cudaGraphInstantiate(&e->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+        set_error(std::string("impec_ensemble_create: instantiation failed: ") + cudaGetErrorString(ce));
+        return fail(IMPEC_ERR_CUDA);
+    }
+    *out = e;
+    return IMPEC_OK;
+}
+
+extern "C" impec_status impec_ensemble_step(impec_ensemble* e, int nsteps, int sync) {
+    if (!e || nsteps < 0) return IMPEC_ERR_ARG;
+    for (impec_ctx* c : e->m) {  // work queued on a member's own stream comes first
+        IMPEC_CUDA_TRY(cudaEventRecord(e->done, c->stream));
+        IMPEC_CUDA_TRY(cudaStreamWaitEvent(e->stream, e->done, 0));
+    }
+    for (int k = 0; k < nsteps; ++k) IMPEC_CUDA_TRY(cudaGraphLaunch(e->exec, e->stream));
+    IMPEC_CUDA_TRY(cudaEventRecord(e->done, e->stream));
+    for (impec_ctx* c : e->m) IMPEC_CUDA_TRY(cudaStreamWaitEvent(c->stream, e->done, 0));
+    if (sync) IMPEC_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return IMPEC_OK;
+}
+
+extern "C" impec_status impec_ensemble_destroy(impec_ensemble* e) {
+    if (!e) return IMPEC_OK;
+    cudaStreamSynchronize(e->stream);
+    ensemble_free(e);
+    return IMPEC_OK;
+}

@@ -115,6 +115,19 @@ struct DevScalars {
 
 }  // namespace impec
 
+namespace impec {
+// Engine tunables of one context (defaults from the IMPEC_MG_* environment at creation).
+struct Tuning {
+    long pre = 2, post = 2;        // smoother sweeps before / after the coarse correction
+    long cluster = 1;              // coarse levels in one thread-block-cluster launch
+    long cl_cells = 16384;         // largest level of the cluster V-cycle
+    long cl_cta0 = 256;            // cluster levels up to this many cells run on CTA 0
+    long coarse_cells64 = 256;     // single-CTA coarse V-cycle (nine-point path), FP64
+    long coarse_cells32 = 1024;    // the same, FP32
+    long fused32 = 0, fused64 = 0, fuse_fine = 0;  // temporally blocked level kernels (V(2,2) only)
+};
+}  // namespace impec
+
 struct impec_ctx {
     impec_params P;
     impec::Geo G;
@@ -134,6 +147,7 @@ struct impec_ctx {
     // V-cycle preconditioned conjugate gradients: iterate, search direction, A p
     double *cg_x = nullptr, *cg_p = nullptr, *cg_q = nullptr;
     int krylov = 1;  // 1: CG with one V-cycle as preconditioner; 0: stationary V-cycles
+    impec::Tuning tune;
     double solve_tol = 1e-10;  // tolerance of the pressure solve being launched or captured
     int dense_n = 0;
     int pin_i = 1, pin_j = 1;

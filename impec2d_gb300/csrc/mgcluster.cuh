@@ -30,6 +30,7 @@ struct ClusterArgs {
     int nl;  // levels handled: 0 .. nl-1 (nl-1 is the dense coarsest level)
     int nd;  // levels 0 .. nd-1 are spread over the cluster; nd .. nl-1 live on CTA 0
     int singular, dn;
+    int pre, post;  // smoother sweeps before / after the coarse correction
     int n1[CL_MAXL], n2[CL_MAXL], rows[CL_MAXL];
     unsigned off[CL_MAXL][6];  // shared-memory offsets (elements of T) of tx, ty, id, dg, x, b
     const T* tx[CL_MAXL];
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
     cl.sync();
     // down: levels spread over the cluster
     for (int l = 0; l < A.nd; ++l) {
-        for (int s = 0; s < 4; ++s) {
+        for (int s = 0; s < 2 * A.pre; ++s) {
             cl_sweep(cl, sm, rank, A, l, s & 1);
             cl.sync();
         }
@@ -231,7 +232,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
     // the small levels and the dense solve on CTA 0
     if (rank == 0) {
         for (int l = A.nd; l < A.nl - 1; ++l) {
-            for (int s = 0; s < 4; ++s) {
+            for (int s = 0; s < 2 * A.pre; ++s) {
                 cl_sweep(cl, sm, 0, A, l, s & 1);
                 __syncthreads();
             }
@@ -243,7 +244,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
         for (int l = A.nl - 2; l >= A.nd; --l) {
             cl_prolong(cl, sm, 0, A, l);
             __syncthreads();
-            for (int s = 0; s < 4; ++s) {
+            for (int s = 0; s < 2 * A.post; ++s) {
                 cl_sweep(cl, sm, 0, A, l, 1 - (s & 1));
                 __syncthreads();
             }
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
     for (int l = A.nd - 1; l >= 0; --l) {
         cl_prolong(cl, sm, rank, A, l);
         cl.sync();
-        for (int s = 0; s < 4; ++s) {
+        for (int s = 0; s < 2 * A.post; ++s) {
             cl_sweep(cl, sm, rank, A, l, 1 - (s & 1));
             cl.sync();
         }

@@ -16,6 +16,7 @@ constexpr int MGC_MAXL = 8;
 template <class T>
 struct CoarseArgs {
     int nl, singular, dn;
+    int pre, post;  // smoother sweeps before / after the coarse correction
     int n1[MGC_MAXL], n2[MGC_MAXL];
     const T* tx[MGC_MAXL];
     const T* ty[MGC_MAXL];
@@ -29,9 +30,9 @@ struct CoarseArgs {
 
 template <class T, int KIND>
 __device__ void cv_smooth(int n1, int n2, const T* tx, const T* ty, const T* a9, const T* id, const T* b, T* x,
-                          bool reverse) {
+                          bool reverse, int sweeps) {
     const int n = n1 * n2;
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < sweeps; ++s) {
         const int ncol = KIND == FACE5 ? 2 : 4;
         for (int cc = 0; cc < ncol; ++cc) {
             const int col = reverse ? ncol - 1 - cc : cc;
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
     const int L = A.nl - 1;  // dense level
     for (int l = 0; l < L; ++l) {
         const int n1 = A.n1[l], n2 = A.n2[l], c1 = A.n1[l + 1], c2 = A.n2[l + 1];
-        cv_smooth<T, KIND>(n1, n2, tx[l], ty[l], a9[l], id[l], b[l], x[l], false);
+        cv_smooth<T, KIND>(n1, n2, tx[l], ty[l], a9[l], id[l], b[l], x[l], false, A.pre);
         for (int K = threadIdx.x; K < c1 * c2; K += blockDim.x) {
             const int I = K / c2, J = K % c2;
             T s = 0;
@@ -184,7 +185,7 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
             x[l][k] = v;
         }
         __syncthreads();
-        cv_smooth<T, KIND>(n1, n2, tx[l], ty[l], a9[l], id[l], b[l], x[l], true);
+        cv_smooth<T, KIND>(n1, n2, tx[l], ty[l], a9[l], id[l], b[l], x[l], true, A.post);
     }
     const int n0 = A.n1[0] * A.n2[0];
     for (int k = threadIdx.x; k < n0; k += blockDim.x) A.x0[k] = x[0][k];

@@ -709,6 +709,17 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->cg_q, nf * 8));
         IMPEC_CUDA_TRY(cudaMemset(ctx->cg_q, 0, nf * 8));
         ctx->krylov = (int)env_long("IMPEC_MG_KRYLOV", 1) != 0;
+        Tuning& T = ctx->tune;
+        T.pre = env_long("IMPEC_MG_PRE", T.pre);
+        T.post = env_long("IMPEC_MG_POST", T.post);
+        T.cluster = env_long("IMPEC_MG_CLUSTER", T.cluster);
+        T.cl_cells = env_long("IMPEC_MG_CL_CELLS", T.cl_cells);
+        T.cl_cta0 = env_long("IMPEC_MG_CL_CTA0", T.cl_cta0);
+        T.coarse_cells64 = env_long("IMPEC_MG_COARSE_CELLS64", T.coarse_cells64);
+        T.coarse_cells32 = env_long("IMPEC_MG_COARSE_CELLS32", T.coarse_cells32);
+        T.fused32 = env_long("IMPEC_MG_FUSED32", T.fused32);
+        T.fused64 = env_long("IMPEC_MG_FUSED64", T.fused64);
+        T.fuse_fine = env_long("IMPEC_MG_FUSE_FINE", T.fuse_fine);
         if (ctx->dir_row >= 0) {
             IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dmask, nf));
             IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dfd, nf * 8));
@@ -904,8 +915,7 @@ static size_t coarse_bytes(const impec_ctx* ctx, size_t l) {
 // within the precision's limit (FP64 work on one SM is slow, FP32 is 57x faster per SM).
 template <class T>
 static size_t coarse_start(const impec_ctx* ctx) {
-    const size_t cells = (size_t)(sizeof(T) == 8 ? env_long("IMPEC_MG_COARSE_CELLS64", 256)
-                                                 : env_long("IMPEC_MG_COARSE_CELLS32", 1024));
+    const size_t cells = (size_t)(sizeof(T) == 8 ? ctx->tune.coarse_cells64 : ctx->tune.coarse_cells32);
     // with a Dirichlet row the finest level keeps its own kernels (its prolongation is masked)
     const size_t l0 = ctx->dir_row >= 0 && ctx->L.size() > 1 ? 1 : 0;
     for (size_t l = l0; l < ctx->L.size(); ++l)
@@ -918,6 +928,8 @@ static void launch_coarse(impec_ctx* ctx, size_t lc) {
     CoarseArgs<T> A{};
     A.nl = (int)(ctx->L.size() - lc);
     A.singular = ctx->singular;
+    A.pre = (int)ctx->tune.pre;
+    A.post = (int)ctx->tune.post;
     A.dn = ctx->dense_n;
     A.dinv = ctx->dense_inv;
     for (int k = 0; k < A.nl; ++k) {
@@ -947,10 +959,12 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
     const int CS = ctx->cl_size;
     const size_t nl = ctx->L.size() - ls;
     if (CS < 2 || nl < 2 || nl > (size_t)CL_MAXL || ctx->dense_n > CL_THREADS) return false;
-    const long cta0 = env_long("IMPEC_MG_CL_CTA0", 256);
+    const long cta0 = ctx->tune.cl_cta0;
     A = ClusterArgs<T>{};
     A.nl = (int)nl;
     A.singular = ctx->singular;
+    A.pre = (int)ctx->tune.pre;
+    A.post = (int)ctx->tune.post;
     A.dn = ctx->dense_n;
     A.dinv = ctx->dense_inv;
     size_t off = 0;
@@ -994,8 +1008,8 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
 // whose plan fits), or SIZE_MAX for the per-level path.
 template <class T>
 static size_t cluster_start(impec_ctx* ctx) {
-    if (ctx->cl_size < 2 || env_long("IMPEC_MG_CLUSTER", 1) == 0) return SIZE_MAX;
-    const long cells = env_long("IMPEC_MG_CL_CELLS", 16384);
+    if (ctx->cl_size < 2 || ctx->tune.cluster == 0) return SIZE_MAX;
+    const long cells = ctx->tune.cl_cells;
     ClusterArgs<T> A;
     size_t smem;
     const size_t l0 = ctx->dir_row >= 0 ? 1 : 0;  // the finest level's prolongation is masked there
@@ -1031,9 +1045,11 @@ static void launch_cluster(impec_ctx* ctx, size_t ls) {
 // GB300 they are slower than full-sweep launches in both precisions, because the halo cells
 // they recompute cost FP64 issue slots and their per-CTA phases serialise.
 template <class T>
-static bool use_fused_level(size_t l) {
-    if (sizeof(T) == 4) return env_long("IMPEC_MG_FUSED32", 0) != 0 && (l > 0 || env_long("IMPEC_MG_FUSE_FINE", 0) != 0);
-    return env_long("IMPEC_MG_FUSED64", 0) != 0 && (l > 0 || env_long("IMPEC_MG_FUSE_FINE", 0) != 0);
+static bool use_fused_level(const impec_ctx* ctx, size_t l) {
+    const Tuning& t = ctx->tune;
+    if (t.pre != 2 || t.post != 2) return false;  // the fused kernels do V(2,2)
+    const bool level_ok = l > 0 || (t.fuse_fine != 0 && ctx->dir_row < 0);
+    return level_ok && (sizeof(T) == 4 ? t.fused32 : t.fused64) != 0;
 }
 
 template <class T>
@@ -1055,7 +1071,7 @@ static void vcycle(impec_ctx* ctx, size_t l) {
     const T *ctx_, *cty, *ca9, *cid;
     T *cx, *cb;
     level_ptrs<T>(C, ctx_, cty, ca9, cid, cx, cb);
-    const bool fused = F.kind == FACE5 && use_fused_level<T>(l);
+    const bool fused = F.kind == FACE5 && use_fused_level<T>(ctx, l);
     if (fused) {  // two launches for this level: smooth+residual+restrict, prolong+smooth
         dim3 g((F.n2 + TB - 1) / TB, (F.n1 + TB - 1) / TB);
         ++ctx->nlaunch;
@@ -1065,7 +1081,7 @@ static void vcycle(impec_ctx* ctx, size_t l) {
         launch_k(ctx->stream, k_level_post<T>, g, TBT, tb_smem<T, TBH_POST>(), F.n1, F.n2, tx, ty, id, b, x, C.n1, C.n2, cx);
         return;
     }
-    smooth<T>(ctx, F, 2, false);
+    smooth<T>(ctx, F, (int)ctx->tune.pre, false);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_restrict<T>, grid2(C.n1, C.n2), dim3(BX, BY), 0, F, tx, ty, a9, level_diag<T>(F), b, x,
              C.n1, C.n2, cb, cx);
@@ -1073,7 +1089,7 @@ static void vcycle(impec_ctx* ctx, size_t l) {
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_prolong<T>, grid2(F.n1, F.n2), dim3(BX, BY), 0, F.n1, F.n2, x, C.n1, C.n2, cx,
              l == 0 && ctx->dir_row >= 0 ? ctx->dmask : nullptr);
-    smooth<T>(ctx, F, 2, true);
+    smooth<T>(ctx, F, (int)ctx->tune.post, true);
 }
 
 // Convergence check of the multigrid loop (one thread): relres = ||r||/||f||; decides whether

@@ -1,6 +1,9 @@
 // IMPES step orchestration, diagnostics, host-layout transfers and the per-operation C ABI.
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "internal.cuh"
@@ -355,6 +358,112 @@ impec_status impec_state_download(impec_ctx* ctx, double* c_host, double* p_host
             for (int j = 0; j < N2; ++j) v_host[((size_t)(i + g) * wv + (j + g)) * 2 + 0] = hu[IX(i, j, N2)];
         for (int i = 0; i < N1; ++i)
             for (int j = 0; j <= N2; ++j) v_host[((size_t)(i + g) * wv + (j + g)) * 2 + 1] = hv[IX(i, j, N2 + 1)];
+    }
+    return IMPEC_OK;
+}
+
+
+// ---------------------------------------------------------------- tuning and autotuner
+static long* tuning_field(impec_ctx* ctx, const char* name) {
+    Tuning& t = ctx->tune;
+    struct { const char* n; long* v; } tab[] = {
+        {"mg_pre", &t.pre},          {"mg_post", &t.post},         {"cluster", &t.cluster},
+        {"cluster_cells", &t.cl_cells}, {"cluster_cta0", &t.cl_cta0}, {"coarse_cells64", &t.coarse_cells64},
+        {"coarse_cells32", &t.coarse_cells32}};
+    for (auto& e : tab)
+        if (!strcmp(e.n, name)) return e.v;
+    return nullptr;
+}
+
+impec_status impec_set_tuning(impec_ctx* ctx, const char* name, long value) {
+    if (!ctx || !name) return IMPEC_ERR_ARG;
+    long* f = tuning_field(ctx, name);
+    if (!f) {
+        set_error(std::string("unknown tunable ") + name);
+        return IMPEC_ERR_ARG;
+    }
+    if (value < 0 || ((!strcmp(name, "mg_pre") || !strcmp(name, "mg_post")) && value > 8)) {
+        set_error(std::string("tunable out of range: ") + name);
+        return IMPEC_ERR_ARG;
+    }
+    if (*f != value) {
+        const long old = *f;
+        *f = value;
+        if (ctx->tune.pre + ctx->tune.post < 1) {
+            *f = old;
+            set_error("mg_pre + mg_post must be at least 1");
+            return IMPEC_ERR_ARG;
+        }
+        invalidate_step_graph(ctx);  // the captured graphs bake the launch structure in
+    }
+    return IMPEC_OK;
+}
+
+impec_status impec_get_tuning(impec_ctx* ctx, const char* name, long* value) {
+    if (!ctx || !name || !value) return IMPEC_ERR_ARG;
+    long* f = tuning_field(ctx, name);
+    if (!f) {
+        set_error(std::string("unknown tunable ") + name);
+        return IMPEC_ERR_ARG;
+    }
+    *value = *f;
+    return IMPEC_OK;
+}
+
+// Times the resident pressure solve (graph replay, CUDA events on the context stream) on the
+// context's current state for each candidate smoother schedule and cluster choice, keeps the
+// fastest, and leaves it set.  Every candidate still solves to the context's tolerance.
+impec_status impec_autotune(impec_ctx* ctx, int reps, char* report, int report_len) {
+    if (!ctx || reps < 1) return IMPEC_ERR_ARG;
+    struct Cand { long pre, post, cluster; };
+    const Cand cands[] = {{2, 2, 1}, {1, 1, 1}, {2, 1, 1}, {1, 2, 1}, {3, 3, 1}, {2, 2, 0}, {1, 1, 0}};
+    const Tuning saved = ctx->tune;
+    cudaEvent_t e0, e1;
+    IMPEC_CUDA_TRY(cudaEventCreate(&e0));
+    IMPEC_CUDA_TRY(cudaEventCreate(&e1));
+    std::string rep;
+    double best = 1e300;
+    Cand pick = {saved.pre, saved.post, saved.cluster};
+    for (const Cand& c : cands) {
+        if (c.cluster && ctx->cl_size < 2) continue;
+        IMPEC_TRY(impec_set_tuning(ctx, "mg_pre", c.pre));
+        IMPEC_TRY(impec_set_tuning(ctx, "mg_post", c.post));
+        IMPEC_TRY(impec_set_tuning(ctx, "cluster", c.cluster));
+        int cyc = 0;
+        double rr = 0;
+        impec_status s = impec_pressure_solve_resident(ctx, 1, &cyc, &rr);  // capture + warm-up
+        if (s != IMPEC_OK) continue;
+        std::vector<float> ms;
+        for (int r = 0; r < reps; ++r) {
+            IMPEC_CUDA_TRY(cudaEventRecord(e0, ctx->stream));
+            IMPEC_TRY(impec_pressure_solve_resident(ctx, 0, nullptr, nullptr));
+            IMPEC_CUDA_TRY(cudaEventRecord(e1, ctx->stream));
+            IMPEC_CUDA_TRY(cudaEventSynchronize(e1));
+            float t = 0;
+            cudaEventElapsedTime(&t, e0, e1);
+            ms.push_back(t);
+        }
+        std::sort(ms.begin(), ms.end());
+        const double med = ms[ms.size() / 2];
+        char line[160];
+        snprintf(line, sizeof line, "pre=%ld post=%ld cluster=%ld: %.4f ms, %d iterations\n", c.pre, c.post,
+                 c.cluster, med, cyc);
+        rep += line;
+        if (med < best) {
+            best = med;
+            pick = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->tune = saved;
+    invalidate_step_graph(ctx);
+    IMPEC_TRY(impec_set_tuning(ctx, "mg_pre", pick.pre));
+    IMPEC_TRY(impec_set_tuning(ctx, "mg_post", pick.post));
+    IMPEC_TRY(impec_set_tuning(ctx, "cluster", pick.cluster));
+    if (report && report_len > 0) {
+        snprintf(report, (size_t)report_len, "%schosen: pre=%ld post=%ld cluster=%ld\n", rep.c_str(), pick.pre,
+                 pick.post, pick.cluster);
     }
     return IMPEC_OK;
 }

@@ -181,6 +181,18 @@ impec_status impec_project_diagonal(impec_ctx* ctx, int field, double* out_dev, 
 /* The same into a host buffer of d_N1*d_N2 values (d_N1*d_N2 <= N1*N2); returns when it is filled. */
 impec_status impec_project_diagonal_download(impec_ctx* ctx, int field, double* out_host, int d_N1, int d_N2);
 
+/* Engine tunables of a context (no counterpart in the reference): "mg_pre", "mg_post" (smoother
+ * sweeps before / after the coarse correction, 0..8, sum >= 1), "cluster" (0/1: coarse levels in
+ * one thread-block-cluster launch), "cluster_cells", "cluster_cta0", "coarse_cells64",
+ * "coarse_cells32" (level-size thresholds).  Defaults come from the IMPEC_MG_* environment at
+ * context creation.  Changing a value drops the captured graphs. */
+impec_status impec_set_tuning(impec_ctx* ctx, const char* name, long value);
+impec_status impec_get_tuning(impec_ctx* ctx, const char* name, long* value);
+/* Autotuner: times the resident pressure solve on the context's current state (reps replays
+ * per candidate, CUDA events) for several smoother schedules and cluster choices, keeps the
+ * fastest and leaves it set.  report (may be NULL) receives one line per candidate. */
+impec_status impec_autotune(impec_ctx* ctx, int reps, char* report, int report_len);
+
 /* FP64 fused multiply-adds per second that the current device sustains (eight independent
  * chains per thread on every SM): the denominator of the FP64-pipe fractions reported beside
  * the HBM roofline.  No counterpart in the reference. */
@@ -201,6 +213,19 @@ impec_status impec_measure_fp64(double* fma_per_second);
  * overlaps on the GPU (different streams, or different host threads) race on it. */
 impec_status impec_advect_symmetric_noalloc(const impec_params* P, double* c_dev, const double* u_dev,
                                             const double* v_dev, double dt, void* stream);
+
+/* ---- ensembles of independent realisations ---- */
+/* One CUDA graph holding each member's whole IMPES step as a parallel branch, so one launch
+ * advances every member (BASELINE's batched-ensemble mode; no counterpart in the reference,
+ * whose driver runs one realisation per process).  Members must not use alternating sweeps and
+ * run without output-time clipping.  A member's later changes (source cells, tunables,
+ * permeability) are not seen by an existing ensemble: create it again. */
+typedef struct impec_ensemble impec_ensemble;
+impec_status impec_ensemble_create(impec_ctx* const* members, int n, impec_ensemble** out);
+/* nsteps graph launches on the ensemble's stream, ordered after work already queued on the
+ * members' streams and before work queued on them afterwards; sync != 0 waits for the end. */
+impec_status impec_ensemble_step(impec_ensemble* e, int nsteps, int sync);
+impec_status impec_ensemble_destroy(impec_ensemble* e);
 
 /* ---- host-buffer entry points (reference Blitz layouts; copies inside the call) ---- */
 impec_status impec_state_upload(impec_ctx* ctx, const double* c_host, const double* q_host,
