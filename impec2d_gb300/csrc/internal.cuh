@@ -148,6 +148,7 @@ struct impec_ctx {
     double *cg_x = nullptr, *cg_p = nullptr, *cg_q = nullptr;
     int krylov = 1;  // 1: CG with one V-cycle as preconditioner; 0: stationary V-cycles
     impec::Tuning tune;
+    int cn_predict = 1;  // CN starts from the explicit-Euler predictor (IMPEC_CN_PREDICT=0: from c)
     double solve_tol = 1e-10;  // tolerance of the pressure solve being launched or captured
     int dense_n = 0;
     int pin_i = 1, pin_j = 1;
@@ -214,7 +215,7 @@ impec_status advect_split_dev(impec_ctx* ctx, double* c, const double* u, const 
 impec_status average_dev(impec_ctx* ctx, double* c, const double* a, const double* b);
 // dispersion.cu
 impec_status cn_setup(impec_ctx* ctx, const double* u, const double* v, double dt_scale, const double* dt_dev);
-impec_status cn_prepare(impec_ctx* ctx, const double* c, double dt_scale, const double* dt_dev);
+impec_status cn_prepare(impec_ctx* ctx, double* c, double dt_scale, const double* dt_dev);
 impec_status cn_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h);
 impec_status cn_iteration(impec_ctx* ctx, double* c);
 impec_status dispersion_cn_dev(impec_ctx* ctx, double* c, const double* u, const double* v, double dt_scale,

@@ -720,6 +720,7 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         T.fused32 = env_long("IMPEC_MG_FUSED32", T.fused32);
         T.fused64 = env_long("IMPEC_MG_FUSED64", T.fused64);
         T.fuse_fine = env_long("IMPEC_MG_FUSE_FINE", T.fuse_fine);
+        ctx->cn_predict = env_long("IMPEC_CN_PREDICT", 1) != 0;
         if (ctx->dir_row >= 0) {
             IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dmask, nf));
             IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dfd, nf * 8));
