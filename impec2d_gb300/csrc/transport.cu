@@ -59,10 +59,20 @@ impec_status tr_integrate_dev(impec_ctx* ctx, double* c, double dt_scale, const 
 // arithmetic, minmod(a, b) (r = a/b <= 1 gives a, r > 1 gives b, a*b <= 0 gives 0); the
 // selection below evaluates that value without the three divisions.
 // kap = 0.5 dt / (dx phi).  sl: state at the cell's left face, sr: at its right face.
+// Comparisons on the integer pipe.  FP64 compares issue on the FP64 pipe, the bottleneck of
+// the transport kernels on GB300; for non-NaN doubles these are exact equivalents (a NaN
+// operand still yields a NaN result through the arithmetic around them).
+// x > 0: the bit pattern, read as a signed integer, is positive (+0 is 0, negatives are < 0).
+__device__ __forceinline__ bool pos(double x) { return __double_as_longlong(x) > 0LL; }
+// |a| <= |b|: IEEE magnitudes order like their bit patterns with the sign bit cleared.
+__device__ __forceinline__ bool abs_le(double a, double b) {
+    return (__double_as_longlong(a) & 0x7fffffffffffffffLL) <= (__double_as_longlong(b) & 0x7fffffffffffffffLL);
+}
+
 __device__ __forceinline__ void hancock(double cm, double c0, double cp, double ul, double ur, double kap,
                                         double& sl, double& sr) {
     double a = c0 - cm, b = cp - c0;
-    double d = (a * b > 0.0) ? (fabs(a) <= fabs(b) ? a : b) : 0.0;
+    double d = pos(a * b) ? (abs_le(a, b) ? a : b) : 0.0;
     double UR = fma(0.5, d, c0), UL = fma(-0.5, d, c0);
     double df = kap * (ul * UL - ur * UR);
     sl = UL + df;
@@ -108,8 +118,8 @@ __device__ __forceinline__ double sweep_cell(const double* __restrict__ c, const
     double Fw, Fe;
     if (SCHEME == IMPEC_UPWINDSPLIT) {  // src/UpwindSplitSolver.cpp:43-65
         double cm = C(k - 1), c0 = C(k), cp = C(k + 1);
-        Fw = uw * (uw > 0 ? cm : c0);
-        Fe = ue * (ue > 0 ? c0 : cp);
+        Fw = uw * (pos(uw) ? cm : c0);
+        Fe = ue * (pos(ue) ? c0 : cp);
         return c0 + lam * (Fw - Fe);
     }
     double cmm = C(k - 2), cm = C(k - 1), c0 = C(k), cp = C(k + 1), cpp = C(k + 2);
@@ -120,8 +130,8 @@ __device__ __forceinline__ double sweep_cell(const double* __restrict__ c, const
     hancock(c0, cp, cpp, ue, uee, kap, slp, srp);
     (void)slm;
     (void)srp;
-    Fw = uw * (uw > 0 ? srm : sl0);
-    Fe = ue * (ue > 0 ? sr0 : slp);
+    Fw = uw * (pos(uw) ? srm : sl0);
+    Fe = ue * (pos(ue) ? sr0 : slp);
     return c0 + lam * (Fw - Fe);
 }
 
@@ -218,8 +228,8 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_advect_symmetric(int n1, int 
     for (int k = t; k < TI * CW; k += FUSED_THREADS) {
         int a = k / CW, b = k % CW;  // cell i = i0+a: states at a+1, faces fi = i0+a (su row a+1), i0+a+1
         double uw = su[(a + 1) * CW + b], ue = su[(a + 2) * CW + b];
-        double Fw = uw * (uw > 0 ? hr[a * CW + b] : hl[(a + 1) * CW + b]);
-        double Fe = ue * (ue > 0 ? hr[(a + 1) * CW + b] : hl[(a + 2) * CW + b]);
+        double Fw = uw * (pos(uw) ? hr[a * CW + b] : hl[(a + 1) * CW + b]);
+        double Fe = ue * (pos(ue) ? hr[(a + 1) * CW + b] : hl[(a + 2) * CW + b]);
         s1[k] = sc[(a + 2) * CW + b] + lx * (Fw - Fe);
     }
     __syncthreads();
@@ -236,8 +246,8 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_advect_symmetric(int n1, int 
         const double* vr = sv + (a + 2) * VW;
         const int h = a * (TJ + 2);
         double vs = vr[b + 1], vn = vr[b + 2];
-        double Fs = vs * (vs > 0 ? hr[h + b] : hl[h + b + 1]);
-        double Fn = vn * (vn > 0 ? hr[h + b + 1] : hl[h + b + 2]);
+        double Fs = vs * (pos(vs) ? hr[h + b] : hl[h + b + 1]);
+        double Fn = vn * (pos(vn) ? hr[h + b + 1] : hl[h + b + 2]);
         sxy[k] = s1[a * CW + b + 2] + ly * (Fs - Fn);
     }
     __syncthreads();
@@ -254,8 +264,8 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_advect_symmetric(int n1, int 
         const double* vr = sv + a * VW;
         const int h = a * (TJ + 2);
         double vs = vr[b + 1], vn = vr[b + 2];
-        double Fs = vs * (vs > 0 ? hr[h + b] : hl[h + b + 1]);
-        double Fn = vn * (vn > 0 ? hr[h + b + 1] : hl[h + b + 2]);
+        double Fs = vs * (pos(vs) ? hr[h + b] : hl[h + b + 1]);
+        double Fn = vn * (pos(vn) ? hr[h + b + 1] : hl[h + b + 2]);
         s2[k] = sc[a * CW + b + 2] + ly * (Fs - Fn);
     }
     __syncthreads();
@@ -271,8 +281,8 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_advect_symmetric(int n1, int 
         const int gi = i0 + a, gj = j0 + b;
         if (gi >= n1 || gj >= n2) continue;
         double uw = su[(a + 1) * CW + b + 2], ue = su[(a + 2) * CW + b + 2];
-        double Fw = uw * (uw > 0 ? hr[a * TJ + b] : hl[(a + 1) * TJ + b]);
-        double Fe = ue * (ue > 0 ? hr[(a + 1) * TJ + b] : hl[(a + 2) * TJ + b]);
+        double Fw = uw * (pos(uw) ? hr[a * TJ + b] : hl[(a + 1) * TJ + b]);
+        double Fe = ue * (pos(ue) ? hr[(a + 1) * TJ + b] : hl[(a + 2) * TJ + b]);
         double yx = s2[(a + 2) * TJ + b] + lx * (Fw - Fe);
         cout[IX(gi, gj, n2)] = 0.5 * (sxy[k] + yx);
     }

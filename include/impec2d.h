@@ -193,6 +193,13 @@ impec_status impec_get_tuning(impec_ctx* ctx, const char* name, long* value);
  * fastest and leaves it set.  report (may be NULL) receives one line per candidate. */
 impec_status impec_autotune(impec_ctx* ctx, int reps, char* report, int report_len);
 
+/* Tensor-core GEMM of the learned warm start (no counterpart in the reference):
+ * C[M x N] (fp32, row stride ldc) = A[M x K] (bf16, row stride lda) * B[N x K]^T (bf16, row
+ * stride ldb), device pointers, on `stream`; returns after it completes.  K must be a multiple
+ * of 64, lda and ldb multiples of 8, the operands 16-byte aligned. */
+impec_status impec_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, int M, int N, int K,
+                             void* stream);
+
 /* FP64 fused multiply-adds per second that the current device sustains (eight independent
  * chains per thread on every SM): the denominator of the FP64-pipe fractions reported beside
  * the HBM roofline.  No counterpart in the reference. */
