@@ -107,6 +107,11 @@ _SIGS = {
     "impec_get_tuning": (C.c_int, [_VP, C.c_char_p, C.POINTER(C.c_long)]),
     "impec_autotune": (C.c_int, [_VP, C.c_int, C.c_char_p, C.c_int]),
     "impec_gemm_bf16": (C.c_int, [_VP, C.c_int, _VP, C.c_int, _VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP]),
+    "impec_conv3x3_forward": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP, C.c_int, C.c_int, _VP, _VP,
+                                        _VP, _VP, _VP]),
+    "impec_conv3x3_input_grad": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, C.c_int, _VP, _VP, _VP, _VP,
+                                           _VP]),
+    "impec_conv3x3_weight_grad": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "impec_ensemble_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "impec_ensemble_step": (C.c_int, [_VP, C.c_int, C.c_int]),
     "impec_ensemble_destroy": (C.c_int, [_VP]),

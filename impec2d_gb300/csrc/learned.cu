@@ -11,6 +11,7 @@
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <string>
 
 #include "internal.cuh"
 #include "umma.cuh"
@@ -99,6 +100,257 @@ __global__ void __launch_bounds__(GB_THREADS) k_gemm_bf16_tn(int M, int N, int K
     if (warp == 0) umma::tmem_free(tmem, GB_TMEM_COLS);
 }
 
+// ---------------------------------------------------------------- 3x3 convolution (implicit GEMM)
+// Activations are NHWC bf16 with C a multiple of 8.  Weights are [cout rows][Kp] bf16 with
+// k = tap * cin + c (tap = 3 * (dy + 1) + (dx + 1)), Kp = 9 cin rounded up to 64, zero beyond.
+// GEMM rows are the B*H*W output pixels (128 per CTA), columns the output channels (BN per
+// CTA), K the taps x input channels: each 16-byte chunk of the A tile is one tap's 8 channels
+// of one pixel, copied from the neighbour (y + s dy, x + s dx) or zero-filled outside the image
+// (s = +1 forward; s = -1 gives the transposed convolution of the input gradient, with the
+// weights rearranged by k_conv_wt_transpose).  Epilogue per (pixel, channel):
+//   v = acc + bias;  then either  Z = v, Y = act(v) (+ skip)          (forward)
+//                    or           Y = (v + add) * gelu'(gz)            (input gradient)
+struct ConvArgs {
+    const __nv_bfloat16* X;  // input activations [B][H][W][cin]
+    const __nv_bfloat16* W;  // weights [cout_rows][Kp]
+    const float* bias;       // [cout] or null
+    __nv_bfloat16* Z;        // pre-activation output or null
+    __nv_bfloat16* Y;        // output (activation, or gradient) or null
+    float* Yf;               // fp32 output or null
+    const __nv_bfloat16* skip;  // added after the activation, or null
+    const __nv_bfloat16* add;   // gradient mode: added before the gelu' factor, or null
+    const __nv_bfloat16* gz;    // gradient mode: pre-activation of the layer whose gradient this is
+    __nv_bfloat16* R;           // gradient mode: the raw gradient (acc) as well, or null
+    int B, H, W_, cin, cout, Kp, tapsign, act;
+    int* err;
+};
+
+__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+template <int BN>
+__global__ void __launch_bounds__(GB_THREADS) k_conv3x3(ConvArgs a) {
+    extern __shared__ __align__(1024) unsigned char cv_smem[];
+    unsigned char* sA = cv_smem;
+    unsigned char* sB = cv_smem + GB_TILE_BYTES;
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tslot;
+    constexpr uint32_t TCOLS = BN < 32 ? 32 : BN;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int M = a.B * a.H * a.W_;
+    const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * BN;
+    if (warp == 0) umma::tmem_alloc(&tslot, TCOLS);
+    if (tid == 0) umma::mbar_init(&mbar, 1);
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+    const uint32_t idesc = umma::idesc_bf16_f32(GB_M, BN);
+    const int nk = a.Kp / GB_K, K9 = 9 * a.cin;
+    bool ok = true;
+    int issued = 0;
+    for (int kt = 0; kt < nk; ++kt) {
+        for (int c = tid; c < GB_M * 8; c += GB_THREADS) {  // A: 128 pixels x 8 chunks
+            const int r = c >> 3, kg = c & 7, m = m0 + r, k0 = kt * GB_K + kg * 8;
+            const __nv_bfloat16* src = a.X;
+            uint32_t bytes = 0;
+            if (m < M && k0 < K9) {
+                const int tap = k0 / a.cin, ch = k0 - tap * a.cin;
+                const int x = m % a.W_, t = m / a.W_, y = t % a.H, b = t / a.H;
+                const int yy = y + a.tapsign * (tap / 3 - 1), xx = x + a.tapsign * (tap % 3 - 1);
+                if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W_) {
+                    src = a.X + (((size_t)b * a.H + yy) * a.W_ + xx) * a.cin + ch;
+                    bytes = 16;
+                }
+            }
+            umma::cp_async16(sA + tile_off(r, kg), src, bytes);
+        }
+        for (int c = tid; c < BN * 8; c += GB_THREADS) {  // B: BN weight rows x 8 chunks
+            const int r = c >> 3, kg = c & 7, n = n0 + r;
+            const bool in = n < a.cout;
+            umma::cp_async16(sB + tile_off(r, kg), in ? a.W + (size_t)n * a.Kp + (size_t)kt * GB_K + kg * 8 : a.W,
+                             in ? 16u : 0u);
+        }
+        umma::cp_async_wait_all();
+        umma::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fence_after();
+#pragma unroll
+            for (int ks = 0; ks < GB_K / 16; ++ks) {
+                const uint64_t ad = umma::smem_desc(umma::smem_u32(sA) + ks * 256, 128, 1024);
+                const uint64_t bd = umma::smem_desc(umma::smem_u32(sB) + ks * 256, 128, 1024);
+                umma::mma_bf16(tmem, ad, bd, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+            }
+            umma::commit(&mbar);
+        }
+        issued = kt + 1;
+        const bool done = umma::mbar_wait(&mbar, (uint32_t)(kt & 1), GB_WAIT_TRIES);
+        ok = __syncthreads_and(done) != 0;
+        if (!ok) break;
+        umma::fence_after();
+    }
+    if (ok) {
+        const int m = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int cb = 0; cb < (BN + 31) / 32; ++cb) {
+            float v[32];
+            umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
+            if (m >= M) continue;
+            const size_t row = (size_t)m * a.cout;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+                const int n = n0 + cb * 32 + k;
+                if (n >= a.cout || cb * 32 + k >= BN) continue;
+                float z = v[k] + (a.bias ? a.bias[n] : 0.0f);
+                if (a.gz) {  // input gradient: (acc + add) * gelu'(gz)
+                    if (a.R) a.R[row + n] = __float2bfloat16(z);
+                    if (a.add) z += __bfloat162float(a.add[row + n]);
+                    z *= gelu_grad(__bfloat162float(a.gz[row + n]));
+                    if (a.Y) a.Y[row + n] = __float2bfloat16(z);
+                    if (a.Yf) a.Yf[row + n] = z;
+                    continue;
+                }
+                if (a.Z) a.Z[row + n] = __float2bfloat16(z);
+                float y = a.act ? gelu_f(z) : z;
+                if (a.skip) y += __bfloat162float(a.skip[row + n]);
+                if (a.Y) a.Y[row + n] = __float2bfloat16(y);
+                if (a.Yf) a.Yf[row + n] = y;
+            }
+        }
+    } else {
+        if (tid == 0) atomicExch(a.err, 1);
+        umma::mbar_wait(&mbar, (uint32_t)((issued - 1) & 1), GB_WAIT_TRIES);
+    }
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    if (warp == 0) umma::tmem_free(tmem, TCOLS);
+}
+
+// Weights of the input-gradient convolution: Wd[ci][tap * cout + co] = W[co][tap * cin + ci],
+// Kd = 9 cout rounded up to 64.  The taps keep their index: k_conv3x3 with tapsign = -1 reads
+// the neighbour at -d, which is the transposed convolution.
+__global__ void k_conv_wt_transpose(const __nv_bfloat16* __restrict__ W, int cin, int cout, int Kp,
+                                    __nv_bfloat16* __restrict__ Wd, int Kd) {
+    const size_t n = (size_t)cin * Kd;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const int ci = (int)(idx / Kd), k = (int)(idx % Kd);
+        __nv_bfloat16 v = __float2bfloat16(0.0f);
+        if (k < 9 * cout) {
+            const int tap = k / cout, co = k % cout;
+            v = W[(size_t)co * Kp + (size_t)tap * cin + ci];
+        }
+        Wd[idx] = v;
+    }
+}
+
+// Weight gradient: dW[co][tap * cin + ci] += sum over pixels p of dZ[p][co] * X[p + d(tap)][ci].
+// GEMM rows: output channels (128 per CTA), columns: (tap, ci) pairs (128 per CTA), K: pixels,
+// split over blockIdx.z (each CTA adds its partial sums with fp32 atomics).  Both operands are
+// channel-contiguous in memory, so the staging transposes them: every 16-byte load (8 channels
+// of one pixel) is scattered into 8 rows of the K-major tile.
+__global__ void __launch_bounds__(GB_THREADS) k_conv_wgrad(const __nv_bfloat16* __restrict__ dZ,
+                                                           const __nv_bfloat16* __restrict__ X, int B, int H, int W_,
+                                                           int cin, int cout, int Kp, int pix_per_split,
+                                                           float* __restrict__ dW, int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char wg_smem[];
+    unsigned char* sA = wg_smem;
+    unsigned char* sB = wg_smem + GB_TILE_BYTES;
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int P = B * H * W_, K9 = 9 * cin;
+    const int co0 = blockIdx.y * GB_M, k0 = blockIdx.x * GB_N;
+    const int p_begin = blockIdx.z * pix_per_split;
+    const int p_end = p_begin + pix_per_split < P ? p_begin + pix_per_split : P;
+    if (warp == 0) umma::tmem_alloc(&tslot, GB_TMEM_COLS);
+    if (tid == 0) umma::mbar_init(&mbar, 1);
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+    const uint32_t idesc = umma::idesc_bf16_f32(GB_M, GB_N);
+    const int nk = p_end > p_begin ? (p_end - p_begin + GB_K - 1) / GB_K : 0;
+    bool ok = true;
+    int issued = 0;
+    __nv_bfloat16* a16 = reinterpret_cast<__nv_bfloat16*>(sA);
+    __nv_bfloat16* b16 = reinterpret_cast<__nv_bfloat16*>(sB);
+    for (int kt = 0; kt < nk; ++kt) {
+        const int pb = p_begin + kt * GB_K;
+        // A: rows co (128), K = 64 pixels.  One task = 8 channels of one pixel (16 bytes).
+        for (int c = tid; c < (GB_M / 8) * GB_K; c += GB_THREADS) {
+            const int cg = c / GB_K, kk = c % GB_K, p = pb + kk, co = co0 + cg * 8;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (p < p_end && co < cout) v = *reinterpret_cast<const uint4*>(dZ + (size_t)p * cout + co);
+            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int r = cg * 8 + q;  // tile row
+                a16[(tile_off(r, kk >> 3) >> 1) + (kk & 7)] = e[q];
+            }
+        }
+        // B: rows n = (tap, ci) (128), K = 64 pixels.  One task = 8 input channels of one tap.
+        for (int c = tid; c < (GB_N / 8) * GB_K; c += GB_THREADS) {
+            const int ng = c / GB_K, kk = c % GB_K, p = pb + kk, n = k0 + ng * 8;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (p < p_end && n < K9) {
+                const int tap = n / cin, ci = n - tap * cin;
+                const int x = p % W_, t = p / W_, y = t % H, b = t / H;
+                const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+                if (yy >= 0 && yy < H && xx >= 0 && xx < W_)
+                    v = *reinterpret_cast<const uint4*>(X + (((size_t)b * H + yy) * W_ + xx) * cin + ci);
+            }
+            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int r = ng * 8 + q;
+                b16[(tile_off(r, kk >> 3) >> 1) + (kk & 7)] = e[q];
+            }
+        }
+        umma::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fence_after();
+#pragma unroll
+            for (int ks = 0; ks < GB_K / 16; ++ks) {
+                const uint64_t ad = umma::smem_desc(umma::smem_u32(sA) + ks * 256, 128, 1024);
+                const uint64_t bd = umma::smem_desc(umma::smem_u32(sB) + ks * 256, 128, 1024);
+                umma::mma_bf16(tmem, ad, bd, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+            }
+            umma::commit(&mbar);
+        }
+        issued = kt + 1;
+        const bool done = umma::mbar_wait(&mbar, (uint32_t)(kt & 1), GB_WAIT_TRIES);
+        ok = __syncthreads_and(done) != 0;
+        if (!ok) break;
+        umma::fence_after();
+    }
+    if (ok && nk > 0) {
+        const int co = co0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int cb = 0; cb < GB_N / 32; ++cb) {
+            float v[32];
+            umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
+            if (co >= cout) continue;
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                const int k = k0 + cb * 32 + q;
+                if (k < K9) atomicAdd(dW + (size_t)co * Kp + k, v[q]);
+            }
+        }
+    } else if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+        umma::mbar_wait(&mbar, (uint32_t)((issued - 1) & 1), GB_WAIT_TRIES);
+    }
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    if (warp == 0) umma::tmem_free(tmem, GB_TMEM_COLS);
+}
+
 static int* device_error_flag() {
     static int* flag = nullptr;
     if (!flag) {
@@ -123,9 +375,131 @@ impec_status gemm_bf16_tn(int M, int N, int K, const void* A, int lda, const voi
     return IMPEC_OK;
 }
 
+static int conv_kp(int cin) { return (9 * cin + GB_K - 1) / GB_K * GB_K; }
+
+template <int BN>
+static impec_status launch_conv_bn(const ConvArgs& a, cudaStream_t s) {
+    static bool attr = false;
+    const int smem = 2 * GB_TILE_BYTES + 1024;
+    if (!attr) {
+        IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_conv3x3<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    const int M = a.B * a.H * a.W_;
+    dim3 g((a.cout + BN - 1) / BN, (M + GB_M - 1) / GB_M);
+    k_conv3x3<BN><<<g, GB_THREADS, smem, s>>>(a);
+    IMPEC_CUDA_TRY(cudaGetLastError());
+    return IMPEC_OK;
+}
+
+// The output-channel tile: the smallest of 32, 64, 128 covering cout (128 beyond).
+impec_status launch_conv(const ConvArgs& a, cudaStream_t s) {
+    if (a.cout <= 32) return launch_conv_bn<32>(a, s);
+    if (a.cout <= 64) return launch_conv_bn<64>(a, s);
+    return launch_conv_bn<128>(a, s);
+}
+
+impec_status launch_wgrad(const __nv_bfloat16* dZ, const __nv_bfloat16* X, int B, int H, int W_, int cin, int cout,
+                          float* dW, int* err, int num_sms, cudaStream_t s) {
+    static bool attr = false;
+    const int smem = 2 * GB_TILE_BYTES + 1024;
+    if (!attr) {
+        IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    const int P = B * H * W_, Kp = conv_kp(cin);
+    const int nt = (9 * cin + GB_N - 1) / GB_N, mt = (cout + GB_M - 1) / GB_M;
+    int splits = (2 * num_sms + nt * mt - 1) / (nt * mt);  // about two waves of CTAs
+    int per = (P + splits - 1) / splits;
+    per = (per + GB_K - 1) / GB_K * GB_K;
+    splits = (P + per - 1) / per;
+    dim3 g(nt, mt, splits);
+    k_conv_wgrad<<<g, GB_THREADS, smem, s>>>(dZ, X, B, H, W_, cin, cout, Kp, per, dW, err);
+    IMPEC_CUDA_TRY(cudaGetLastError());
+    return IMPEC_OK;
+}
+
+static impec_status check_err(int* err, cudaStream_t s, const char* what) {
+    int h = 0;
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h) {
+        cudaMemsetAsync(err, 0, sizeof(int), s);
+        set_error(std::string(what) + ": a tensor-core wait timed out");
+        return IMPEC_ERR_CUDA;
+    }
+    return IMPEC_OK;
+}
+
 }  // namespace impec
 
 using namespace impec;
+
+static bool conv_shape_ok(int B, int H, int W, int cin, int cout) {
+    return B > 0 && H > 0 && W > 0 && cin > 0 && cout > 0 && cin % 8 == 0 && cout % 8 == 0 &&
+           (long long)B * H * W < (1LL << 31) / 256;
+}
+
+extern "C" impec_status impec_conv3x3_forward(const void* X, int B, int H, int W, int cin, const void* Wt,
+                                              const float* bias, int cout, int act, void* Z, void* Y, float* Yf,
+                                              const void* skip, void* stream) {
+    if (!X || !Wt || !conv_shape_ok(B, H, W, cin, cout) || (!Z && !Y && !Yf)) {
+        set_error("impec_conv3x3_forward: bad arguments (channels must be multiples of 8)");
+        return IMPEC_ERR_ARG;
+    }
+    int* err = device_error_flag();
+    if (!err) return IMPEC_ERR_CUDA;
+    ConvArgs a = {};
+    a.X = (const __nv_bfloat16*)X; a.W = (const __nv_bfloat16*)Wt; a.bias = bias;
+    a.Z = (__nv_bfloat16*)Z; a.Y = (__nv_bfloat16*)Y; a.Yf = Yf; a.skip = (const __nv_bfloat16*)skip;
+    a.B = B; a.H = H; a.W_ = W; a.cin = cin; a.cout = cout; a.Kp = conv_kp(cin); a.tapsign = 1; a.act = act; a.err = err;
+    cudaStream_t s = (cudaStream_t)stream;
+    IMPEC_TRY(launch_conv(a, s));
+    return check_err(err, s, "impec_conv3x3_forward");
+}
+
+// dX (or the gradient of the pre-activation below, when gz is given) from dZ: the transposed
+// convolution with weights rearranged from W.
+extern "C" impec_status impec_conv3x3_input_grad(const void* dZ, int B, int H, int W, int cout, const void* Wt,
+                                                 int cin, const void* gz, const void* add, void* Y, float* Yf,
+                                                 void* stream) {
+    if (!dZ || !Wt || !conv_shape_ok(B, H, W, cin, cout) || (!Y && !Yf)) {
+        set_error("impec_conv3x3_input_grad: bad arguments");
+        return IMPEC_ERR_ARG;
+    }
+    int* err = device_error_flag();
+    if (!err) return IMPEC_ERR_CUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int Kp = conv_kp(cin), Kd = conv_kp(cout);
+    __nv_bfloat16* Wd = nullptr;
+    IMPEC_CUDA_TRY(cudaMallocAsync((void**)&Wd, (size_t)cin * Kd * 2, s));
+    k_conv_wt_transpose<<<64, 256, 0, s>>>((const __nv_bfloat16*)Wt, cin, cout, Kp, Wd, Kd);
+    ConvArgs a = {};
+    a.X = (const __nv_bfloat16*)dZ; a.W = Wd; a.gz = (const __nv_bfloat16*)gz; a.add = (const __nv_bfloat16*)add;
+    a.Y = (__nv_bfloat16*)Y; a.Yf = Yf;
+    a.B = B; a.H = H; a.W_ = W; a.cin = cout; a.cout = cin; a.Kp = Kd; a.tapsign = -1; a.err = err;
+    impec_status st = launch_conv(a, s);
+    cudaFreeAsync(Wd, s);
+    IMPEC_TRY(st);
+    return check_err(err, s, "impec_conv3x3_input_grad");
+}
+
+// dW (fp32 [cout][Kp], accumulated into) from dZ and the layer input X.
+extern "C" impec_status impec_conv3x3_weight_grad(const void* dZ, const void* X, int B, int H, int W, int cin,
+                                                  int cout, float* dW, void* stream) {
+    if (!dZ || !X || !dW || !conv_shape_ok(B, H, W, cin, cout)) {
+        set_error("impec_conv3x3_weight_grad: bad arguments");
+        return IMPEC_ERR_ARG;
+    }
+    int* err = device_error_flag();
+    if (!err) return IMPEC_ERR_CUDA;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaStream_t s = (cudaStream_t)stream;
+    IMPEC_TRY(launch_wgrad((const __nv_bfloat16*)dZ, (const __nv_bfloat16*)X, B, H, W, cin, cout, dW, err, sms, s));
+    return check_err(err, s, "impec_conv3x3_weight_grad");
+}
 
 extern "C" impec_status impec_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, int M,
                                         int N, int K, void* stream) {

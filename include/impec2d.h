@@ -200,6 +200,20 @@ impec_status impec_autotune(impec_ctx* ctx, int reps, char* report, int report_l
 impec_status impec_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, int M, int N, int K,
                              void* stream);
 
+/* 3x3 convolutions of the learned warm start on tcgen05 (no counterpart in the reference).
+ * Activations NHWC bf16, channels multiples of 8; weights Wt [cout][Kp] bf16 with
+ * k = tap * cin + c, tap = 3 (dy + 1) + (dx + 1), Kp = 9 cin rounded up to 64, zero padded.
+ * Forward: v = conv(X) + bias; Z = v (bf16, optional), Y = act(v) (+ skip) (bf16, optional),
+ * Yf = the same in fp32 (optional); act 0 = none, 1 = GELU.  Input gradient: the transposed
+ * convolution of dZ; with gz given, multiplied by gelu'(gz) after adding `add`.  Weight
+ * gradient: dW [cout][Kp] fp32 is accumulated into.  All return after completion. */
+impec_status impec_conv3x3_forward(const void* X, int B, int H, int W, int cin, const void* Wt, const float* bias,
+                                   int cout, int act, void* Z, void* Y, float* Yf, const void* skip, void* stream);
+impec_status impec_conv3x3_input_grad(const void* dZ, int B, int H, int W, int cout, const void* Wt, int cin,
+                                      const void* gz, const void* add, void* Y, float* Yf, void* stream);
+impec_status impec_conv3x3_weight_grad(const void* dZ, const void* X, int B, int H, int W, int cin, int cout, float* dW,
+                                       void* stream);
+
 /* FP64 fused multiply-adds per second that the current device sustains (eight independent
  * chains per thread on every SM): the denominator of the FP64-pipe fractions reported beside
  * the HBM roofline.  No counterpart in the reference. */

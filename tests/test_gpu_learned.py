@@ -29,3 +29,79 @@ def test_gemm_bf16_matches_fp32_reference(engine, M, N, K):
     ref = A.float() @ B.float().T
     assert torch.isfinite(got).all()
     assert (got - ref).abs().max().item() <= 1e-5 * ref.abs().max().item() + 1e-6
+
+
+def _vp(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _conv_setup(B, H, W, cin, cout, seed):
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    X = torch.randn((B, H, W, cin), generator=g, device="cuda").to(torch.bfloat16)
+    Kp = (9 * cin + 63) // 64 * 64
+    Wt = torch.zeros((cout, Kp), device="cuda", dtype=torch.bfloat16)
+    Wt[:, :9 * cin] = (torch.randn((cout, 9 * cin), generator=g, device="cuda") / (3.0 * cin ** 0.5)).to(torch.bfloat16)
+    bias = torch.randn(cout, generator=g, device="cuda") * 0.1
+    return X, Wt, bias
+
+
+def _w4(Wt, cin, cout):
+    """(cout, Kp) with k = tap * cin + c, tap = 3 (dy + 1) + (dx + 1)  ->  conv2d weights (cout, cin, 3, 3)."""
+    return Wt[:, :9 * cin].float().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2).contiguous()
+
+
+@pytest.mark.parametrize("B,H,W,cin,cout", [(2, 20, 20, 8, 32), (1, 37, 29, 32, 64), (2, 16, 24, 64, 256),
+                                            (1, 12, 12, 128, 128)])
+def test_conv3x3_forward_and_gradients(engine, B, H, W, cin, cout):
+    """Implicit-GEMM convolution on tcgen05: forward (linear; GELU with a skip add), input
+    gradient (plain; times gelu'(z) with an added gradient) and weight gradient, against
+    PyTorch fp32 conv2d / autograd of the same bf16 inputs."""
+    import torch
+    import torch.nn.functional as F
+    E = engine
+    L = E.lib()
+    X, Wt, bias = _conv_setup(B, H, W, cin, cout, B * 1000 + cin * 10 + cout)
+    w4 = _w4(Wt, cin, cout)
+    x = X.float().permute(0, 3, 1, 2).contiguous().requires_grad_(True)
+    z_ref = F.conv2d(x, w4, bias, padding=1)
+    zf = torch.empty((B, H, W, cout), device="cuda")
+    assert L.impec_conv3x3_forward(_vp(X), B, H, W, cin, _vp(Wt), _vp(bias), cout, 0, None, None, _vp(zf), None,
+                                   None) == 0, E.last_error()
+    zr = z_ref.detach().permute(0, 2, 3, 1)
+    scale = zr.abs().max().item()
+    assert (zf - zr).abs().max().item() <= 2e-5 * scale + 1e-6
+    # GELU + skip, bf16 outputs
+    skip = torch.randn((B, H, W, cout), device="cuda").to(torch.bfloat16)
+    Z = torch.empty((B, H, W, cout), device="cuda", dtype=torch.bfloat16)
+    Y = torch.empty_like(Z)
+    assert L.impec_conv3x3_forward(_vp(X), B, H, W, cin, _vp(Wt), _vp(bias), cout, 1, _vp(Z), _vp(Y), None, _vp(skip),
+                                   None) == 0, E.last_error()
+    y_ref = F.gelu(zr) + skip.float()
+    assert (Z.float() - zr).abs().max().item() <= 1e-2 * scale
+    assert (Y.float() - y_ref).abs().max().item() <= 1e-2 * (y_ref.abs().max().item() + 1)
+    # gradients
+    dZ = (torch.randn((B, H, W, cout), device="cuda") * 0.5).to(torch.bfloat16)
+    z_ref.backward(dZ.float().permute(0, 3, 1, 2))
+    dx_ref = x.grad.permute(0, 2, 3, 1)
+    dxf = torch.empty((B, H, W, cin), device="cuda")
+    assert L.impec_conv3x3_input_grad(_vp(dZ), B, H, W, cout, _vp(Wt), cin, None, None, None, _vp(dxf), None) == 0, \
+        E.last_error()
+    assert (dxf - dx_ref).abs().max().item() <= 2e-5 * dx_ref.abs().max().item() + 1e-6
+    gz = torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16)
+    add = torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16)
+    dgf = torch.empty((B, H, W, cin), device="cuda")
+    assert L.impec_conv3x3_input_grad(_vp(dZ), B, H, W, cout, _vp(Wt), cin, _vp(gz), _vp(add), None, _vp(dgf),
+                                      None) == 0, E.last_error()
+    gzf = gz.float()
+    gelu_d = 0.5 * (1 + torch.erf(gzf / 2 ** 0.5)) + gzf * torch.exp(-0.5 * gzf * gzf) / (2 * torch.pi) ** 0.5
+    dg_ref = (dx_ref + add.float()) * gelu_d
+    assert (dgf - dg_ref).abs().max().item() <= 1e-4 * dg_ref.abs().max().item() + 1e-5
+    Kp = Wt.shape[1]
+    dW = torch.zeros((cout, Kp), device="cuda")
+    assert L.impec_conv3x3_weight_grad(_vp(dZ), _vp(X), B, H, W, cin, cout, _vp(dW), None) == 0, E.last_error()
+    dw_ref = torch.zeros_like(dW)
+    dw_ref[:, :9 * cin] = torch.autograd.grad(
+        F.conv2d(X.float().permute(0, 3, 1, 2), w4.requires_grad_(True), None, padding=1),
+        w4, dZ.float().permute(0, 3, 1, 2))[0].permute(0, 2, 3, 1).reshape(cout, 9 * cin)
+    assert (dW - dw_ref).abs().max().item() <= 2e-5 * dw_ref.abs().max().item() + 1e-5
