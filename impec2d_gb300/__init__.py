@@ -112,6 +112,14 @@ _SIGS = {
     "impec_conv3x3_input_grad": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, C.c_int, _VP, _VP, _VP, _VP,
                                            _VP]),
     "impec_conv3x3_weight_grad": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
+    "impec_net_create": (C.c_int, [C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    "impec_net_destroy": (C.c_int, [_VP]),
+    "impec_net_train_batch": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _PD, _VP]),
+    "impec_net_backprop": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, _PD, _VP]),
+    "impec_net_forward": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, _VP, _VP]),
+    "impec_net_parameters": (C.c_int, [_VP, _VP, _VP, C.POINTER(C.c_size_t), C.c_int]),
+    "impec_net_features": (C.c_int, [_VP, _VP, _VP, _PD]),
+    "impec_net_warm_start": (C.c_int, [_VP, _VP, _VP]),
     "impec_ensemble_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "impec_ensemble_step": (C.c_int, [_VP, C.c_int, C.c_int]),
     "impec_ensemble_destroy": (C.c_int, [_VP]),
@@ -182,6 +190,69 @@ def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None, traffi
                        "frac": ops / (ms * 1e-3) / fma, "ops_per_launch": ops,
                        "peak_source": "measured (impec_measure_fp64: DFMA lanes per second)"}
     return out
+
+
+class Net:
+    """Learned warm start: the convolutional encoder-decoder of the tensor-core kernels."""
+
+    def __init__(self, seed: int = 0):
+        h = C.c_void_p()
+        _chk(lib().impec_net_create(seed, C.byref(h)), "net_create")
+        self.h = h
+
+    @staticmethod
+    def _ptr(t):
+        return C.c_void_p(t.data_ptr())
+
+    def train_batch(self, X, T, lr=3e-4, weight_decay=1e-4) -> float:
+        B, H, W, _ = X.shape
+        loss = C.c_double()
+        _chk(lib().impec_net_train_batch(self.h, self._ptr(X), self._ptr(T), B, H, W, lr, weight_decay,
+                                          C.byref(loss), None), "net_train_batch")
+        return loss.value
+
+    def backprop(self, X, T) -> float:
+        B, H, W, _ = X.shape
+        loss = C.c_double()
+        _chk(lib().impec_net_backprop(self.h, self._ptr(X), self._ptr(T), B, H, W, C.byref(loss), None),
+             "net_backprop")
+        return loss.value
+
+    def forward(self, X):
+        import torch
+        B, H, W, _ = X.shape
+        out = torch.empty((B, H, W), dtype=torch.float32, device=X.device)
+        _chk(lib().impec_net_forward(self.h, self._ptr(X), B, H, W, self._ptr(out), None), "net_forward")
+        return out
+
+    def parameters(self, which: int = 0):
+        import numpy as np
+        n = C.c_size_t()
+        _chk(lib().impec_net_parameters(self.h, None, None, C.byref(n), which), "net_parameters")
+        a = np.empty(n.value, dtype=np.float32)
+        _chk(lib().impec_net_parameters(self.h, a.ctypes.data_as(C.c_void_p), None, C.byref(n), which),
+             "net_parameters")
+        return a
+
+    def set_parameters(self, a):
+        import numpy as np
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        n = C.c_size_t()
+        _chk(lib().impec_net_parameters(self.h, None, a.ctypes.data_as(C.c_void_p), C.byref(n), 0),
+             "net_parameters")
+
+    def features(self, ctx, X) -> float:
+        s = C.c_double()
+        _chk(lib().impec_net_features(ctx.h, self.h, self._ptr(X), C.byref(s)), "net_features")
+        return s.value
+
+    def warm_start(self, ctx, workspace):
+        _chk(lib().impec_net_warm_start(ctx.h, self.h, self._ptr(workspace)), "net_warm_start")
+
+    def close(self):
+        if self.h:
+            lib().impec_net_destroy(self.h)
+            self.h = None
 
 
 class Ensemble:

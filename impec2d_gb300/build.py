@@ -19,7 +19,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libimpec2d.so")
 CLI = os.path.join(HERE, "Impec2D")
 
-CU_SOURCES = ["ctx.cu", "pressure.cu", "transport.cu", "dispersion.cu", "step.cu", "graph.cu", "project.cu", "learned.cu"]
+CU_SOURCES = ["ctx.cu", "pressure.cu", "transport.cu", "dispersion.cu", "step.cu", "graph.cu", "project.cu", "learned.cu", "learned_net.cu"]
 CPP_SOURCES = ["host/SimParams.cpp", "host/Impec2DSolver.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]

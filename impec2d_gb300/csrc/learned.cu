@@ -13,7 +13,7 @@
 #include <cstdint>
 #include <string>
 
-#include "internal.cuh"
+#include "learned.cuh"
 #include "umma.cuh"
 
 namespace impec {
@@ -110,20 +110,6 @@ __global__ void __launch_bounds__(GB_THREADS) k_gemm_bf16_tn(int M, int N, int K
 // weights rearranged by k_conv_wt_transpose).  Epilogue per (pixel, channel):
 //   v = acc + bias;  then either  Z = v, Y = act(v) (+ skip)          (forward)
 //                    or           Y = (v + add) * gelu'(gz)            (input gradient)
-struct ConvArgs {
-    const __nv_bfloat16* X;  // input activations [B][H][W][cin]
-    const __nv_bfloat16* W;  // weights [cout_rows][Kp]
-    const float* bias;       // [cout] or null
-    __nv_bfloat16* Z;        // pre-activation output or null
-    __nv_bfloat16* Y;        // output (activation, or gradient) or null
-    float* Yf;               // fp32 output or null
-    const __nv_bfloat16* skip;  // added after the activation, or null
-    const __nv_bfloat16* add;   // gradient mode: added before the gelu' factor, or null
-    const __nv_bfloat16* gz;    // gradient mode: pre-activation of the layer whose gradient this is
-    __nv_bfloat16* R;           // gradient mode: the raw gradient (acc) as well, or null
-    int B, H, W_, cin, cout, Kp, tapsign, act;
-    int* err;
-};
 
 __device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad(float x) {
@@ -351,7 +337,11 @@ __global__ void __launch_bounds__(GB_THREADS) k_conv_wgrad(const __nv_bfloat16* 
     if (warp == 0) umma::tmem_free(tmem, GB_TMEM_COLS);
 }
 
-static int* device_error_flag() {
+void launch_wt_transpose(const __nv_bfloat16* W, int cin, int cout, __nv_bfloat16* Wd, cudaStream_t s) {
+    k_conv_wt_transpose<<<128, 256, 0, s>>>(W, cin, cout, conv_kp(cin), Wd, conv_kp(cout));
+}
+
+int* device_error_flag() {
     static int* flag = nullptr;
     if (!flag) {
         if (cudaMalloc((void**)&flag, sizeof(int)) != cudaSuccess) return nullptr;
@@ -375,7 +365,7 @@ impec_status gemm_bf16_tn(int M, int N, int K, const void* A, int lda, const voi
     return IMPEC_OK;
 }
 
-static int conv_kp(int cin) { return (9 * cin + GB_K - 1) / GB_K * GB_K; }
+int conv_kp(int cin) { return (9 * cin + GB_K - 1) / GB_K * GB_K; }
 
 template <int BN>
 static impec_status launch_conv_bn(const ConvArgs& a, cudaStream_t s) {
@@ -419,7 +409,7 @@ impec_status launch_wgrad(const __nv_bfloat16* dZ, const __nv_bfloat16* X, int B
     return IMPEC_OK;
 }
 
-static impec_status check_err(int* err, cudaStream_t s, const char* what) {
+impec_status check_err(int* err, cudaStream_t s, const char* what) {
     int h = 0;
     IMPEC_CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     IMPEC_CUDA_TRY(cudaStreamSynchronize(s));

@@ -214,6 +214,32 @@ impec_status impec_conv3x3_input_grad(const void* dZ, int B, int H, int W, int c
 impec_status impec_conv3x3_weight_grad(const void* dZ, const void* X, int B, int H, int W, int cin, int cout, float* dW,
                                        void* stream);
 
+/* Learned warm start (no counterpart in the reference): a 4-level convolutional encoder-decoder
+ * (15 3x3 convolutions, 32..256 channels, GELU, additive skips; BF16 weights and activations,
+ * fp32 accumulation on the tensor cores, fp32 AdamW master weights) that predicts the pressure
+ * of the next solve from [log mobility ratio, log K, well rate, previous pressure / RMS].
+ * Features X are [B][H][W][8] bf16 (channels 4..7 zero), targets T and predictions [B][H][W]
+ * fp32 in units of the previous pressure's RMS; H and W multiples of 8. */
+typedef struct impec_net impec_net;
+impec_status impec_net_create(unsigned long long seed, impec_net** out);
+impec_status impec_net_destroy(impec_net* net);
+/* One AdamW step (lr, decoupled weight decay) on a batch; *loss = the batch's mean squared error. */
+impec_status impec_net_train_batch(impec_net* net, const void* X, const float* T, int B, int H, int W, double lr,
+                                   double weight_decay, double* loss, void* stream);
+/* Forward and backward only: the parameter gradients are left for impec_net_parameters(which = 1). */
+impec_status impec_net_backprop(impec_net* net, const void* X, const float* T, int B, int H, int W, double* loss,
+                                void* stream);
+impec_status impec_net_forward(impec_net* net, const void* X, int B, int H, int W, float* out, void* stream);
+/* *count = number of parameters; which 0: weights (host_out receives, host_in replaces),
+ * which 1: gradients (host_out receives).  Order: per layer, weights [cout][Kp] then bias. */
+impec_status impec_net_parameters(impec_net* net, float* host_out, const float* host_in, size_t* count, int which);
+/* Features of the context's resident state (its p is the previous pressure) into X [N1][N2][8];
+ * *scale = RMS of p. */
+impec_status impec_net_features(impec_ctx* ctx, impec_net* net, void* X, double* scale);
+/* p := RMS(p) * prediction: the initial guess of the next pressure solve (with warm_start set).
+ * workspace: N1*N2*8 bf16 on the device. */
+impec_status impec_net_warm_start(impec_ctx* ctx, impec_net* net, void* workspace);
+
 /* FP64 fused multiply-adds per second that the current device sustains (eight independent
  * chains per thread on every SM): the denominator of the FP64-pipe fractions reported beside
  * the HBM roofline.  No counterpart in the reference. */

@@ -105,3 +105,77 @@ def test_conv3x3_forward_and_gradients(engine, B, H, W, cin, cout):
         F.conv2d(X.float().permute(0, 3, 1, 2), w4.requires_grad_(True), None, padding=1),
         w4, dZ.float().permute(0, 3, 1, 2))[0].permute(0, 2, 3, 1).reshape(cout, 9 * cin)
     assert (dW - dw_ref).abs().max().item() <= 2e-5 * dw_ref.abs().max().item() + 1e-5
+
+
+def test_net_gradients_match_the_cpu_oracle(engine):
+    """Forward + backward of the whole encoder-decoder on the tensor cores against the CPU
+    restatement (oracle/learned_ref.py, bf16 rounding where the GPU stores bf16): loss and every
+    layer's weight and bias gradients."""
+    import numpy as np
+    import torch
+    from oracle import learned_ref as R
+    E = engine
+    net = E.Net(seed=3)
+    H = W = 16
+    g = torch.Generator(device="cuda").manual_seed(5)
+    X = torch.zeros((1, H, W, 8), device="cuda")
+    X[..., :4] = torch.randn((1, H, W, 4), generator=g, device="cuda")
+    X = X.to(torch.bfloat16)
+    T = torch.randn((1, H, W), generator=g, device="cuda")
+    loss = net.backprop(X, T)
+    grads = net.parameters(which=1)
+    params = net.parameters(which=0)
+    loss_ref, grads_ref = R.forward_backward(params, X[0].float().cpu().numpy(), T[0].cpu().numpy())
+    assert abs(loss - loss_ref) <= 1e-3 * abs(loss_ref)
+    off = 0
+    for l, (cin, cout, *_) in enumerate(R.LAYERS):
+        n = cout * R.kp(cin) + cout
+        a, b = grads[off:off + n], grads_ref[off:off + n]
+        assert np.linalg.norm(a - b) <= 3e-2 * np.linalg.norm(b) + 1e-12, (l, np.linalg.norm(a - b), np.linalg.norm(b))
+        off += n
+    net.close()
+
+
+def test_net_training_reduces_the_loss(engine):
+    """AdamW steps on a fixed batch drive its loss down (the target is a smooth function of the
+    input channels)."""
+    import torch
+    E = engine
+    net = E.Net(seed=1)
+    B, H, W = 4, 32, 32
+    g = torch.Generator(device="cuda").manual_seed(9)
+    X = torch.zeros((B, H, W, 8), device="cuda")
+    X[..., :4] = torch.randn((B, H, W, 4), generator=g, device="cuda")
+    T = (0.5 * X[..., 3] + 0.25 * torch.tanh(X[..., 0])).contiguous()
+    X = X.to(torch.bfloat16)
+    first = net.train_batch(X, T, lr=1e-3)
+    for _ in range(60):
+        last = net.train_batch(X, T, lr=1e-3)
+    assert last < 0.2 * first
+    out = net.forward(X)
+    assert torch.isfinite(out).all()
+    net.close()
+
+
+def test_net_warm_start_keeps_the_solve_converging(engine):
+    """The learned guess (untrained here) is only an initial iterate: the solve from it reaches
+    the same tolerance."""
+    import numpy as np
+    import torch
+    from helpers import cell_ghost, oparams, source
+    E = engine
+    N = 64
+    P = E.default_params(N, N, stype=1, warm_start=1, eps=1e-10)
+    ctx = E.Context(P)
+    OP = oparams(P)
+    ctx.upload(cell_ghost(OP, np.zeros((N, N))), source(OP), ghost=2)
+    ctx.set_time(0.0)
+    ctx.step()  # p now holds a solved pressure
+    net = E.Net(seed=2)
+    ws = torch.empty((N, N, 8), dtype=torch.bfloat16, device="cuda")
+    X = torch.empty((1, N, N, 8), dtype=torch.bfloat16, device="cuda")
+    assert net.features(ctx, X) > 0
+    net.warm_start(ctx, ws)
+    info = ctx.step()
+    assert info.relres <= 1e-10 and info.its < 200
+    net.close()

@@ -229,3 +229,32 @@ def test_parallel_projection_uses_the_mirror_symmetry(oracle_lib):
     out = _project(oracle_lib, P, smooth_field(N, N, 5), dN, dN)
     d = np.abs(out - out.T)
     assert (d > 1e-12).mean() < 0.02 and d.max() < 1e-2
+
+
+def test_learned_reference_gradients_match_finite_differences():
+    """The CPU restatement of the warm-start network (float64, no bf16 rounding): its analytic
+    gradients against central differences of its own loss, for weights and biases of every
+    kind of layer (plain, pooled input, upsampled input, skip source, output)."""
+    from oracle import learned_ref as R
+    rng = np.random.default_rng(4)
+    n = sum(c * R.kp(a) + c for a, c, *_ in R.LAYERS)
+    p = rng.standard_normal(n) * 0.1
+    offs, off = [], 0
+    for cin, cout, *_ in R.LAYERS:
+        offs.append((off, cout * R.kp(cin), cout, 9 * cin))
+        off += cout * R.kp(cin) + cout
+    H = W = 8
+    X = np.zeros((H, W, 8))
+    X[..., :4] = rng.standard_normal((H, W, 4))
+    T = rng.standard_normal((H, W))
+    _, g = R.forward_backward(p, X, T, exact=True)
+    h = 1e-5
+    for l in (0, 1, 2, 5, 7, 8, 12, 14):
+        o, nw, cout, k9 = offs[l]
+        for idx in (o + int(rng.integers(0, cout)) * (nw // cout) + int(rng.integers(0, k9)),
+                    o + nw + int(rng.integers(0, cout))):
+            pp, pm = p.copy(), p.copy()
+            pp[idx] += h
+            pm[idx] -= h
+            fd = (R.forward_backward(pp, X, T, exact=True)[0] - R.forward_backward(pm, X, T, exact=True)[0]) / (2 * h)
+            assert abs(fd - g[idx]) <= 1e-6 * max(1.0, abs(fd)) + 1e-4 * abs(fd), (l, idx, fd, g[idx])
