@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch each kernel on the stream instead of replaying the step graph (for ncu)")
-    ap.add_argument("--study", default=None, choices=["pressure", "warmstart", "ensemble"],
+    ap.add_argument("--study", default=None, choices=["pressure", "warmstart", "ensemble", "learned", "network"],
                     help="pressure: FP64 vs mixed-precision solves on re-seeded heterogeneous fields; "
                          "warmstart: V-cycles and ms per solve along the IMPES run for zero and previous-step "
                          "initial guesses")
@@ -53,6 +53,18 @@ def parse():
     ap.add_argument("--members-per-size", type=int, default=64,
                     help="ensemble study: realisations at each of 128^2, 256^2, 384^2, 512^2")
     ap.add_argument("--no-autotune", action="store_true", help="ensemble study: keep the default schedules")
+    ap.add_argument("--quick", action="store_true", help="network study: two shapes, few repetitions (profiling)")
+    ap.add_argument("--members", type=int, default=100, help="learned study: 256^2 realisations for training pairs")
+    ap.add_argument("--pairs-per-member", type=int, default=200, help="learned study: pairs per realisation")
+    ap.add_argument("--epochs", type=float, default=2.0, help="learned study: training epochs")
+    ap.add_argument("--seed", type=int, default=7, help="learned study: network initialisation seed")
+    ap.add_argument("--net-in", default=None, help="learned study: load trained weights (.npy) instead of training")
+    ap.add_argument("--net-out", default=None, help="learned study: save the trained weights (.npy)")
+    ap.add_argument("--eval-sizes", default="512,1024", help="learned study: evaluation grid sides")
+    ap.add_argument("--eval-seeds", type=int, default=4, help="learned study: held-out realisations per size")
+    ap.add_argument("--eval-samples", type=int, default=8, help="learned study: timed solves per realisation")
+    ap.add_argument("--eval-skip", type=int, default=20, help="learned study: IMPES steps before the first solve")
+    ap.add_argument("--eval-every", type=int, default=10, help="learned study: IMPES steps between solves")
     return ap.parse_args()
 
 
@@ -174,16 +186,8 @@ def run_reference(args):
 
 
 def grf(N, ell, seed):
-    """Seeded Gaussian random field on the GPU: white noise (Philox, seeded) filtered in Fourier
-    space to the covariance exp(-r^2 / ell^2) (ell in cells, periodic), zero mean, unit variance."""
-    import torch
-    g = torch.Generator(device="cuda")
-    g.manual_seed(seed)
-    w = torch.randn((N, N), generator=g, device="cuda", dtype=torch.float64)
-    f = torch.fft.fftfreq(N, device="cuda", dtype=torch.float64)
-    H = torch.exp(-(math.pi * ell) ** 2 * (f[:, None] ** 2 + f[None, :] ** 2) / 2)
-    x = torch.fft.ifft2(torch.fft.fft2(w) * H).real
-    return ((x - x.mean()) / x.std()).contiguous()
+    from impec2d_gb300.workloads import grf as _grf
+    return _grf(N, ell, seed)
 
 
 def study_pressure(args):
@@ -278,33 +282,11 @@ def study_warmstart(args):
 
 
 def ensemble_member(E, N, seed, precision="mixed"):
-    """One realisation of the batched-ensemble workload: lognormal K (sigma 0.5, correlation
-    16 cells), M from {5, 20, 41, 100} and diagonal or parallel orientation chosen by the seed,
-    MUSCL + Peaceman dispersion (alpha_l 1e-3, alpha_t 1e-4), FP64 transport and
-    mixed-precision pressure."""
-    import numpy as np
-    import torch
-    M = (5.0, 20.0, 41.0, 100.0)[seed % 4]
-    parallel = (seed // 4) % 2 == 1
-    L = math.sqrt(2.0) if parallel else 1.0
-    P = E.default_params(N, N, x_ub=L, y_ub=L, stype=E.PARALLEL if parallel else E.DIAGONAL, hmtype=E.MUSCL,
-                         nu=1.0, diffusion=1, alpha_l=1e-3, alpha_t=1e-4, cfl=0.5, porosity=1.0, eps=1e-10,
-                         para_eps=1e-10, mu_res=M, mu_inj=1.0, max_cycles=200,
-                         precision=E.PREC_MIXED if precision == "mixed" else E.PREC_FP64)
-    ctx = E.Context(P)
-    dx = L / N
-    qv = 1.0 / (dx * dx)
-    q = np.zeros(N * N)
-    q[0] = qv
-    if parallel:
-        q[-1], q[N - 1], q[(N - 1) * N] = qv, -qv, -qv
-    else:
-        q[-1] = -qv
-    K = torch.exp(0.5 * grf(N, 16.0, 5000 + seed)).contiguous()
-    ctx.upload(np.zeros((N + 4, N + 4)), q, ghost=2)
-    ctx.set_permeability(K, K)
-    ctx.set_time(0.0)
-    return ctx
+    """One realisation of the batched-ensemble workload (lognormal K with sigma 0.5 and
+    correlation 16 cells, M from {5, 20, 41, 100}, diagonal or parallel by seed, MUSCL +
+    Peaceman, FP64 transport, pressure in the given precision)."""
+    from impec2d_gb300.workloads import realisation
+    return realisation(E, N, seed, precision=precision)
 
 
 def study_ensemble(args):
@@ -369,6 +351,179 @@ def study_ensemble(args):
         c.close()
 
 
+NET_LAYERS = [(8, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2), (128, 256, 3),
+              (256, 256, 3), (256, 128, 2), (128, 128, 2), (128, 64, 1), (64, 64, 1), (64, 32, 0), (32, 32, 0),
+              (32, 8, 0)]  # (cin, cout, level) of the warm-start network
+
+
+def net_flops(B, H, W):
+    """Dense 3x3-convolution FLOPs of one forward pass (2 * 9 * cin * cout per output pixel)."""
+    return sum(2 * 9 * ci * co * B * (H >> lv) * (W >> lv) for ci, co, lv in NET_LAYERS)
+
+
+def study_network(args):
+    """Tensor-core throughput of the warm-start network's own kernels: forward passes at the
+    inference shapes (one 256^2 / 512^2 map) and the training batch (64 x 256^2), and AdamW
+    training steps (forward + input and weight gradients = 3x the forward FLOPs), against the
+    measured dense BF16 peak.  CUDA events around `reps` back-to-back calls."""
+    import torch
+
+    import impec2d_gb300 as E
+    from impec2d_gb300 import build as B
+    B.build()
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    peak = peaks.get("bf16_tflops", 1900.0)
+    net = E.Net(seed=1)
+    out = {"study": "network", "peak_bf16_tflops": peak,
+           "peak_source": "measured" if "bf16_tflops" in peaks else "fallback", "data": "synthetic (random maps)"}
+    reps = 3 if args.quick else 20
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    shapes = [(1, 256), (64, 256)] if args.quick else [(1, 128), (1, 256), (1, 512), (8, 256), (64, 256)]
+    for Bn, H in shapes:
+        X = torch.randn((Bn, H, H, 8), generator=g, device="cuda").to(torch.bfloat16)
+        for _ in range(2):
+            net.forward(X)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            net.forward(X)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        tf = net_flops(Bn, H, H) / ms / 1e9
+        out[f"forward_{Bn}x{H}x{H}"] = {"ms": ms, "tflops": tf, "frac": tf / peak}
+    for Bn, H in [(64, 256)]:
+        X = torch.randn((Bn, H, H, 8), generator=g, device="cuda").to(torch.bfloat16)
+        T = torch.randn((Bn, H, H), generator=g, device="cuda")
+        net.train_batch(X, T, lr=1e-6)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(max(2, reps // 4)):
+            net.train_batch(X, T, lr=1e-6)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / max(2, reps // 4)
+        tf = 3 * net_flops(Bn, H, H) / ms / 1e9
+        out[f"train_step_{Bn}x{H}x{H}"] = {"ms": ms, "tflops": tf, "frac": tf / peak}
+    print(json.dumps(out))
+    net.close()
+
+
+def study_learned(args):
+    """Learned warm start (the heterogeneous batched-ensemble family): training pairs written
+    by the solver from 256^2 realisations, AdamW training (lr 3e-4, batch 64) with the
+    engine's tensor-core kernels, then pressure solves to 1e-10 along held-out 512^2 and
+    1024^2 runs, started from zero, from the previous pressure, and from the previous pressure
+    moved by the network's prediction, in FP64 and mixed precision.  Reports V-cycles and ms per
+    solve (CUDA events around the captured solve)."""
+    import numpy as np
+    import torch
+
+    import impec2d_gb300 as E
+    from impec2d_gb300 import build as B
+    from impec2d_gb300 import learned as LW
+    from impec2d_gb300.workloads import device_view, realisation
+    B.build()
+
+    def log(m):
+        print(m, file=sys.stderr, flush=True)
+    out = {"study": "learned", "data": "synthetic (seeded lognormal-K realisations; pairs written by the GPU solver)"}
+    net = E.Net(seed=args.seed)
+    if args.net_in:
+        net.set_parameters(np.load(args.net_in))
+        out["net"] = {"loaded": os.path.basename(args.net_in)}
+    else:
+        X, T, t_gen = LW.generate_pairs(E, args.members, args.pairs_per_member, N=256, every=2, skip=2, log=log)
+        nval = args.pairs_per_member * max(1, args.members // 20)  # whole realisations held out
+        Xva, Tva, Xtr, Ttr = X[:nval], T[:nval], X[nval:], T[nval:]
+        v0 = LW.validation_mse(net, Xva, Tva)
+        hist, t_train = LW.train(net, Xtr, Ttr, epochs=args.epochs, batch=64, lr=3e-4, weight_decay=1e-4,
+                                 Xval=Xva, Tval=Tva, log=log)
+        out["training"] = {"pairs": int(X.shape[0]), "train_pairs": int(Xtr.shape[0]), "validation_pairs": nval,
+                           "grid": "256x256", "generation_s": t_gen, "epochs": args.epochs, "batch": 64, "lr": 3e-4,
+                           "steps": hist[-1][0], "train_s": t_train, "ms_per_train_step": 1e3 * t_train / hist[-1][0],
+                           "validation_mse_untrained": v0, "history": hist}
+        if args.net_out:
+            np.save(args.net_out, net.parameters())
+        del X, T, Xva, Tva, Xtr, Ttr
+        torch.cuda.empty_cache()
+    modes = [("fp64", "zero"), ("fp64", "previous"), ("mixed", "zero"), ("mixed", "previous"), ("mixed", "learned"),
+             ("fp64", "learned")]
+    evals = {}
+    for N in [int(x) for x in args.eval_sizes.split(",")]:
+        factor = max(1, N // 256)
+        ell = 16.0 * N / 256
+        res = {f"{p}/{g}": {"cycles": [], "ms": [], "alpha": [], "relres0": []} for p, g in modes}
+        for si in range(args.eval_seeds):
+            seed = 10000 + si
+            drv = realisation(E, N, seed, "mixed", ell=ell, warm_start=1)
+            ctxs = {}
+            for p, g in modes:
+                cx = realisation(E, N, seed, p, ell=ell, warm_start=0 if g == "zero" else 1)
+                if g == "learned":
+                    net.attach(cx, factor=factor, mode=1)
+                ctxs[f"{p}/{g}"] = cx
+            drv.run_steps(args.eval_skip)
+            cd, pd = [device_view(x, (N, N)) for x in drv.state_ptrs()[:2]]
+            for k in range(args.eval_samples + 1):
+                drv.run_steps(args.eval_every)
+                torch.cuda.synchronize()
+                for name, cx in ctxs.items():
+                    cc, pc = [device_view(x, (N, N)) for x in cx.state_ptrs()[:2]]
+                    cc.copy_(cd)
+                    pc.copy_(pd)
+                    torch.cuda.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    cx.pressure_solve_resident(sync=False)
+                    e1.record()
+                    e1.synchronize()
+                    cyc, rr, rr0 = cx.last_solve()
+                    assert rr <= 1e-10, (name, rr)
+                    if k == 0:
+                        continue  # the first solve captures the graph
+                    res[name]["cycles"].append(cyc)
+                    res[name]["relres0"].append(rr0)
+                    res[name]["ms"].append(e0.elapsed_time(e1))
+                    if name.endswith("learned"):
+                        res[name]["alpha"].append(E.Net.last_alpha(cx))
+            for name, cx in ctxs.items():
+                if name.endswith("learned"):
+                    E.Net.detach(cx)
+                cx.close()
+            drv.close()
+        ev = {"net_grid": f"{N // factor}x{N // factor}", "feature_factor": factor, "seeds": args.eval_seeds,
+              "solves_per_seed": args.eval_samples, "permeability_correlation_cells": ell}
+        for name, r in res.items():
+            ev[name] = {"cycles_mean": statistics.mean(r["cycles"]), "ms_per_solve_median": statistics.median(r["ms"]),
+                        "ms_per_solve_mean": statistics.mean(r["ms"]),
+                        "initial_relres_median": statistics.median(r["relres0"])}
+            if r["alpha"]:
+                ev[name]["alpha_median"] = statistics.median(r["alpha"])
+        for p in ("fp64", "mixed"):
+            L_, Pv, Z = ev[f"{p}/learned"], ev[f"{p}/previous"], ev[f"{p}/zero"]
+            ev[f"{p}_learned_saves"] = {
+                "cycles_vs_previous": Pv["cycles_mean"] - L_["cycles_mean"],
+                "cycles_vs_zero": Z["cycles_mean"] - L_["cycles_mean"],
+                "ms_vs_previous": Pv["ms_per_solve_median"] - L_["ms_per_solve_median"],
+                "ms_vs_zero": Z["ms_per_solve_median"] - L_["ms_per_solve_median"]}
+        ev["mixed_learned_vs_fp64_zero_speedup"] = (ev["fp64/zero"]["ms_per_solve_median"]
+                                                    / ev["mixed/learned"]["ms_per_solve_median"])
+        evals[f"{N}x{N}"] = ev
+        log(json.dumps({f"{N}x{N}": ev}))
+    out["evaluation"] = evals
+    print(json.dumps(out))
+    net.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -379,6 +534,10 @@ def main():
         return study_warmstart(args)
     if args.study == "ensemble":
         return study_ensemble(args)
+    if args.study == "learned":
+        return study_learned(args)
+    if args.study == "network":
+        return study_network(args)
     if args.no_graph:
         os.environ["IMPEC_NO_GRAPH"] = "1"  # read by the engine at each step
     import numpy as np

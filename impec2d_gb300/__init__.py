@@ -118,8 +118,11 @@ _SIGS = {
     "impec_net_backprop": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, _PD, _VP]),
     "impec_net_forward": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "impec_net_parameters": (C.c_int, [_VP, _VP, _VP, C.POINTER(C.c_size_t), C.c_int]),
-    "impec_net_features": (C.c_int, [_VP, _VP, _VP, _PD]),
-    "impec_net_warm_start": (C.c_int, [_VP, _VP, _VP]),
+    "impec_last_solve": (C.c_int, [_VP, C.POINTER(C.c_int), _PD, _PD]),
+    "impec_learned_attach": (C.c_int, [_VP, _VP, C.c_int, C.c_int]),
+    "impec_learned_features": (C.c_int, [_VP, _VP]),
+    "impec_learned_target": (C.c_int, [_VP, _VP]),
+    "impec_learned_alpha": (C.c_int, [_VP, _PD]),
     "impec_ensemble_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "impec_ensemble_step": (C.c_int, [_VP, C.c_int, C.c_int]),
     "impec_ensemble_destroy": (C.c_int, [_VP]),
@@ -241,17 +244,32 @@ class Net:
         _chk(lib().impec_net_parameters(self.h, None, a.ctypes.data_as(C.c_void_p), C.byref(n), 0),
              "net_parameters")
 
-    def features(self, ctx, X) -> float:
-        s = C.c_double()
-        _chk(lib().impec_net_features(ctx.h, self.h, self._ptr(X), C.byref(s)), "net_features")
-        return s.value
+    def attach(self, ctx, factor: int = 1, mode: int = 1):
+        """Use this network as the initial guess of ctx's pressure solves (mode 1), or only
+        record their features and targets (mode 2)."""
+        _chk(lib().impec_learned_attach(ctx.h, self.h, factor, mode), "learned_attach")
 
-    def warm_start(self, ctx, workspace):
-        _chk(lib().impec_net_warm_start(ctx.h, self.h, self._ptr(workspace)), "net_warm_start")
+    @staticmethod
+    def detach(ctx):
+        _chk(lib().impec_learned_attach(ctx.h, None, 1, 0), "learned_attach")
+
+    @staticmethod
+    def last_features(ctx, X):
+        _chk(lib().impec_learned_features(ctx.h, C.c_void_p(X.data_ptr())), "learned_features")
+
+    @staticmethod
+    def last_target(ctx, T):
+        _chk(lib().impec_learned_target(ctx.h, C.c_void_p(T.data_ptr())), "learned_target")
+
+    @staticmethod
+    def last_alpha(ctx) -> float:
+        a = C.c_double()
+        _chk(lib().impec_learned_alpha(ctx.h, C.byref(a)), "learned_alpha")
+        return a.value
 
     def close(self):
         if self.h:
-            lib().impec_net_destroy(self.h)
+            _chk(lib().impec_net_destroy(self.h), "net_destroy")
             self.h = None
 
 
@@ -455,6 +473,12 @@ class Context:
         _chk(lib().impec_pressure_solve_resident(self.h, 1 if sync else 0, C.byref(cyc), C.byref(rr)),
              "pressure_solve_resident")
         return cyc.value, rr.value
+
+    def last_solve(self):
+        """(cycles, relres, initial relres) of the last pressure solve."""
+        cyc, rr, r0 = C.c_int(), C.c_double(), C.c_double()
+        _chk(lib().impec_last_solve(self.h, C.byref(cyc), C.byref(rr), C.byref(r0)), "last_solve")
+        return cyc.value, rr.value, r0.value
 
     def set_time(self, t0: float):
         _chk(lib().impec_set_time(self.h, t0), "set_time")

@@ -212,6 +212,7 @@ impec_status impec_ctx_destroy(impec_ctx* ctx) {
     if (!ctx) return IMPEC_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream); else cudaDeviceSynchronize();
     invalidate_step_graph(ctx);
+    learned_release(ctx);
     if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
     if (ctx->body_stream) cudaStreamDestroy(ctx->body_stream);
     pressure_free(ctx);

@@ -109,6 +109,7 @@ struct DevScalars {
     double relres, cn_relres, t_clip;
     double pcg_rz, pcg_zq;  // (r, z) and (z, q_old) of the current CG iteration (written as a pair)
     double pcg_pq, pcg_alpha, pcg_rz_old;
+    double relres0;  // relative residual of the initial iterate of the last pressure solve
     int mg_cycles, cn_cycles, cn_cycles_total, flags, go, clipped, steps;
     long long graph_launches;  // kernels executed by step-graph replays
 };
@@ -117,6 +118,8 @@ struct DevScalars {
 
 namespace impec {
 // Engine tunables of one context (defaults from the IMPEC_MG_* environment at creation).
+struct LearnedHook;  // learned_net.cu
+
 struct Tuning {
     long pre = 2, post = 2;        // smoother sweeps before / after the coarse correction
     long cluster = 1;              // coarse levels in one thread-block-cluster launch
@@ -188,6 +191,10 @@ struct impec_ctx {
     cudaGraphExec_t pressure_exec = nullptr;
     long long pressure_outer_launches = 0;
     long long step_outer_launches = 0, step_mg_body_launches = 0, step_cn_body_launches = 0;
+    // learned initial guess (learned_net.cu): the attached network's state, and the residual of
+    // the previous pressure, the predicted direction, its image under A and the step length
+    impec::LearnedHook* learned = nullptr;
+    double *lrn_r0 = nullptr, *lrn_d = nullptr, *lrn_Ad = nullptr, *lrn_alpha = nullptr;
 };
 
 namespace impec {
@@ -220,6 +227,10 @@ impec_status cn_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalH
 impec_status cn_iteration(impec_ctx* ctx, double* c);
 impec_status dispersion_cn_dev(impec_ctx* ctx, double* c, const double* u, const double* v, double dt_scale,
                                const double* dt_dev, double tol, int* its, double* relres);
+// learned_net.cu
+bool learned_predicts(const impec_ctx* ctx);
+impec_status learned_predict(impec_ctx* ctx, const double* x, const double* r0, double* d);
+void learned_release(impec_ctx* ctx);
 // graph.cu
 impec_status launch_step_graph(impec_ctx* ctx, double t_clip);
 impec_status launch_pressure_graph(impec_ctx* ctx);

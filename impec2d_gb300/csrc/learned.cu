@@ -116,69 +116,110 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 
+// Pipelined over CV_STAGES shared-memory stages: while the tensor core works on stage k, the
+// copies of stages k+1 .. k+CV_STAGES-1 are in flight.  A stage's slot is refilled only after
+// the mbarrier of the MMAs that read it has completed.  Thread t always copies chunk t % 8 of
+// rows t / 8 + 16 i, so each thread resolves its pixels' coordinates once.
+constexpr int CV_STAGES = 4;
+
+template <int BN>
+constexpr int conv_smem_bytes() { return CV_STAGES * (GB_TILE_BYTES + BN * GB_K * 2) + 1024; }
+
 template <int BN>
 __global__ void __launch_bounds__(GB_THREADS) k_conv3x3(ConvArgs a) {
     extern __shared__ __align__(1024) unsigned char cv_smem[];
-    unsigned char* sA = cv_smem;
-    unsigned char* sB = cv_smem + GB_TILE_BYTES;
-    __shared__ uint64_t mbar;
+    constexpr int B_BYTES = BN * GB_K * 2, STAGE = GB_TILE_BYTES + B_BYTES;
+    constexpr int AR = GB_M * 8 / GB_THREADS, BR = BN * 8 / GB_THREADS;  // rows per thread (A: 8, B: BN / 16)
+    __shared__ uint64_t mbar[CV_STAGES];
     __shared__ uint32_t tslot;
     constexpr uint32_t TCOLS = BN < 32 ? 32 : BN;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, kg = tid & 7, r0 = tid >> 3;
     const int M = a.B * a.H * a.W_;
     const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * BN;
     if (warp == 0) umma::tmem_alloc(&tslot, TCOLS);
-    if (tid == 0) umma::mbar_init(&mbar, 1);
+    if (tid == 0)
+        for (int st = 0; st < CV_STAGES; ++st) umma::mbar_init(&mbar[st], 1);
     umma::fence_before();
     __syncthreads();
     umma::fence_after();
     const uint32_t tmem = tslot;
     const uint32_t idesc = umma::idesc_bf16_f32(GB_M, BN);
     const int nk = a.Kp / GB_K, K9 = 9 * a.cin;
-    bool ok = true;
+    // this thread's A rows: pixel index (or -1) and its y, x
+    int pix[AR], py[AR], px[AR];
+#pragma unroll
+    for (int i = 0; i < AR; ++i) {
+        const int m = m0 + r0 + 16 * i;
+        pix[i] = m < M ? m : -1;
+        const int mm = m < M ? m : 0;
+        px[i] = mm % a.W_;
+        py[i] = (mm / a.W_) % a.H;
+    }
+    auto load = [&](int kt, int slot) {
+        unsigned char* sA = cv_smem + slot * STAGE;
+        unsigned char* sB = sA + GB_TILE_BYTES;
+        const int k0 = kt * GB_K + kg * 8;
+        const bool kin = k0 < K9;
+        const int tap = kin ? k0 / a.cin : 0, ch = k0 - tap * a.cin;
+        const int dy = a.tapsign * (tap / 3 - 1), dx = a.tapsign * (tap % 3 - 1);
+        const long long shift = ((long long)dy * a.W_ + dx) * a.cin + ch;
+#pragma unroll
+        for (int i = 0; i < AR; ++i) {
+            const int yy = py[i] + dy, xx = px[i] + dx;
+            const bool in = kin && pix[i] >= 0 && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W_;
+            const __nv_bfloat16* src = in ? a.X + (long long)pix[i] * a.cin + shift : a.X;
+            umma::cp_async16(sA + tile_off(r0 + 16 * i, kg), src, in ? 16u : 0u);
+        }
+#pragma unroll
+        for (int i = 0; i < BR; ++i) {
+            const int n = n0 + r0 + 16 * i;
+            const bool in = n < a.cout;
+            umma::cp_async16(sB + tile_off(r0 + 16 * i, kg),
+                             in ? a.W + (size_t)n * a.Kp + (size_t)kt * GB_K + kg * 8 : a.W, in ? 16u : 0u);
+        }
+    };
+#pragma unroll
+    for (int st = 0; st < CV_STAGES - 1; ++st) {
+        if (st < nk) load(st, st);
+        umma::cp_async_commit();
+    }
+    bool ok = true, mine = true;
     int issued = 0;
     for (int kt = 0; kt < nk; ++kt) {
-        for (int c = tid; c < GB_M * 8; c += GB_THREADS) {  // A: 128 pixels x 8 chunks
-            const int r = c >> 3, kg = c & 7, m = m0 + r, k0 = kt * GB_K + kg * 8;
-            const __nv_bfloat16* src = a.X;
-            uint32_t bytes = 0;
-            if (m < M && k0 < K9) {
-                const int tap = k0 / a.cin, ch = k0 - tap * a.cin;
-                const int x = m % a.W_, t = m / a.W_, y = t % a.H, b = t / a.H;
-                const int yy = y + a.tapsign * (tap / 3 - 1), xx = x + a.tapsign * (tap % 3 - 1);
-                if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W_) {
-                    src = a.X + (((size_t)b * a.H + yy) * a.W_ + xx) * a.cin + ch;
-                    bytes = 16;
-                }
-            }
-            umma::cp_async16(sA + tile_off(r, kg), src, bytes);
-        }
-        for (int c = tid; c < BN * 8; c += GB_THREADS) {  // B: BN weight rows x 8 chunks
-            const int r = c >> 3, kg = c & 7, n = n0 + r;
-            const bool in = n < a.cout;
-            umma::cp_async16(sB + tile_off(r, kg), in ? a.W + (size_t)n * a.Kp + (size_t)kt * GB_K + kg * 8 : a.W,
-                             in ? 16u : 0u);
-        }
-        umma::cp_async_wait_all();
+        const int slot = kt % CV_STAGES;
+        umma::cp_async_wait_group<CV_STAGES - 2>();
         umma::fence_proxy_async();
-        __syncthreads();
+        ok = __syncthreads_and(mine) != 0;
+        if (!ok) break;
         if (tid == 0) {
             umma::fence_after();
+            const uint32_t base = umma::smem_u32(cv_smem + slot * STAGE);
 #pragma unroll
             for (int ks = 0; ks < GB_K / 16; ++ks) {
-                const uint64_t ad = umma::smem_desc(umma::smem_u32(sA) + ks * 256, 128, 1024);
-                const uint64_t bd = umma::smem_desc(umma::smem_u32(sB) + ks * 256, 128, 1024);
+                const uint64_t ad = umma::smem_desc(base + ks * 256, 128, 1024);
+                const uint64_t bd = umma::smem_desc(base + GB_TILE_BYTES + ks * 256, 128, 1024);
                 umma::mma_bf16(tmem, ad, bd, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
             }
-            umma::commit(&mbar);
+            umma::commit(&mbar[slot]);
         }
         issued = kt + 1;
-        const bool done = umma::mbar_wait(&mbar, (uint32_t)(kt & 1), GB_WAIT_TRIES);
-        ok = __syncthreads_and(done) != 0;
-        if (!ok) break;
-        umma::fence_after();
+        const int nxt = kt + CV_STAGES - 1;
+        if (nxt < nk) {
+            // the slot of stage nxt was last read by the MMAs of stage kt - 1
+            if (kt >= 1) mine = umma::mbar_wait(&mbar[(kt - 1) % CV_STAGES], (uint32_t)(((kt - 1) / CV_STAGES) & 1), GB_WAIT_TRIES);
+            if (mine) load(nxt, nxt % CV_STAGES);
+        }
+        umma::cp_async_commit();
     }
     if (ok) {
+        const int last = nk - 1;
+        mine = umma::mbar_wait(&mbar[last % CV_STAGES], (uint32_t)((last / CV_STAGES) & 1), GB_WAIT_TRIES);
+        ok = __syncthreads_and(mine) != 0;
+        if (!ok) issued = 0;  // the wait above already gave up on the last group
+    }
+    umma::cp_async_wait_all();
+    if (ok) {
+        umma::fence_after();
         const int m = m0 + warp * 32 + lane;
 #pragma unroll 1
         for (int cb = 0; cb < (BN + 31) / 32; ++cb) {
@@ -186,9 +227,60 @@ __global__ void __launch_bounds__(GB_THREADS) k_conv3x3(ConvArgs a) {
             umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
             if (m >= M) continue;
             const size_t row = (size_t)m * a.cout;
+            const int nb = n0 + cb * 32;
+            if (nb + 32 <= a.cout && (a.cout & 7) == 0) {  // 32 whole channels: 16-byte accesses
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float z[8], y[8];
+                    const size_t o = row + nb + 8 * q;
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) z[k] = v[8 * q + k] + (a.bias ? a.bias[nb + 8 * q + k] : 0.0f);
+                    if (a.gz) {
+                        __align__(16) __nv_bfloat16 g8[8], ad8[8], o8[8];
+                        *reinterpret_cast<uint4*>(g8) = *reinterpret_cast<const uint4*>(a.gz + o);
+                        if (a.add) *reinterpret_cast<uint4*>(ad8) = *reinterpret_cast<const uint4*>(a.add + o);
+                        if (a.R) {
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) o8[k] = __float2bfloat16(z[k]);
+                            *reinterpret_cast<uint4*>(a.R + o) = *reinterpret_cast<const uint4*>(o8);
+                        }
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            float t = z[k];
+                            if (a.add) t += __bfloat162float(ad8[k]);
+                            y[k] = t * gelu_grad(__bfloat162float(g8[k]));
+                        }
+                    } else {
+                        if (a.Z) {
+                            __align__(16) __nv_bfloat16 o8[8];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) o8[k] = __float2bfloat16(z[k]);
+                            *reinterpret_cast<uint4*>(a.Z + o) = *reinterpret_cast<const uint4*>(o8);
+                        }
+                        __align__(16) __nv_bfloat16 s8[8];
+                        if (a.skip) *reinterpret_cast<uint4*>(s8) = *reinterpret_cast<const uint4*>(a.skip + o);
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            y[k] = a.act ? gelu_f(z[k]) : z[k];
+                            if (a.skip) y[k] += __bfloat162float(s8[k]);
+                        }
+                    }
+                    if (a.Y) {
+                        __align__(16) __nv_bfloat16 o8[8];
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) o8[k] = __float2bfloat16(y[k]);
+                        *reinterpret_cast<uint4*>(a.Y + o) = *reinterpret_cast<const uint4*>(o8);
+                    }
+                    if (a.Yf) {
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) a.Yf[o + k] = y[k];
+                    }
+                }
+                continue;
+            }
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
-                const int n = n0 + cb * 32 + k;
+                const int n = nb + k;
                 if (n >= a.cout || cb * 32 + k >= BN) continue;
                 float z = v[k] + (a.bias ? a.bias[n] : 0.0f);
                 if (a.gz) {  // input gradient: (acc + add) * gelu'(gz)
@@ -208,7 +300,10 @@ __global__ void __launch_bounds__(GB_THREADS) k_conv3x3(ConvArgs a) {
         }
     } else {
         if (tid == 0) atomicExch(a.err, 1);
-        umma::mbar_wait(&mbar, (uint32_t)((issued - 1) & 1), GB_WAIT_TRIES);
+        if (issued > 0) {
+            const int last = issued - 1;
+            umma::mbar_wait(&mbar[last % CV_STAGES], (uint32_t)((last / CV_STAGES) & 1), GB_WAIT_TRIES);
+        }
     }
     umma::fence_before();
     __syncthreads();
@@ -370,7 +465,7 @@ int conv_kp(int cin) { return (9 * cin + GB_K - 1) / GB_K * GB_K; }
 template <int BN>
 static impec_status launch_conv_bn(const ConvArgs& a, cudaStream_t s) {
     static bool attr = false;
-    const int smem = 2 * GB_TILE_BYTES + 1024;
+    const int smem = conv_smem_bytes<BN>();
     if (!attr) {
         IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_conv3x3<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr = true;
@@ -382,11 +477,20 @@ static impec_status launch_conv_bn(const ConvArgs& a, cudaStream_t s) {
     return IMPEC_OK;
 }
 
-// The output-channel tile: the smallest of 32, 64, 128 covering cout (128 beyond).
+// The output-channel tile: the widest of 128, 64, 32 (not beyond cout) that still gives one
+// CTA per SM; small layers take 32 for more CTAs.
 impec_status launch_conv(const ConvArgs& a, cudaStream_t s) {
-    if (a.cout <= 32) return launch_conv_bn<32>(a, s);
-    if (a.cout <= 64) return launch_conv_bn<64>(a, s);
-    return launch_conv_bn<128>(a, s);
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const long long mt = ((long long)a.B * a.H * a.W_ + GB_M - 1) / GB_M;
+    auto ctas = [&](int bn) { return mt * ((a.cout + bn - 1) / bn); };
+    if (a.cout >= 128 && ctas(128) >= sms) return launch_conv_bn<128>(a, s);
+    if (a.cout >= 64 && ctas(64) >= sms) return launch_conv_bn<64>(a, s);
+    return launch_conv_bn<32>(a, s);
 }
 
 impec_status launch_wgrad(const __nv_bfloat16* dZ, const __nv_bfloat16* X, int B, int H, int W_, int cin, int cout,

@@ -1,6 +1,6 @@
-// Learned pressure warm start: a 4-level convolutional encoder-decoder that predicts the
-// pressure of an IMPES step from [log mobility ratio, log permeability, well rate, previous
-// pressure], used only as the initial guess of the pressure solve (which still converges to
+// Learned pressure warm start: a 4-level convolutional encoder-decoder that predicts, from
+// the state at the start of a pressure solve, the error of the previous step's pressure as an
+// initial guess.  It is used only to move the initial iterate (the solve still converges to
 // its tolerance).  No counterpart in the reference.
 //
 // Layers (3x3 convolutions, GELU, BF16 weights and activations, fp32 accumulation on tcgen05):
@@ -14,6 +14,19 @@
 //   head:    14: 32 -> 8, linear; channel 0 is the prediction.
 // Skips add the encoder output after the decoder convolution's activation.  Training: MSE
 // loss, AdamW on fp32 master weights (the bf16 copies feed the tensor cores).
+//
+// Use inside the pressure solve (impec_learned_attach): with the operator of the new
+// mobility built and x0 = the previous pressure, the solve computes r0 = f - A x0, the
+// features below averaged over factor x factor cells, the network's prediction d (bilinear
+// back to the fine grid), and steps x0 += alpha d with alpha = (r0, d) / (d, A d), the step
+// that minimises the A-norm error along d.  Features per coarse cell:
+//   0: mean of 4 log(1 - c + M^(1/4) c)   (log of the mobility ratio to the resident fluid)
+//   1: mean of log K
+//   2: sum of q dA / I                    (+1 at the injector, -1 at a producer)
+//   3: mean of x0, centred and divided by its RMS over the coarse cells
+//   4: mean of r0, divided by its RMS over the coarse cells
+// The training target of a recorded solve is the mean over each coarse cell of (p - x0), p
+// the converged pressure, centred and scaled to unit RMS (alpha makes the scale irrelevant).
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -47,6 +60,18 @@ struct NetBuffers {
     std::vector<void*> all;
 };
 
+// State of a network attached to a context as the initial guess of its pressure solves.
+struct LearnedHook {
+    impec_net* net = nullptr;
+    int factor = 1, mode = 0, h = 0, w = 0;
+    NetBuffers nb;                  // inference buffers at (1, h, w), separate from the training ones
+    __nv_bfloat16* X = nullptr;     // features [h][w][8]
+    float* raw = nullptr;           // pooled raw channels [h][w][5]
+    float* T = nullptr;             // target scratch [h][w]
+    double* x0 = nullptr;           // initial iterate of the last solve
+    double* sums = nullptr;         // [0] sum x, [1] sum x^2, [2] sum r^2 over coarse cells; [3], [4] target sums
+};
+
 }  // namespace impec
 
 struct impec_net {
@@ -54,8 +79,8 @@ struct impec_net {
     impec::NetBuffers buf;
     long long step = 0;
     int num_sms = 148;
+    int attached = 0;  // contexts whose pressure solves use this network
     int* err = nullptr;
-    double* dscal = nullptr;  // [0] sum of squares, [1] RMS scale of the previous pressure
 };
 
 namespace impec {
@@ -173,41 +198,124 @@ __global__ void k_adamw(float* __restrict__ w, __nv_bfloat16* __restrict__ wb, f
     }
 }
 
-// Features of a resident IMPES state: [4 log(1 - c + M^(1/4) c) (= log of the mobility
-// ratio to the resident fluid), log K, q dA / I, p / s, 0, 0, 0, 0], s = RMS of p.
-__global__ void k_rms(const double* __restrict__ p, size_t n, double* out) {
-    __shared__ double sh[32];
-    double s = 0.0;
-    for (size_t k = threadIdx.x; k < n; k += blockDim.x) s += p[k] * p[k];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
-        out[0] = t;
-        out[1] = sqrt(t / (double)n) + 1e-300;
-    }
-}
-
-__global__ void k_features(size_t n, const double* __restrict__ c, const double* __restrict__ K,
-                           const double* __restrict__ q, const double* __restrict__ p, double m14, double qnorm,
-                           const double* __restrict__ scal, __nv_bfloat16* __restrict__ X) {
-    const double inv_s = 1.0 / scal[1];
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-        const double ck = c[k];
-        float f[NET_IN] = {(float)(4.0 * log(1.0 - ck + m14 * ck)), K ? (float)log(K[k]) : 0.0f, (float)(q[k] * qnorm),
-                           (float)(p[k] * inv_s), 0.0f, 0.0f, 0.0f, 0.0f};
+// Block sum of K values into out[0..K) with one atomic per block (blockDim.x = 256).
+template <int K>
+__device__ __forceinline__ void block_add(double (&v)[K], double* out) {
+    __shared__ double sh[K][8];
 #pragma unroll
-        for (int j = 0; j < NET_IN; ++j) X[k * NET_IN + j] = __float2bfloat16(f[j]);
+    for (int j = 0; j < K; ++j)
+        for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
+    const int wid = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int j = 0; j < K; ++j) sh[j][wid] = v[j];
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[threadIdx.x][k];
+        atomicAdd(out + threadIdx.x, t);
     }
 }
 
-__global__ void k_prediction_to_pressure(size_t n, const float* __restrict__ out, const double* __restrict__ scal,
-                                         double* __restrict__ p) {
-    const double s = scal[1];
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-        p[k] = s * (double)out[k * NET_OUT];
+// Raw features per coarse cell (f x f fine cells) into raw [h][w][5]; sums of the centred
+// pressure's moments and of the residual's square into sums[0..3).
+__global__ void __launch_bounds__(256) k_learn_pool(int n1, int n2, int f, const double* __restrict__ c,
+                                                    const double* __restrict__ K, const double* __restrict__ q,
+                                                    const double* __restrict__ x, const double* __restrict__ r,
+                                                    double m14, double qnorm, float* __restrict__ raw,
+                                                    double* sums) {
+    const int h = n1 / f, w = n2 / f;
+    const size_t m = (size_t)h * w;
+    double acc[3] = {0.0, 0.0, 0.0};
+    const double inv = 1.0 / ((double)f * f);
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x) {
+        const int I = (int)(k / w), J = (int)(k % w);
+        double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int a = 0; a < f; ++a)
+            for (int b = 0; b < f; ++b) {
+                const size_t g = (size_t)(I * f + a) * n2 + (size_t)J * f + b;
+                const double cg = c[g];
+                s[0] += 4.0 * log(1.0 - cg + m14 * cg);
+                s[1] += K ? log(K[g]) : 0.0;
+                s[2] += q[g];
+                s[3] += x[g];
+                s[4] += r[g];
+            }
+        const double xm = s[3] * inv, rm = s[4] * inv;
+        raw[k * 5 + 0] = (float)(s[0] * inv);
+        raw[k * 5 + 1] = (float)(s[1] * inv);
+        raw[k * 5 + 2] = (float)(s[2] * qnorm);
+        raw[k * 5 + 3] = (float)xm;
+        raw[k * 5 + 4] = (float)rm;
+        acc[0] += xm;
+        acc[1] += xm * xm;
+        acc[2] += rm * rm;
+    }
+    block_add<3>(acc, sums);
+}
+
+__global__ void k_learn_pack(size_t m, const float* __restrict__ raw, const double* __restrict__ sums,
+                             __nv_bfloat16* __restrict__ X) {
+    const double mean = sums[0] / (double)m;
+    const double var = sums[1] / (double)m - mean * mean;
+    const double sx = 1.0 / (sqrt(var > 0.0 ? var : 0.0) + 1e-300), sr = 1.0 / (sqrt(sums[2] / (double)m) + 1e-300);
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x) {
+        const float v[NET_IN] = {raw[k * 5 + 0], raw[k * 5 + 1], raw[k * 5 + 2],
+                                 (float)(((double)raw[k * 5 + 3] - mean) * sx), (float)((double)raw[k * 5 + 4] * sr),
+                                 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int j = 0; j < NET_IN; ++j) X[k * NET_IN + j] = __float2bfloat16(v[j]);
+    }
+}
+
+// Prediction (channel 0 of out [h][w][8]) to the fine grid, bilinear between coarse cell
+// centres (constant beyond the outermost centres).
+__global__ void k_learn_direction(int n1, int n2, int f, const float* __restrict__ out, double* __restrict__ d) {
+    const int h = n1 / f, w = n2 / f;
+    const size_t n = (size_t)n1 * n2;
+    const float inv = 1.0f / (float)f;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(k / n2), j = (int)(k % n2);
+        const float fi = ((float)i + 0.5f) * inv - 0.5f, fj = ((float)j + 0.5f) * inv - 0.5f;
+        const int i0 = min(max((int)floorf(fi), 0), h - 1), j0 = min(max((int)floorf(fj), 0), w - 1);
+        const int i1 = min(i0 + 1, h - 1), j1 = min(j0 + 1, w - 1);
+        const float a = fminf(fmaxf(fi - (float)i0, 0.0f), 1.0f), b = fminf(fmaxf(fj - (float)j0, 0.0f), 1.0f);
+        const float v00 = out[((size_t)i0 * w + j0) * NET_OUT], v01 = out[((size_t)i0 * w + j1) * NET_OUT];
+        const float v10 = out[((size_t)i1 * w + j0) * NET_OUT], v11 = out[((size_t)i1 * w + j1) * NET_OUT];
+        d[k] = (double)((1.0f - a) * ((1.0f - b) * v00 + b * v01) + a * ((1.0f - b) * v10 + b * v11));
+    }
+}
+
+// Target of a recorded solve: mean over each coarse cell of (p - x0), then centred and scaled
+// to unit RMS (second kernel).
+__global__ void __launch_bounds__(256) k_learn_target(int n1, int n2, int f, const double* __restrict__ p,
+                                                      const double* __restrict__ x0, float* __restrict__ T,
+                                                      double* sums) {
+    const int h = n1 / f, w = n2 / f;
+    const size_t m = (size_t)h * w;
+    double acc[2] = {0.0, 0.0};
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x) {
+        const int I = (int)(k / w), J = (int)(k % w);
+        double s = 0.0;
+        for (int a = 0; a < f; ++a)
+            for (int b = 0; b < f; ++b) {
+                const size_t g = (size_t)(I * f + a) * n2 + (size_t)J * f + b;
+                s += p[g] - x0[g];
+            }
+        s /= (double)f * f;
+        T[k] = (float)s;
+        acc[0] += s;
+        acc[1] += s * s;
+    }
+    block_add<2>(acc, sums);
+}
+
+__global__ void k_learn_target_scale(size_t m, const double* __restrict__ sums, const float* __restrict__ T,
+                                     float* __restrict__ out) {
+    const double mean = sums[0] / (double)m, var = sums[1] / (double)m - mean * mean;
+    const double sc = 1.0 / (sqrt(var > 0.0 ? var : 0.0) + 1e-300);
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x)
+        out[k] = (float)(((double)T[k] - mean) * sc);
 }
 
 // ---------------------------------------------------------------- host side
@@ -225,8 +333,8 @@ static void free_buffers(NetBuffers& nb) {
     nb = NetBuffers();
 }
 
-static impec_status ensure_buffers(impec_net* net, int B, int H, int W) {
-    NetBuffers& nb = net->buf;
+// Activation buffers for a batch shape; train adds the pre-activations and gradients.
+static impec_status alloc_buffers(NetBuffers& nb, const impec_net* net, int B, int H, int W, bool train) {
     if (nb.B == B && nb.H == H && nb.W == W) return IMPEC_OK;
     free_buffers(nb);
     nb.B = B;
@@ -239,8 +347,9 @@ static impec_status ensure_buffers(impec_net* net, int B, int H, int W) {
     };
     for (int l = 0; l < NET_LAYERS; ++l) {
         const size_t P = level_pixels(nb, net->L[l].level), e = P * net->L[l].cout * 2;
-        IMPEC_TRY(alloc((void**)&nb.z[l], e));
         IMPEC_TRY(alloc((void**)&nb.y[l], e));
+        if (!train) continue;
+        IMPEC_TRY(alloc((void**)&nb.z[l], e));
         IMPEC_TRY(alloc((void**)&nb.dz[l], e));
     }
     const size_t P0 = level_pixels(nb, 0), P1 = level_pixels(nb, 1), P2 = level_pixels(nb, 2), P3 = level_pixels(nb, 3);
@@ -250,17 +359,21 @@ static impec_status ensure_buffers(impec_net* net, int B, int H, int W) {
     IMPEC_TRY(alloc((void**)&nb.u2, P2 * 256 * 2));
     IMPEC_TRY(alloc((void**)&nb.u1, P1 * 128 * 2));
     IMPEC_TRY(alloc((void**)&nb.u0, P0 * 64 * 2));
+    IMPEC_TRY(alloc((void**)&nb.out, P0 * NET_OUT * 4));
+    if (!train) return IMPEC_OK;
     IMPEC_TRY(alloc((void**)&nb.graw, P0 * 64 * 2));
     IMPEC_TRY(alloc((void**)&nb.ds0, P0 * 32 * 2));
     IMPEC_TRY(alloc((void**)&nb.ds1, P1 * 64 * 2));
     IMPEC_TRY(alloc((void**)&nb.ds2, P2 * 128 * 2));
-    IMPEC_TRY(alloc((void**)&nb.out, P0 * NET_OUT * 4));
     IMPEC_TRY(alloc((void**)&nb.loss, sizeof(double)));
     return IMPEC_OK;
 }
 
-static const __nv_bfloat16* layer_input(const impec_net* net, const __nv_bfloat16* X, int l) {
-    const NetBuffers& nb = net->buf;
+static impec_status ensure_buffers(impec_net* net, int B, int H, int W) {
+    return alloc_buffers(net->buf, net, B, H, W, true);
+}
+
+static const __nv_bfloat16* layer_input(const NetBuffers& nb, const __nv_bfloat16* X, int l) {
     switch (l) {
         case 0: return X;
         case 2: return nb.d1;
@@ -273,11 +386,11 @@ static const __nv_bfloat16* layer_input(const impec_net* net, const __nv_bfloat1
     }
 }
 
-static impec_status conv_forward(impec_net* net, const __nv_bfloat16* X, int l, bool train, cudaStream_t s) {
+static impec_status conv_forward(impec_net* net, const NetBuffers& nb, const __nv_bfloat16* X, int l, bool train,
+                                 cudaStream_t s) {
     const NetLayer& L = net->L[l];
-    const NetBuffers& nb = net->buf;
     ConvArgs a = {};
-    a.X = layer_input(net, X, l);
+    a.X = layer_input(nb, X, l);
     a.W = L.w;
     a.bias = L.b;
     a.Z = train ? nb.z[l] : nullptr;
@@ -296,11 +409,12 @@ static impec_status conv_forward(impec_net* net, const __nv_bfloat16* X, int l, 
     return launch_conv(a, s);
 }
 
-static impec_status net_forward(impec_net* net, const __nv_bfloat16* X, bool train, cudaStream_t s) {
-    NetBuffers& nb = net->buf;
+// Launch only (no host synchronisation): also used inside captured pressure solves.
+static impec_status net_forward(impec_net* net, const NetBuffers& nb, const __nv_bfloat16* X, bool train,
+                                cudaStream_t s) {
     const int B = nb.B, H = nb.H, W = nb.W;
     for (int l = 0; l < NET_LAYERS; ++l) {
-        IMPEC_TRY(conv_forward(net, X, l, train, s));
+        IMPEC_TRY(conv_forward(net, nb, X, l, train, s));
         switch (l) {
             case 1: k_pool2<<<egrid(level_pixels(nb, 1) * 32), 256, 0, s>>>(nb.y[1], B, H >> 1, W >> 1, 32, nb.d1); break;
             case 3: k_pool2<<<egrid(level_pixels(nb, 2) * 64), 256, 0, s>>>(nb.y[3], B, H >> 2, W >> 2, 64, nb.d2); break;
@@ -347,7 +461,7 @@ static impec_status net_backward(impec_net* net, const __nv_bfloat16* X, cudaStr
     for (int l = NET_LAYERS - 1; l >= 0; --l) {
         const NetLayer& L = net->L[l];
         const int h = H >> L.level, w = W >> L.level;
-        IMPEC_TRY(launch_wgrad(nb.dz[l], layer_input(net, X, l), B, h, w, L.cin, L.cout, L.gw, net->err, net->num_sms, s));
+        IMPEC_TRY(launch_wgrad(nb.dz[l], layer_input(nb, X, l), B, h, w, L.cin, L.cout, L.gw, net->err, net->num_sms, s));
         const size_t P = level_pixels(nb, L.level);
         k_bias_grad<<<256, 256, 0, s>>>(nb.dz[l], P, L.cout, L.gb);
         switch (l) {
@@ -423,7 +537,6 @@ static void net_free(impec_net* net) {
             if (p) cudaFree(p);
     }
     free_buffers(net->buf);
-    if (net->dscal) cudaFree(net->dscal);
 }
 
 static size_t net_param_count(const impec_net* net) {
@@ -444,7 +557,6 @@ extern "C" impec_status impec_net_create(unsigned long long seed, impec_net** ou
     cudaDeviceGetAttribute(&net->num_sms, cudaDevAttrMultiProcessorCount, dev);
     net->err = device_error_flag();
     impec_status s = net->err ? net_init(net, seed) : IMPEC_ERR_CUDA;
-    if (s == IMPEC_OK && cudaMalloc((void**)&net->dscal, 4 * sizeof(double)) != cudaSuccess) s = IMPEC_ERR_CUDA;
     if (s != IMPEC_OK) {
         net_free(net);
         delete net;
@@ -456,6 +568,10 @@ extern "C" impec_status impec_net_create(unsigned long long seed, impec_net** ou
 
 extern "C" impec_status impec_net_destroy(impec_net* net) {
     if (!net) return IMPEC_OK;
+    if (net->attached > 0) {
+        set_error("impec_net_destroy: the network is still attached to a context (impec_learned_attach with NULL first)");
+        return IMPEC_ERR_ARG;
+    }
     cudaDeviceSynchronize();
     net_free(net);
     delete net;
@@ -475,7 +591,7 @@ extern "C" impec_status impec_net_train_batch(impec_net* net, const void* X, con
     IMPEC_TRY(ensure_buffers(net, B, H, W));
     NetBuffers& nb = net->buf;
     const __nv_bfloat16* x = (const __nv_bfloat16*)X;
-    IMPEC_TRY(net_forward(net, x, true, s));
+    IMPEC_TRY(net_forward(net, nb, x, true, s));
     const size_t P = level_pixels(nb, 0);
     IMPEC_CUDA_TRY(cudaMemsetAsync(nb.loss, 0, sizeof(double), s));
     k_mse<<<egrid(P), 256, 0, s>>>(nb.out, T, P, nb.dz[NET_LAYERS - 1], nb.loss);
@@ -507,7 +623,7 @@ extern "C" impec_status impec_net_backprop(impec_net* net, const void* X, const 
         IMPEC_CUDA_TRY(cudaMemsetAsync(L.gb, 0, (size_t)L.cout * 4, s));
     }
     const __nv_bfloat16* x = (const __nv_bfloat16*)X;
-    IMPEC_TRY(net_forward(net, x, true, s));
+    IMPEC_TRY(net_forward(net, nb, x, true, s));
     const size_t P = level_pixels(nb, 0);
     IMPEC_CUDA_TRY(cudaMemsetAsync(nb.loss, 0, sizeof(double), s));
     k_mse<<<egrid(P), 256, 0, s>>>(nb.out, T, P, nb.dz[NET_LAYERS - 1], nb.loss);
@@ -521,7 +637,7 @@ extern "C" impec_status impec_net_forward(impec_net* net, const void* X, int B, 
     if (!net || !X || !out || !net_shape_ok(B, H, W)) return IMPEC_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     IMPEC_TRY(ensure_buffers(net, B, H, W));
-    IMPEC_TRY(net_forward(net, (const __nv_bfloat16*)X, false, s));
+    IMPEC_TRY(net_forward(net, net->buf, (const __nv_bfloat16*)X, false, s));
     const size_t P = level_pixels(net->buf, 0);
     IMPEC_CUDA_TRY(cudaMemcpy2DAsync(out, sizeof(float), net->buf.out, NET_OUT * sizeof(float), sizeof(float), P,
                                      cudaMemcpyDeviceToDevice, s));
@@ -554,42 +670,125 @@ extern "C" impec_status impec_net_parameters(impec_net* net, float* host_out, co
     return IMPEC_OK;
 }
 
-// Features of the context's resident state (c, K, q and the current p as the previous
-// pressure) into X [N1][N2][8] bf16; *scale = RMS of p (the unit of the pressure channel and of
-// the prediction).
-extern "C" impec_status impec_net_features(impec_ctx* ctx, impec_net* net, void* X, double* scale) {
-    if (!ctx || !net || !X) return IMPEC_ERR_ARG;
-    const size_t n = (size_t)ctx->P.N1 * ctx->P.N2;
+// ---------------------------------------------------------------- pressure-solve hook
+namespace impec {
+
+bool learned_predicts(const impec_ctx* ctx) { return ctx->learned && ctx->learned->mode == 1; }
+
+// Inside pressure_prepare, after x = the previous pressure and r0 = f - A x (launch only):
+// features of this solve, a copy of x, and (predicting) the direction d on the fine grid.
+impec_status learned_predict(impec_ctx* ctx, const double* x, const double* r0, double* d) {
+    LearnedHook* H = ctx->learned;
+    const int N1 = ctx->P.N1, N2 = ctx->P.N2;
+    const size_t n = (size_t)N1 * N2, m = (size_t)H->h * H->w;
     cudaStream_t s = ctx->stream;
-    k_rms<<<1, 1024, 0, s>>>(ctx->p, n, net->dscal);
+    IMPEC_CUDA_TRY(cudaMemsetAsync(H->sums, 0, 3 * sizeof(double), s));
     const double qnorm = ctx->G.dA / (ctx->P.I != 0.0 ? ctx->P.I : 1.0);
-    k_features<<<egrid(n), 256, 0, s>>>(n, ctx->c, ctx->K11, ctx->q, ctx->p, ctx->G.mob1over4, qnorm, net->dscal,
-                                         (__nv_bfloat16*)X);
+    ++ctx->nlaunch;
+    k_learn_pool<<<egrid(m), 256, 0, s>>>(N1, N2, H->factor, ctx->c, ctx->K11, ctx->q, x, r0, ctx->G.mob1over4, qnorm,
+                                          H->raw, H->sums);
+    ++ctx->nlaunch;
+    k_learn_pack<<<egrid(m), 256, 0, s>>>(m, H->raw, H->sums, H->X);
     IMPEC_CUDA_TRY(cudaGetLastError());
-    if (scale) {
-        double h[2];
-        IMPEC_CUDA_TRY(cudaMemcpyAsync(h, net->dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-        IMPEC_CUDA_TRY(cudaStreamSynchronize(s));
-        *scale = h[1];
-    }
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(H->x0, x, n * 8, cudaMemcpyDeviceToDevice, s));
+    if (H->mode != 1) return IMPEC_OK;
+    IMPEC_TRY(net_forward(H->net, H->nb, H->X, false, s));
+    ctx->nlaunch += NET_LAYERS + 6;
+    ++ctx->nlaunch;
+    k_learn_direction<<<egrid(n), 256, 0, s>>>(N1, N2, H->factor, H->nb.out, d);
+    IMPEC_CUDA_TRY(cudaGetLastError());
     return IMPEC_OK;
 }
 
-// Learned initial guess for the next pressure solve: features of the resident state, one
-// forward pass, p := RMS(p) * prediction.  The context's solve must use warm_start for the guess
-// to matter; it still converges to its tolerance.
-extern "C" impec_status impec_net_warm_start(impec_ctx* ctx, impec_net* net, void* workspace) {
-    if (!ctx || !net || !workspace || !net_shape_ok(1, ctx->P.N1, ctx->P.N2)) {
-        set_error("impec_net_warm_start: N1 and N2 must be multiples of 8");
+void learned_release(impec_ctx* ctx) {
+    LearnedHook* H = ctx->learned;
+    if (!H) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream); else cudaDeviceSynchronize();
+    free_buffers(H->nb);
+    void* ps[] = {H->X, H->raw, H->T, H->x0, H->sums, ctx->lrn_r0, ctx->lrn_d, ctx->lrn_Ad, ctx->lrn_alpha};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    ctx->lrn_r0 = ctx->lrn_d = ctx->lrn_Ad = ctx->lrn_alpha = nullptr;
+    if (H->net) H->net->attached--;
+    delete H;
+    ctx->learned = nullptr;
+}
+
+}  // namespace impec
+
+extern "C" impec_status impec_learned_attach(impec_ctx* ctx, impec_net* net, int factor, int mode) {
+    if (!ctx) return IMPEC_ERR_ARG;
+    if (ctx->stream) IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream)); else IMPEC_CUDA_TRY(cudaDeviceSynchronize());
+    invalidate_step_graph(ctx);
+    learned_release(ctx);
+    if (!net || mode == 0) return IMPEC_OK;
+    const int N1 = ctx->P.N1, N2 = ctx->P.N2;
+    if ((mode != 1 && mode != 2) || (factor != 1 && factor != 2 && factor != 4 && factor != 8) ||
+        N1 % (8 * factor) != 0 || N2 % (8 * factor) != 0) {
+        set_error("impec_learned_attach: mode 1 or 2, factor 1, 2, 4 or 8 with N1 and N2 multiples of 8 * factor");
         return IMPEC_ERR_ARG;
     }
-    const int N1 = ctx->P.N1, N2 = ctx->P.N2;
-    const size_t n = (size_t)N1 * N2;
-    IMPEC_TRY(impec_net_features(ctx, net, workspace, nullptr));
+    if (!ctx->singular || !ctx->P.warm_start) {
+        set_error("impec_learned_attach: needs warm_start and a pure-Neumann (well-driven) pressure system");
+        return IMPEC_ERR_ARG;
+    }
+    LearnedHook* H = new LearnedHook();
+    ctx->learned = H;
+    H->net = net;
+    net->attached++;
+    H->factor = factor;
+    H->mode = mode;
+    H->h = N1 / factor;
+    H->w = N2 / factor;
+    const size_t n = (size_t)N1 * N2, m = (size_t)H->h * H->w;
+    auto fail = [&](impec_status st) { learned_release(ctx); return st; };
+    if (alloc_buffers(H->nb, net, 1, H->h, H->w, false) != IMPEC_OK) return fail(IMPEC_ERR_CUDA);
+    if (cudaMalloc((void**)&H->X, m * NET_IN * 2) != cudaSuccess || cudaMalloc((void**)&H->raw, m * 5 * 4) != cudaSuccess ||
+        cudaMalloc((void**)&H->T, m * 4) != cudaSuccess || cudaMalloc((void**)&H->x0, n * 8) != cudaSuccess ||
+        cudaMalloc((void**)&H->sums, 8 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void**)&ctx->lrn_r0, n * 8) != cudaSuccess || cudaMalloc((void**)&ctx->lrn_d, n * 8) != cudaSuccess ||
+        cudaMalloc((void**)&ctx->lrn_Ad, n * 8) != cudaSuccess || cudaMalloc((void**)&ctx->lrn_alpha, sizeof(double)) != cudaSuccess)
+        return fail(IMPEC_ERR_CUDA);
     cudaStream_t s = ctx->stream;
-    IMPEC_TRY(ensure_buffers(net, 1, N1, N2));
-    IMPEC_TRY(net_forward(net, (const __nv_bfloat16*)workspace, false, s));
-    k_prediction_to_pressure<<<egrid(n), 256, 0, s>>>(n, net->buf.out, net->dscal, ctx->p);
+    IMPEC_CUDA_TRY(cudaMemsetAsync(H->X, 0, m * NET_IN * 2, s));
+    IMPEC_CUDA_TRY(cudaMemsetAsync(H->x0, 0, n * 8, s));
+    IMPEC_CUDA_TRY(cudaMemsetAsync(ctx->lrn_alpha, 0, sizeof(double), s));
+    // one forward outside any capture: kernel attributes are set before the solve graph records it
+    impec_status st = net_forward(net, H->nb, H->X, false, s);
+    if (st != IMPEC_OK) return fail(st);
+    st = check_err(net->err, s, "impec_learned_attach");
+    if (st != IMPEC_OK) return fail(st);
+    return IMPEC_OK;
+}
+
+// Features of the last solve (bf16 [N1/f][N2/f][8], device).
+extern "C" impec_status impec_learned_features(impec_ctx* ctx, void* X) {
+    if (!ctx || !ctx->learned || !X) return IMPEC_ERR_ARG;
+    LearnedHook* H = ctx->learned;
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(X, H->X, (size_t)H->h * H->w * NET_IN * 2, cudaMemcpyDeviceToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IMPEC_OK;
+}
+
+// Training target of the last solve from the resident (converged) pressure: fp32 [N1/f][N2/f], device.
+extern "C" impec_status impec_learned_target(impec_ctx* ctx, float* T) {
+    if (!ctx || !ctx->learned || !T) return IMPEC_ERR_ARG;
+    LearnedHook* H = ctx->learned;
+    const size_t m = (size_t)H->h * H->w;
+    cudaStream_t s = ctx->stream;
+    IMPEC_CUDA_TRY(cudaMemsetAsync(H->sums + 3, 0, 2 * sizeof(double), s));
+    k_learn_target<<<egrid(m), 256, 0, s>>>(ctx->P.N1, ctx->P.N2, H->factor, ctx->p, H->x0, H->T, H->sums + 3);
+    k_learn_target_scale<<<egrid(m), 256, 0, s>>>(m, H->sums + 3, H->T, T);
     IMPEC_CUDA_TRY(cudaGetLastError());
-    return check_err(net->err, s, "impec_net_warm_start");
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(s));
+    return IMPEC_OK;
+}
+
+// Step length alpha of the last solve's learned correction (0 when the prediction was
+// rejected); IMPEC_ERR_CUDA if a tensor-core wait of the network gave up (the solve itself
+// is unaffected: its alpha is then whatever the partial prediction gave, or 0).
+extern "C" impec_status impec_learned_alpha(impec_ctx* ctx, double* alpha) {
+    if (!ctx || !ctx->learned || !alpha) return IMPEC_ERR_ARG;
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(alpha, ctx->lrn_alpha, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    return check_err(ctx->learned->net->err, ctx->stream, "impec_learned_alpha");
 }

@@ -1114,6 +1114,7 @@ __global__ void k_mg_check(DevScalars* S, double tol, int max_cycles, int inc, c
     double fn = S->fnorm2, rn = S->rnorm2;
     double rr = fn > 0 ? sqrt(rn / fn) : sqrt(rn);
     S->relres = rr;
+    if (!inc && S->mg_cycles == 0) S->relres0 = rr;
     const bool bad = !(rr == rr) || isinf(rr);
     const bool go = !bad && !breakdown && rr > tol && S->mg_cycles < max_cycles;
     if (bad) S->flags |= FLAG_MG_NAN;
@@ -1240,6 +1241,43 @@ static impec_status fine_residual(impec_ctx* ctx, const double* x, float* r32, d
     return IMPEC_OK;
 }
 
+// x += alpha d with alpha = (r0, d) / (d, A d) (from k_cg_dots: pcg_rz, pcg_zq), the step
+// along the learned direction that minimises the A-norm error; 0 when (d, A d) is not
+// positive or alpha is not finite.
+__global__ void k_learn_step(size_t n, double* __restrict__ x, const double* __restrict__ d,
+                             const DevScalars* __restrict__ S, double* alpha_out) {
+    pdl_enter();
+    const double dad = S->pcg_zq, rd = S->pcg_rz;
+    double a = dad > 0.0 ? rd / dad : 0.0;
+    if (!(a == a) || isinf(a)) a = 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *alpha_out = a;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        x[k] += a * d[k];
+}
+
+// Learned initial guess (an attached network): r0 = f - A x, the network's direction d from
+// the state and r0, then the A-norm-optimal step along d (launch only).
+static impec_status learned_guess(impec_ctx* ctx, double* x) {
+    Level& F = ctx->L[0];
+    DevScalars* S = ctx->dscal;
+    IMPEC_TRY(fine_residual(ctx, x, nullptr, ctx->lrn_r0));
+    IMPEC_TRY(learned_predict(ctx, x, ctx->lrn_r0, ctx->lrn_d));
+    if (!learned_predicts(ctx)) return IMPEC_OK;
+    const int cap = red_cap(ctx->num_sms, ctx->max_blocks), blocks = seg_blocks(F.n1, F.n2, cap);
+    ++ctx->nlaunch;
+    launch_k(ctx->stream, k_cg_apply, blocks, RED_THREADS, 0, F, (const double*)ctx->lrn_d, ctx->lrn_Ad, ctx->partials,
+             ctx->max_blocks, ctx->counter, &S->pcg_pq);
+    ++ctx->nlaunch;
+    launch_k(ctx->stream, k_cg_dots, blocks, RED_THREADS, 0, F.n1, F.n2, (const double*)ctx->lrn_r0,
+             (const double*)ctx->lrn_d, (const float*)nullptr, (const double*)ctx->lrn_Ad, ctx->partials,
+             ctx->max_blocks, ctx->counter, &S->pcg_rz);
+    ++ctx->nlaunch;
+    launch_k(ctx->stream, k_learn_step, ctx->num_sms * 4, 256, 0, F.n(), x, (const double*)ctx->lrn_d,
+             (const DevScalars*)S, ctx->lrn_alpha);
+    IMPEC_LAUNCH_CHECK();
+    return IMPEC_OK;
+}
+
 // Operator, hierarchy, consistent rhs, initial iterate and initial residual (launch only).
 impec_status pressure_prepare(impec_ctx* ctx, const double* c, const double* p) {
     const impec_params& P = ctx->P;
@@ -1266,6 +1304,7 @@ impec_status pressure_prepare(impec_ctx* ctx, const double* c, const double* p) 
         launch_k(ctx->stream, k_dirichlet_rhs, ctx->num_sms * 4, 256, 0, n, ctx->f, x, ctx->dfd, ctx->dmask);
         IMPEC_LAUNCH_CHECK();
     }
+    if (ctx->learned) IMPEC_TRY(learned_guess(ctx, x));
     if (!ctx->krylov) IMPEC_CUDA_TRY(cudaMemcpyAsync(F.b, ctx->f, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     IMPEC_CUDA_TRY(cudaMemsetAsync(&S->mg_cycles, 0, sizeof(int), ctx->stream));
     const bool mixed = P.precision == IMPEC_PREC_MIXED;

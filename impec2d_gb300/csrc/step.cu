@@ -312,6 +312,17 @@ impec_status impec_pressure_solve_resident(impec_ctx* ctx, int sync, int* cycles
     return IMPEC_OK;
 }
 
+// Cycles, final and initial relative residual of the last pressure solve (waits for the
+// context's stream).
+impec_status impec_last_solve(impec_ctx* ctx, int* cycles, double* relres, double* relres0) {
+    if (!ctx) return IMPEC_ERR_ARG;
+    IMPEC_TRY(sync_scalars(ctx));
+    if (cycles) *cycles = ctx->hscal->mg_cycles;
+    if (relres) *relres = ctx->hscal->relres;
+    if (relres0) *relres0 = ctx->hscal->relres0;
+    return IMPEC_OK;
+}
+
 impec_status impec_launch_count(impec_ctx* ctx, long long* n) {
     if (!ctx || !n) return IMPEC_ERR_ARG;
     IMPEC_TRY(sync_scalars(ctx));

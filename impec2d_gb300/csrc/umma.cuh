@@ -109,6 +109,10 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t 
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Close the group of this thread's outstanding cp.async; wait until at most N groups are pending.
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 }  // namespace umma
 }  // namespace impec

@@ -162,6 +162,9 @@ impec_status impec_run_steps(impec_ctx* ctx, int n, impec_step_info* info);
 /* Pressure solve of the resident state (c -> p) as one CUDA graph (no host round trip per
  * cycle).  With sync = 0 the call only enqueues; cycles/relres are then not written. */
 impec_status impec_pressure_solve_resident(impec_ctx* ctx, int sync, int* cycles, double* relres);
+/* Cycles, final and initial relative residual of the last pressure solve (waits for the
+ * context's stream). */
+impec_status impec_last_solve(impec_ctx* ctx, int* cycles, double* relres, double* relres0);
 /* Kernel launches executed by this context so far (stream launches + step-graph replays). */
 impec_status impec_launch_count(impec_ctx* ctx, long long* n);
 /* Engine instrumentation: times `reps` stream launches of one hot kernel on the resident
@@ -216,12 +219,12 @@ impec_status impec_conv3x3_weight_grad(const void* dZ, const void* X, int B, int
 
 /* Learned warm start (no counterpart in the reference): a 4-level convolutional encoder-decoder
  * (15 3x3 convolutions, 32..256 channels, GELU, additive skips; BF16 weights and activations,
- * fp32 accumulation on the tensor cores, fp32 AdamW master weights) that predicts the pressure
- * of the next solve from [log mobility ratio, log K, well rate, previous pressure / RMS].
- * Features X are [B][H][W][8] bf16 (channels 4..7 zero), targets T and predictions [B][H][W]
- * fp32 in units of the previous pressure's RMS; H and W multiples of 8. */
+ * fp32 accumulation on the tensor cores, fp32 AdamW master weights).  Inputs X are
+ * [B][H][W][8] bf16 feature maps (channels 5..7 zero), targets T and predictions [B][H][W]
+ * fp32; H and W multiples of 8. */
 typedef struct impec_net impec_net;
 impec_status impec_net_create(unsigned long long seed, impec_net** out);
+/* Fails while the network is attached to a context. */
 impec_status impec_net_destroy(impec_net* net);
 /* One AdamW step (lr, decoupled weight decay) on a batch; *loss = the batch's mean squared error. */
 impec_status impec_net_train_batch(impec_net* net, const void* X, const float* T, int B, int H, int W, double lr,
@@ -233,12 +236,22 @@ impec_status impec_net_forward(impec_net* net, const void* X, int B, int H, int 
 /* *count = number of parameters; which 0: weights (host_out receives, host_in replaces),
  * which 1: gradients (host_out receives).  Order: per layer, weights [cout][Kp] then bias. */
 impec_status impec_net_parameters(impec_net* net, float* host_out, const float* host_in, size_t* count, int which);
-/* Features of the context's resident state (its p is the previous pressure) into X [N1][N2][8];
- * *scale = RMS of p. */
-impec_status impec_net_features(impec_ctx* ctx, impec_net* net, void* X, double* scale);
-/* p := RMS(p) * prediction: the initial guess of the next pressure solve (with warm_start set).
- * workspace: N1*N2*8 bf16 on the device. */
-impec_status impec_net_warm_start(impec_ctx* ctx, impec_net* net, void* workspace);
+
+/* Attaches net to ctx's pressure solves (mode 1: predict, 2: record only), or detaches it (net
+ * NULL or mode 0).  Needs warm_start (x0 = the previous pressure) and a well-driven pure-Neumann
+ * system.  Each solve then computes r0 = f - A x0 and the features [mean 4 log(1-c+M^(1/4)c),
+ * mean log K, sum q dA/I, centred x0 / RMS, r0 / RMS] over factor x factor cells (factor 1, 2,
+ * 4 or 8; N1 and N2 multiples of 8 * factor).  Predicting, the network's output d (bilinear to
+ * the fine grid) moves the iterate: x0 += alpha d, alpha = (r0, d) / (d, A d); the solve still
+ * converges to its tolerance.  The captured step graph is rebuilt at the next step. */
+impec_status impec_learned_attach(impec_ctx* ctx, impec_net* net, int factor, int mode);
+/* Features of the last solve: X bf16 [N1/factor][N2/factor][8] on the device. */
+impec_status impec_learned_features(impec_ctx* ctx, void* X);
+/* Training target of the last solve: the mean of (p - x0) over each factor x factor block, p the
+ * resident converged pressure, centred and scaled to unit RMS; T fp32 [N1/factor][N2/factor]. */
+impec_status impec_learned_target(impec_ctx* ctx, float* T);
+/* Step length of the last solve's learned correction (0: rejected). */
+impec_status impec_learned_alpha(impec_ctx* ctx, double* alpha);
 
 /* FP64 fused multiply-adds per second that the current device sustains (eight independent
  * chains per thread on every SM): the denominator of the FP64-pipe fractions reported beside

@@ -157,25 +157,79 @@ def test_net_training_reduces_the_loss(engine):
     net.close()
 
 
-def test_net_warm_start_keeps_the_solve_converging(engine):
-    """The learned guess (untrained here) is only an initial iterate: the solve from it reaches
-    the same tolerance."""
+def _member(E, N, seed, warm_start=1):
+    from impec2d_gb300.workloads import realisation
+    return realisation(E, N, seed, precision="mixed", ell=8.0, warm_start=warm_start)
+
+
+def test_learned_record_mode_leaves_the_solve_unchanged(engine):
+    """Recording features and targets does not move the initial iterate: the run is bit-identical
+    to the same run without the hook; the features and targets have their stated normalisation."""
     import numpy as np
     import torch
-    from helpers import cell_ghost, oparams, source
+    E = engine
+    N, f = 64, 2
+    a, b = _member(E, N, 1), _member(E, N, 1)
+    rec = E.Net(seed=0)
+    rec.attach(b, factor=f, mode=2)
+    h = N // f
+    X = torch.empty((h, h, 8), dtype=torch.bfloat16, device="cuda")
+    T = torch.empty((h, h), dtype=torch.float32, device="cuda")
+    for _ in range(5):
+        ia, ib = a.step(), b.step()
+        assert ia.its == ib.its and ia.relres == ib.relres
+    E.Net.last_features(b, X)
+    E.Net.last_target(b, T)
+    out = []
+    for cx in (a, b):
+        ch, ph = np.zeros((N + 4, N + 4)), np.zeros((N + 4, N + 4))
+        cx.download(ch, ph, None, ghost=2)
+        out.append((ch, ph))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    x = X.float()
+    assert (x[..., 5:] == 0).all()
+    assert abs(float(x[..., 2].sum())) < 1e-3 and float(x[..., 2].max()) == 1.0  # injector +1, producer -1
+    assert abs(float(x[..., 3].mean())) < 2e-2 and abs(float(x[..., 3].pow(2).mean().sqrt()) - 1) < 2e-2
+    assert abs(float(x[..., 4].pow(2).mean().sqrt()) - 1) < 2e-2
+    assert abs(float(T.mean())) < 1e-4 and abs(float(T.pow(2).mean().sqrt()) - 1) < 1e-4
+    with pytest.raises(E.ImpecError):
+        rec.close()  # still attached
+    E.Net.detach(b)
+    rec.close()
+    a.close()
+    b.close()
+
+
+def test_learned_guess_keeps_the_solve_converging(engine):
+    """An attached (untrained) network only moves the initial iterate along its prediction by
+    the A-norm-optimal step: every solve still reaches 1e-10."""
+    import math
     E = engine
     N = 64
-    P = E.default_params(N, N, stype=1, warm_start=1, eps=1e-10)
-    ctx = E.Context(P)
-    OP = oparams(P)
-    ctx.upload(cell_ghost(OP, np.zeros((N, N))), source(OP), ghost=2)
-    ctx.set_time(0.0)
-    ctx.step()  # p now holds a solved pressure
+    ctx = _member(E, N, 2)
     net = E.Net(seed=2)
-    ws = torch.empty((N, N, 8), dtype=torch.bfloat16, device="cuda")
-    X = torch.empty((1, N, N, 8), dtype=torch.bfloat16, device="cuda")
-    assert net.features(ctx, X) > 0
-    net.warm_start(ctx, ws)
-    info = ctx.step()
-    assert info.relres <= 1e-10 and info.its < 200
+    ctx.run_steps(2)
+    net.attach(ctx, factor=1, mode=1)
+    for _ in range(4):
+        info = ctx.step()
+        assert info.relres <= 1e-10
+        assert math.isfinite(E.Net.last_alpha(ctx))
+    E.Net.detach(ctx)
+    net.close()
+    ctx.close()
+
+
+def test_learned_attach_rejections(engine):
+    E = engine
+    net = E.Net(seed=0)
+    ctx = _member(E, 64, 3, warm_start=0)
+    with pytest.raises(E.ImpecError):
+        net.attach(ctx, factor=1, mode=1)  # no warm start
+    ctx.close()
+    ctx = _member(E, 72, 3)
+    with pytest.raises(E.ImpecError):
+        net.attach(ctx, factor=2, mode=1)  # 72 / 2 is not a multiple of 8
+    with pytest.raises(E.ImpecError):
+        net.attach(ctx, factor=3, mode=1)
+    ctx.close()
     net.close()
