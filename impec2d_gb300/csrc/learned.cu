@@ -8,9 +8,11 @@
 // the next stage overwrites the tiles.  The epilogue reads the accumulator with tcgen05.ld
 // (warp w owns accumulator rows 32w .. 32w+31).  Every mbarrier wait is bounded: on timeout
 // the CTA records an error, waits once more (bounded) for its own MMAs and frees its TMEM.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 
 #include "learned.cuh"
@@ -116,195 +118,302 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 
-// Pipelined over CV_STAGES shared-memory stages: while the tensor core works on stage k, the
-// copies of stages k+1 .. k+CV_STAGES-1 are in flight.  A stage's slot is refilled only after
-// the mbarrier of the MMAs that read it has completed.  Thread t always copies chunk t % 8 of
-// rows t / 8 + 16 i, so each thread resolves its pixels' coordinates once.
-constexpr int CV_STAGES = 4;
+// Epilogue of both convolution kernels: warp w (0-3) reads TMEM lanes 32w .. 32w + 31 (one
+// output pixel per thread) in blocks of 32 accumulator columns.
+template <int BN>
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t tmem, int m0, int n0, int warp, int lane,
+                                              int M) {
+        const int m = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int cb = 0; cb < (BN + 31) / 32; ++cb) {
+        float v[32];
+        umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
+        if (m >= M) continue;
+        const size_t row = (size_t)m * a.cout;
+        const int nb = n0 + cb * 32;
+        if (nb + 32 <= a.cout && (a.cout & 7) == 0) {  // 32 whole channels: 16-byte accesses
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float z[8], y[8];
+                const size_t o = row + nb + 8 * q;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) z[k] = v[8 * q + k] + (a.bias ? a.bias[nb + 8 * q + k] : 0.0f);
+                if (a.gz) {
+                    __align__(16) __nv_bfloat16 g8[8], ad8[8], o8[8];
+                    *reinterpret_cast<uint4*>(g8) = *reinterpret_cast<const uint4*>(a.gz + o);
+                    if (a.add) *reinterpret_cast<uint4*>(ad8) = *reinterpret_cast<const uint4*>(a.add + o);
+                    if (a.R) {
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) o8[k] = __float2bfloat16(z[k]);
+                        *reinterpret_cast<uint4*>(a.R + o) = *reinterpret_cast<const uint4*>(o8);
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        float t = z[k];
+                        if (a.add) t += __bfloat162float(ad8[k]);
+                        y[k] = t * gelu_grad(__bfloat162float(g8[k]));
+                    }
+                } else {
+                    if (a.Z) {
+                        __align__(16) __nv_bfloat16 o8[8];
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) o8[k] = __float2bfloat16(z[k]);
+                        *reinterpret_cast<uint4*>(a.Z + o) = *reinterpret_cast<const uint4*>(o8);
+                    }
+                    __align__(16) __nv_bfloat16 s8[8];
+                    if (a.skip) *reinterpret_cast<uint4*>(s8) = *reinterpret_cast<const uint4*>(a.skip + o);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        y[k] = a.act ? gelu_f(z[k]) : z[k];
+                        if (a.skip) y[k] += __bfloat162float(s8[k]);
+                    }
+                }
+                if (a.Y) {
+                    __align__(16) __nv_bfloat16 o8[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) o8[k] = __float2bfloat16(y[k]);
+                    *reinterpret_cast<uint4*>(a.Y + o) = *reinterpret_cast<const uint4*>(o8);
+                }
+                if (a.Yf) {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) a.Yf[o + k] = y[k];
+                }
+            }
+            continue;
+        }
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            const int n = nb + k;
+            if (n >= a.cout || cb * 32 + k >= BN) continue;
+            float z = v[k] + (a.bias ? a.bias[n] : 0.0f);
+            if (a.gz) {  // input gradient: (acc + add) * gelu'(gz)
+                if (a.R) a.R[row + n] = __float2bfloat16(z);
+                if (a.add) z += __bfloat162float(a.add[row + n]);
+                z *= gelu_grad(__bfloat162float(a.gz[row + n]));
+                if (a.Y) a.Y[row + n] = __float2bfloat16(z);
+                if (a.Yf) a.Yf[row + n] = z;
+                continue;
+            }
+            if (a.Z) a.Z[row + n] = __float2bfloat16(z);
+            float y = a.act ? gelu_f(z) : z;
+            if (a.skip) y += __bfloat162float(a.skip[row + n]);
+            if (a.Y) a.Y[row + n] = __float2bfloat16(y);
+            if (a.Yf) a.Yf[row + n] = y;
+        }
+    }
+}
+
+// Warp-specialised pipeline over CV_STAGES shared-memory stages.  Warps 0-3 copy the operand
+// tiles with cp.async; each copy arrives on the stage's "full" mbarrier when it lands
+// (cp.async.mbarrier.arrive.noinc, 128 arrivals per phase).  One thread of warp 4 waits for a
+// full stage, issues its four MMAs and commits them to the stage's "empty" mbarrier, which the
+// copiers wait for before refilling the slot; after the last stage it commits to "done".  Warps
+// 0-3 then read the accumulator (warp w owns TMEM lanes 32w .. 32w + 31).  Thread t of the
+// copiers always copies chunk t % 8 of rows t / 8 + 16 i, so it resolves its pixels once.
+constexpr int CV_STAGES = 4, CV_COPIERS = 128, CV_THREADS = 160;
 
 template <int BN>
 constexpr int conv_smem_bytes() { return CV_STAGES * (GB_TILE_BYTES + BN * GB_K * 2) + 1024; }
 
 template <int BN>
-__global__ void __launch_bounds__(GB_THREADS) k_conv3x3(ConvArgs a) {
+__global__ void __launch_bounds__(CV_THREADS) k_conv3x3(ConvArgs a) {
     extern __shared__ __align__(1024) unsigned char cv_smem[];
     constexpr int B_BYTES = BN * GB_K * 2, STAGE = GB_TILE_BYTES + B_BYTES;
-    constexpr int AR = GB_M * 8 / GB_THREADS, BR = BN * 8 / GB_THREADS;  // rows per thread (A: 8, B: BN / 16)
-    __shared__ uint64_t mbar[CV_STAGES];
+    constexpr int AR = GB_M * 8 / CV_COPIERS, BR = BN * 8 / CV_COPIERS;  // rows per copier (A: 8, B: BN / 16)
+    __shared__ uint64_t full[CV_STAGES], empty[CV_STAGES], done;
     __shared__ uint32_t tslot;
+    __shared__ volatile int fail;
     constexpr uint32_t TCOLS = BN < 32 ? 32 : BN;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, kg = tid & 7, r0 = tid >> 3;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int M = a.B * a.H * a.W_;
     const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * BN;
     if (warp == 0) umma::tmem_alloc(&tslot, TCOLS);
-    if (tid == 0)
-        for (int st = 0; st < CV_STAGES; ++st) umma::mbar_init(&mbar[st], 1);
+    if (tid == 0) {
+        for (int st = 0; st < CV_STAGES; ++st) {
+            umma::mbar_init(&full[st], CV_COPIERS);
+            umma::mbar_init(&empty[st], 1);
+        }
+        umma::mbar_init(&done, 1);
+        fail = 0;
+    }
     umma::fence_before();
     __syncthreads();
     umma::fence_after();
     const uint32_t tmem = tslot;
-    const uint32_t idesc = umma::idesc_bf16_f32(GB_M, BN);
     const int nk = a.Kp / GB_K, K9 = 9 * a.cin;
-    // this thread's A rows: pixel index (or -1) and its y, x
-    int pix[AR], py[AR], px[AR];
-#pragma unroll
-    for (int i = 0; i < AR; ++i) {
-        const int m = m0 + r0 + 16 * i;
-        pix[i] = m < M ? m : -1;
-        const int mm = m < M ? m : 0;
-        px[i] = mm % a.W_;
-        py[i] = (mm / a.W_) % a.H;
-    }
-    auto load = [&](int kt, int slot) {
-        unsigned char* sA = cv_smem + slot * STAGE;
-        unsigned char* sB = sA + GB_TILE_BYTES;
-        const int k0 = kt * GB_K + kg * 8;
-        const bool kin = k0 < K9;
-        const int tap = kin ? k0 / a.cin : 0, ch = k0 - tap * a.cin;
-        const int dy = a.tapsign * (tap / 3 - 1), dx = a.tapsign * (tap % 3 - 1);
-        const long long shift = ((long long)dy * a.W_ + dx) * a.cin + ch;
+    if (warp < 4) {  // copiers
+        const int kg = tid & 7, r0 = tid >> 3;
+        int pix[AR], py[AR], px[AR];
 #pragma unroll
         for (int i = 0; i < AR; ++i) {
-            const int yy = py[i] + dy, xx = px[i] + dx;
-            const bool in = kin && pix[i] >= 0 && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W_;
-            const __nv_bfloat16* src = in ? a.X + (long long)pix[i] * a.cin + shift : a.X;
-            umma::cp_async16(sA + tile_off(r0 + 16 * i, kg), src, in ? 16u : 0u);
+            const int m = m0 + r0 + 16 * i;
+            pix[i] = m < M ? m : -1;
+            const int mm = m < M ? m : 0;
+            px[i] = mm % a.W_;
+            py[i] = (mm / a.W_) % a.H;
         }
-#pragma unroll
-        for (int i = 0; i < BR; ++i) {
-            const int n = n0 + r0 + 16 * i;
-            const bool in = n < a.cout;
-            umma::cp_async16(sB + tile_off(r0 + 16 * i, kg),
-                             in ? a.W + (size_t)n * a.Kp + (size_t)kt * GB_K + kg * 8 : a.W, in ? 16u : 0u);
-        }
-    };
-#pragma unroll
-    for (int st = 0; st < CV_STAGES - 1; ++st) {
-        if (st < nk) load(st, st);
-        umma::cp_async_commit();
-    }
-    bool ok = true, mine = true;
-    int issued = 0;
-    for (int kt = 0; kt < nk; ++kt) {
-        const int slot = kt % CV_STAGES;
-        umma::cp_async_wait_group<CV_STAGES - 2>();
-        umma::fence_proxy_async();
-        ok = __syncthreads_and(mine) != 0;
-        if (!ok) break;
-        if (tid == 0) {
-            umma::fence_after();
-            const uint32_t base = umma::smem_u32(cv_smem + slot * STAGE);
-#pragma unroll
-            for (int ks = 0; ks < GB_K / 16; ++ks) {
-                const uint64_t ad = umma::smem_desc(base + ks * 256, 128, 1024);
-                const uint64_t bd = umma::smem_desc(base + GB_TILE_BYTES + ks * 256, 128, 1024);
-                umma::mma_bf16(tmem, ad, bd, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+        for (int kt = 0; kt < nk; ++kt) {
+            const int slot = kt % CV_STAGES, use = kt / CV_STAGES;
+            if (use > 0 && !umma::mbar_wait(&empty[slot], (uint32_t)((use - 1) & 1), GB_WAIT_TRIES)) {
+                fail = 1;
+                break;
             }
-            umma::commit(&mbar[slot]);
+            unsigned char* sA = cv_smem + slot * STAGE;
+            unsigned char* sB = sA + GB_TILE_BYTES;
+            const int k0 = kt * GB_K + kg * 8;
+            const bool kin = k0 < K9;
+            const int tap = kin ? k0 / a.cin : 0, ch = k0 - tap * a.cin;
+            const int dy = a.tapsign * (tap / 3 - 1), dx = a.tapsign * (tap % 3 - 1);
+            const long long shift = ((long long)dy * a.W_ + dx) * a.cin + ch;
+#pragma unroll
+            for (int i = 0; i < AR; ++i) {
+                const int yy = py[i] + dy, xx = px[i] + dx;
+                const bool in = kin && pix[i] >= 0 && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W_;
+                const __nv_bfloat16* src = in ? a.X + (long long)pix[i] * a.cin + shift : a.X;
+                umma::cp_async16(sA + tile_off(r0 + 16 * i, kg), src, in ? 16u : 0u);
+            }
+#pragma unroll
+            for (int i = 0; i < BR; ++i) {
+                const int n = n0 + r0 + 16 * i;
+                const bool in = n < a.cout;
+                umma::cp_async16(sB + tile_off(r0 + 16 * i, kg),
+                                 in ? a.W + (size_t)n * a.Kp + (size_t)kt * GB_K + kg * 8 : a.W, in ? 16u : 0u);
+            }
+            umma::cp_async_mbar_arrive(&full[slot]);
         }
-        issued = kt + 1;
-        const int nxt = kt + CV_STAGES - 1;
-        if (nxt < nk) {
-            // the slot of stage nxt was last read by the MMAs of stage kt - 1
-            if (kt >= 1) mine = umma::mbar_wait(&mbar[(kt - 1) % CV_STAGES], (uint32_t)(((kt - 1) / CV_STAGES) & 1), GB_WAIT_TRIES);
-            if (mine) load(nxt, nxt % CV_STAGES);
+        umma::cp_async_wait_all();
+    } else {  // warp 4: one thread issues the MMAs
+        if (lane == 0) {
+            const uint32_t idesc = umma::idesc_bf16_f32(GB_M, BN);
+            for (int kt = 0; kt < nk; ++kt) {
+                const int slot = kt % CV_STAGES, use = kt / CV_STAGES;
+                if (!umma::mbar_wait(&full[slot], (uint32_t)(use & 1), GB_WAIT_TRIES)) {
+                    fail = 1;
+                    break;
+                }
+                umma::fence_proxy_async();  // the copies, acquired through the mbarrier, to the tensor core
+                umma::fence_after();
+                const uint32_t base = umma::smem_u32(cv_smem + slot * STAGE);
+#pragma unroll
+                for (int ks = 0; ks < GB_K / 16; ++ks) {
+                    const uint64_t ad = umma::smem_desc(base + ks * 256, 128, 1024);
+                    const uint64_t bd = umma::smem_desc(base + GB_TILE_BYTES + ks * 256, 128, 1024);
+                    umma::mma_bf16(tmem, ad, bd, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+                }
+                umma::commit(&empty[slot]);
+            }
+            umma::commit(&done);  // every MMA issued above has completed
         }
-        umma::cp_async_commit();
+        __syncwarp();
     }
-    if (ok) {
-        const int last = nk - 1;
-        mine = umma::mbar_wait(&mbar[last % CV_STAGES], (uint32_t)((last / CV_STAGES) & 1), GB_WAIT_TRIES);
-        ok = __syncthreads_and(mine) != 0;
-        if (!ok) issued = 0;  // the wait above already gave up on the last group
-    }
-    umma::cp_async_wait_all();
-    if (ok) {
+    // all MMAs issued (or given up); the accumulator is final once "done" completes
+    const bool fin = warp < 4 ? umma::mbar_wait(&done, 0u, GB_WAIT_TRIES) : true;
+    const bool ok = __syncthreads_and(fin) != 0 && fail == 0;
+    if (ok && warp < 4) {
         umma::fence_after();
-        const int m = m0 + warp * 32 + lane;
-#pragma unroll 1
-        for (int cb = 0; cb < (BN + 31) / 32; ++cb) {
-            float v[32];
-            umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
-            if (m >= M) continue;
-            const size_t row = (size_t)m * a.cout;
-            const int nb = n0 + cb * 32;
-            if (nb + 32 <= a.cout && (a.cout & 7) == 0) {  // 32 whole channels: 16-byte accesses
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    float z[8], y[8];
-                    const size_t o = row + nb + 8 * q;
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) z[k] = v[8 * q + k] + (a.bias ? a.bias[nb + 8 * q + k] : 0.0f);
-                    if (a.gz) {
-                        __align__(16) __nv_bfloat16 g8[8], ad8[8], o8[8];
-                        *reinterpret_cast<uint4*>(g8) = *reinterpret_cast<const uint4*>(a.gz + o);
-                        if (a.add) *reinterpret_cast<uint4*>(ad8) = *reinterpret_cast<const uint4*>(a.add + o);
-                        if (a.R) {
-#pragma unroll
-                            for (int k = 0; k < 8; ++k) o8[k] = __float2bfloat16(z[k]);
-                            *reinterpret_cast<uint4*>(a.R + o) = *reinterpret_cast<const uint4*>(o8);
-                        }
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            float t = z[k];
-                            if (a.add) t += __bfloat162float(ad8[k]);
-                            y[k] = t * gelu_grad(__bfloat162float(g8[k]));
-                        }
-                    } else {
-                        if (a.Z) {
-                            __align__(16) __nv_bfloat16 o8[8];
-#pragma unroll
-                            for (int k = 0; k < 8; ++k) o8[k] = __float2bfloat16(z[k]);
-                            *reinterpret_cast<uint4*>(a.Z + o) = *reinterpret_cast<const uint4*>(o8);
-                        }
-                        __align__(16) __nv_bfloat16 s8[8];
-                        if (a.skip) *reinterpret_cast<uint4*>(s8) = *reinterpret_cast<const uint4*>(a.skip + o);
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            y[k] = a.act ? gelu_f(z[k]) : z[k];
-                            if (a.skip) y[k] += __bfloat162float(s8[k]);
-                        }
-                    }
-                    if (a.Y) {
-                        __align__(16) __nv_bfloat16 o8[8];
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) o8[k] = __float2bfloat16(y[k]);
-                        *reinterpret_cast<uint4*>(a.Y + o) = *reinterpret_cast<const uint4*>(o8);
-                    }
-                    if (a.Yf) {
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) a.Yf[o + k] = y[k];
-                    }
-                }
-                continue;
-            }
-#pragma unroll
-            for (int k = 0; k < 32; ++k) {
-                const int n = nb + k;
-                if (n >= a.cout || cb * 32 + k >= BN) continue;
-                float z = v[k] + (a.bias ? a.bias[n] : 0.0f);
-                if (a.gz) {  // input gradient: (acc + add) * gelu'(gz)
-                    if (a.R) a.R[row + n] = __float2bfloat16(z);
-                    if (a.add) z += __bfloat162float(a.add[row + n]);
-                    z *= gelu_grad(__bfloat162float(a.gz[row + n]));
-                    if (a.Y) a.Y[row + n] = __float2bfloat16(z);
-                    if (a.Yf) a.Yf[row + n] = z;
-                    continue;
-                }
-                if (a.Z) a.Z[row + n] = __float2bfloat16(z);
-                float y = a.act ? gelu_f(z) : z;
-                if (a.skip) y += __bfloat162float(a.skip[row + n]);
-                if (a.Y) a.Y[row + n] = __float2bfloat16(y);
-                if (a.Yf) a.Yf[row + n] = y;
-            }
-        }
-    } else {
-        if (tid == 0) atomicExch(a.err, 1);
-        if (issued > 0) {
-            const int last = issued - 1;
-            umma::mbar_wait(&mbar[last % CV_STAGES], (uint32_t)((last / CV_STAGES) & 1), GB_WAIT_TRIES);
-        }
+        conv_epilogue<BN>(a, tmem, m0, n0, warp, lane, M);
     }
+    if (!ok && tid == 0) atomicExch(a.err, 1);
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    if (warp == 0) umma::tmem_free(tmem, TCOLS);
+}
+
+// TMA variant for cin a multiple of 32 and tiles of whole image rows (see conv_tma_plan): one
+// K stage is one tap's KS-channel slice (KS = 64: 128-byte swizzle; KS = 32: 64-byte swizzle).
+// The activation tile of a stage is one 4D box (KS channels x wbox x hbox x bbox pixels = the
+// CTA's 128 output pixels) at the tap's offset, zero-filled outside the image by the TMA; the
+// weight tile is one 2D box.  Lane 0 of warp 4 issues both loads per stage on the stage's "full"
+// mbarrier (expected bytes); lane 0 of warp 5 issues the MMAs and commits them to "empty";
+// warps 0-3 run the epilogue.  Stages: as many as fit in 200 KB (at most 8).
+constexpr int CT_THREADS = 192, CT_MAX_STAGES = 8;
+
+struct ConvTmaPlan {
+    int ks, stages, wbox, hbox, bbox;
+};
+
+template <int BN, int KS>
+__global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constant__ CUtensorMap tx,
+                                                            const __grid_constant__ CUtensorMap tw, ConvArgs a,
+                                                            int stages) {
+    extern __shared__ __align__(1024) unsigned char ct_smem[];
+    constexpr int A_BYTES = GB_M * KS * 2, B_BYTES = BN * KS * 2, STAGE = A_BYTES + B_BYTES;
+    __shared__ uint64_t full[CT_MAX_STAGES], empty[CT_MAX_STAGES], done;
+    __shared__ uint32_t tslot;
+    __shared__ volatile int fail, tma_issued;
+    constexpr uint32_t TCOLS = BN < 32 ? 32 : BN;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int M = a.B * a.H * a.W_;
+    const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * BN;
+    unsigned char* base = ct_smem + ((1024 - (umma::smem_u32(ct_smem) & 1023)) & 1023);  // 1024-byte aligned
+    if (warp == 0) umma::tmem_alloc(&tslot, TCOLS);
+    if (tid == 0) {
+        for (int st = 0; st < stages; ++st) {
+            umma::mbar_init(&full[st], 1);
+            umma::mbar_init(&empty[st], 1);
+        }
+        umma::mbar_init(&done, 1);
+        fail = 0;
+        tma_issued = 0;
+    }
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+    const int cs = a.cin / KS, nk = 9 * cs;
+    if (warp == 4) {
+        if (lane == 0) {  // TMA producer
+            const int hw = a.H * a.W_, b0 = m0 / hw, rem = m0 - b0 * hw, y0 = rem / a.W_, x0 = rem - y0 * a.W_;
+            for (int kt = 0; kt < nk; ++kt) {
+                const int slot = kt % stages, use = kt / stages;
+                if (use > 0 && !umma::mbar_wait(&empty[slot], (uint32_t)((use - 1) & 1), GB_WAIT_TRIES)) {
+                    fail = 1;
+                    break;
+                }
+                const int tap = kt / cs, c0 = (kt - tap * cs) * KS;
+                const int dy = a.tapsign * (tap / 3 - 1), dx = a.tapsign * (tap % 3 - 1);
+                unsigned char* sA = base + slot * STAGE;
+                umma::mbar_expect_tx(&full[slot], (uint32_t)STAGE);
+                umma::tma_load_4d(sA, &tx, c0, x0 + dx, y0 + dy, b0, &full[slot]);
+                umma::tma_load_2d(sA + A_BYTES, &tw, tap * a.cin + c0, n0, &full[slot]);
+                tma_issued = kt + 1;
+            }
+        }
+        __syncwarp();
+    } else if (warp == 5) {
+        if (lane == 0) {  // MMA issuer
+            const uint32_t idesc = umma::idesc_bf16_f32(GB_M, BN);
+            for (int kt = 0; kt < nk; ++kt) {
+                const int slot = kt % stages, use = kt / stages;
+                if (!umma::mbar_wait(&full[slot], (uint32_t)(use & 1), GB_WAIT_TRIES)) {
+                    fail = 1;
+                    // let the loads already issued land before the CTA ends (bounded)
+                    for (int j = kt + 1; j < tma_issued; ++j)
+                        umma::mbar_wait(&full[j % stages], (uint32_t)((j / stages) & 1), GB_WAIT_TRIES >> 4);
+                    break;
+                }
+                umma::fence_after();
+                const uint32_t sa = umma::smem_u32(base + slot * STAGE);
+#pragma unroll
+                for (int ks = 0; ks < KS / 16; ++ks) {
+                    const uint64_t ad = umma::smem_desc_sw(sa + ks * 32, KS * 2);
+                    const uint64_t bd = umma::smem_desc_sw(sa + A_BYTES + ks * 32, KS * 2);
+                    umma::mma_bf16(tmem, ad, bd, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+                }
+                umma::commit(&empty[slot]);
+            }
+            umma::commit(&done);
+        }
+        __syncwarp();
+    }
+    const bool fin = warp < 4 ? umma::mbar_wait(&done, 0u, GB_WAIT_TRIES) : true;
+    const bool ok = __syncthreads_and(fin) != 0 && fail == 0;
+    if (ok && warp < 4) {
+        umma::fence_after();
+        conv_epilogue<BN>(a, tmem, m0, n0, warp, lane, M);
+    }
+    if (!ok && tid == 0) atomicExch(a.err, 1);
     umma::fence_before();
     __syncthreads();
     umma::fence_after();
@@ -472,9 +581,104 @@ static impec_status launch_conv_bn(const ConvArgs& a, cudaStream_t s) {
     }
     const int M = a.B * a.H * a.W_;
     dim3 g((a.cout + BN - 1) / BN, (M + GB_M - 1) / GB_M);
-    k_conv3x3<BN><<<g, GB_THREADS, smem, s>>>(a);
+    k_conv3x3<BN><<<g, CV_THREADS, smem, s>>>(a);
     IMPEC_CUDA_TRY(cudaGetLastError());
     return IMPEC_OK;
+}
+
+// ---- TMA path: tensor maps through the driver's cuTensorMapEncodeTiled (runtime entry point).
+typedef CUresult (*TmapEncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static TmapEncodeFn tmap_encoder() {
+    static TmapEncodeFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (TmapEncodeFn)p;
+    }
+    return fn;
+}
+
+// Whether the TMA kernel applies: cin a multiple of 32, and the 128 pixels of a tile form one
+// box of whole rows (W a multiple of 128, or W dividing 128 with H a power-of-two multiple or
+// divisor of 128 / W, so that a box never straddles two images).
+static bool conv_tma_plan(const ConvArgs& a, int BN, ConvTmaPlan& p) {
+    static const bool off = [] {
+        const char* e = getenv("IMPEC_CONV_TMA");
+        return e && e[0] == '0';
+    }();
+    if (off || a.cin % 32 != 0 || !tmap_encoder()) return false;
+    const int W = a.W_, H = a.H;
+    if (W >= GB_M) {
+        if (W % GB_M) return false;
+        p.wbox = GB_M, p.hbox = 1, p.bbox = 1;
+    } else {
+        if (GB_M % W) return false;
+        const int hb = GB_M / W;
+        p.wbox = W;
+        if (hb >= H) {
+            if (hb % H) return false;
+            p.hbox = H, p.bbox = hb / H;
+        } else {
+            if (H % hb) return false;
+            p.hbox = hb, p.bbox = 1;
+        }
+    }
+    p.ks = a.cin % 64 == 0 ? 64 : 32;
+    const int stage = (GB_M + BN) * p.ks * 2;
+    p.stages = 200 * 1024 / stage;
+    if (p.stages > CT_MAX_STAGES) p.stages = CT_MAX_STAGES;
+    if (p.stages < 2) p.stages = 2;
+    return true;
+}
+
+template <int BN, int KS>
+static impec_status launch_conv_tma(const ConvArgs& a, const ConvTmaPlan& p, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_conv3x3_tma<BN, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            200 * 1024 + 1024));
+        attr = true;
+    }
+    TmapEncodeFn enc = tmap_encoder();
+    const CUtensorMapSwizzle sw = KS == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+    CUtensorMap tx, tw;
+    const cuuint64_t xd[4] = {(cuuint64_t)a.cin, (cuuint64_t)a.W_, (cuuint64_t)a.H, (cuuint64_t)a.B};
+    const cuuint64_t xs[3] = {(cuuint64_t)a.cin * 2, (cuuint64_t)a.W_ * a.cin * 2, (cuuint64_t)a.H * a.W_ * a.cin * 2};
+    const cuuint32_t xb[4] = {(cuuint32_t)KS, (cuuint32_t)p.wbox, (cuuint32_t)p.hbox, (cuuint32_t)p.bbox};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.X, xd, xs, xb, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+        set_error("conv: cuTensorMapEncodeTiled (activations) failed");
+        return IMPEC_ERR_CUDA;
+    }
+    const cuuint64_t wd[2] = {(cuuint64_t)a.Kp, (cuuint64_t)a.cout};
+    const cuuint64_t ws[1] = {(cuuint64_t)a.Kp * 2};
+    const cuuint32_t wb[2] = {(cuuint32_t)KS, (cuuint32_t)BN};
+    if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)a.W, wd, ws, wb, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+        set_error("conv: cuTensorMapEncodeTiled (weights) failed");
+        return IMPEC_ERR_CUDA;
+    }
+    const int M = a.B * a.H * a.W_;
+    const int smem = p.stages * (GB_M + BN) * KS * 2 + 1024;
+    dim3 g((a.cout + BN - 1) / BN, (M + GB_M - 1) / GB_M);
+    k_conv3x3_tma<BN, KS><<<g, CT_THREADS, smem, s>>>(tx, tw, a, p.stages);
+    IMPEC_CUDA_TRY(cudaGetLastError());
+    return IMPEC_OK;
+}
+
+template <int BN>
+static impec_status launch_conv_any(const ConvArgs& a, cudaStream_t s) {
+    ConvTmaPlan p;
+    if (conv_tma_plan(a, BN, p)) return p.ks == 64 ? launch_conv_tma<BN, 64>(a, p, s) : launch_conv_tma<BN, 32>(a, p, s);
+    return launch_conv_bn<BN>(a, s);
 }
 
 // The output-channel tile: the widest of 128, 64, 32 (not beyond cout) that still gives one
@@ -488,9 +692,9 @@ impec_status launch_conv(const ConvArgs& a, cudaStream_t s) {
     }
     const long long mt = ((long long)a.B * a.H * a.W_ + GB_M - 1) / GB_M;
     auto ctas = [&](int bn) { return mt * ((a.cout + bn - 1) / bn); };
-    if (a.cout >= 128 && ctas(128) >= sms) return launch_conv_bn<128>(a, s);
-    if (a.cout >= 64 && ctas(64) >= sms) return launch_conv_bn<64>(a, s);
-    return launch_conv_bn<32>(a, s);
+    if (a.cout >= 128 && ctas(128) >= sms) return launch_conv_any<128>(a, s);
+    if (a.cout >= 64 && ctas(64) >= sms) return launch_conv_any<64>(a, s);
+    return launch_conv_any<32>(a, s);
 }
 
 impec_status launch_wgrad(const __nv_bfloat16* dZ, const __nv_bfloat16* X, int B, int H, int W_, int cin, int cout,

@@ -97,30 +97,45 @@ __device__ __forceinline__ float gelu_d(float x) {
     return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 
+// 2x2 average pooling and nearest 2x upsampling, 8 channels (16 bytes) per thread; C is a
+// multiple of 8.
 __global__ void k_pool2(const __nv_bfloat16* __restrict__ in, int B, int h, int w, int C, __nv_bfloat16* __restrict__ out) {
-    const size_t n = (size_t)B * h * w * C;  // output elements, h x w = the pooled size
+    const int C8 = C >> 3;
+    const size_t n = (size_t)B * h * w * C8;  // output vectors, h x w = the pooled size
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        size_t t = i / C;
+        const int c8 = (int)(i % C8);
+        size_t t = i / C8;
         const int x = (int)(t % w);
         t /= w;
         const int y = (int)(t % h), b = (int)(t / h);
         const size_t W2 = 2 * (size_t)w, r0 = ((size_t)b * 2 * h + 2 * y) * W2 + 2 * x;
-        const float s = bf(in[r0 * C + c]) + bf(in[(r0 + 1) * C + c]) + bf(in[(r0 + W2) * C + c]) +
-                        bf(in[(r0 + W2 + 1) * C + c]);
-        out[i] = __float2bfloat16(0.25f * s);
+        const size_t src[4] = {r0, r0 + 1, r0 + W2, r0 + W2 + 1};
+        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            __align__(16) __nv_bfloat16 v[8];
+            *reinterpret_cast<uint4*>(v) = *reinterpret_cast<const uint4*>(in + src[q] * C + 8 * c8);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) acc[k] += bf(v[k]);
+        }
+        __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o[k] = __float2bfloat16(0.25f * acc[k]);
+        *reinterpret_cast<uint4*>(out + i * 8) = *reinterpret_cast<const uint4*>(o);
     }
 }
 
 __global__ void k_up2(const __nv_bfloat16* __restrict__ in, int B, int h, int w, int C, __nv_bfloat16* __restrict__ out) {
-    const size_t n = (size_t)B * 2 * h * 2 * w * C;
+    const int C8 = C >> 3;
+    const size_t n = (size_t)B * 2 * h * 2 * w * C8;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        size_t t = i / C;
+        const int c8 = (int)(i % C8);
+        size_t t = i / C8;
         const int x = (int)(t % (2 * w));
         t /= 2 * w;
         const int y = (int)(t % (2 * h)), b = (int)(t / (2 * h));
-        out[i] = in[(((size_t)b * h + y / 2) * w + x / 2) * C + c];
+        *reinterpret_cast<uint4*>(out + i * 8) =
+            *reinterpret_cast<const uint4*>(in + (((size_t)b * h + y / 2) * w + x / 2) * C + 8 * c8);
     }
 }
 
@@ -416,12 +431,12 @@ static impec_status net_forward(impec_net* net, const NetBuffers& nb, const __nv
     for (int l = 0; l < NET_LAYERS; ++l) {
         IMPEC_TRY(conv_forward(net, nb, X, l, train, s));
         switch (l) {
-            case 1: k_pool2<<<egrid(level_pixels(nb, 1) * 32), 256, 0, s>>>(nb.y[1], B, H >> 1, W >> 1, 32, nb.d1); break;
-            case 3: k_pool2<<<egrid(level_pixels(nb, 2) * 64), 256, 0, s>>>(nb.y[3], B, H >> 2, W >> 2, 64, nb.d2); break;
-            case 5: k_pool2<<<egrid(level_pixels(nb, 3) * 128), 256, 0, s>>>(nb.y[5], B, H >> 3, W >> 3, 128, nb.d3); break;
-            case 7: k_up2<<<egrid(level_pixels(nb, 2) * 256), 256, 0, s>>>(nb.y[7], B, H >> 3, W >> 3, 256, nb.u2); break;
-            case 9: k_up2<<<egrid(level_pixels(nb, 1) * 128), 256, 0, s>>>(nb.y[9], B, H >> 2, W >> 2, 128, nb.u1); break;
-            case 11: k_up2<<<egrid(level_pixels(nb, 0) * 64), 256, 0, s>>>(nb.y[11], B, H >> 1, W >> 1, 64, nb.u0); break;
+            case 1: k_pool2<<<egrid(level_pixels(nb, 1) * 4), 256, 0, s>>>(nb.y[1], B, H >> 1, W >> 1, 32, nb.d1); break;
+            case 3: k_pool2<<<egrid(level_pixels(nb, 2) * 8), 256, 0, s>>>(nb.y[3], B, H >> 2, W >> 2, 64, nb.d2); break;
+            case 5: k_pool2<<<egrid(level_pixels(nb, 3) * 16), 256, 0, s>>>(nb.y[5], B, H >> 3, W >> 3, 128, nb.d3); break;
+            case 7: k_up2<<<egrid(level_pixels(nb, 2) * 32), 256, 0, s>>>(nb.y[7], B, H >> 3, W >> 3, 256, nb.u2); break;
+            case 9: k_up2<<<egrid(level_pixels(nb, 1) * 16), 256, 0, s>>>(nb.y[9], B, H >> 2, W >> 2, 128, nb.u1); break;
+            case 11: k_up2<<<egrid(level_pixels(nb, 0) * 8), 256, 0, s>>>(nb.y[11], B, H >> 1, W >> 1, 64, nb.u0); break;
             default: break;
         }
         IMPEC_CUDA_TRY(cudaGetLastError());

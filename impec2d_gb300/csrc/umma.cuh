@@ -27,6 +27,20 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes
     return d;
 }
 
+// Descriptor of a K-major tile written by TMA with 128- or 64-byte swizzling: rows of 128
+// (64) bytes, 8-row atoms of 1024 (512) bytes stacked along M/N (stride byte offset), layout
+// code 2 (128B) or 4 (64B) in bits 61-63.  A K step of 16 bf16 inside the atom advances the
+// start address by 32 bytes.
+__device__ __forceinline__ uint64_t smem_desc_sw(uint32_t saddr, int row_bytes) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;                                   // leading byte offset: unused for swizzled K-major
+    d |= (uint64_t)(((uint32_t)(8 * row_bytes) >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)(row_bytes == 128 ? 2 : 4) << 61;
+    return d;
+}
+
 // Instruction descriptor of kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9 and
 // 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
@@ -103,12 +117,40 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
     return false;
 }
 
+// mbarrier arrive by this thread, announcing tx_bytes of TMA data for the current phase.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t tx_bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(tx_bytes)
+                 : "memory");
+}
+
+// TMA tiled loads (global -> shared, completion counted in bytes on the mbarrier).  The tensor
+// map is a __grid_constant__ kernel parameter; coordinates are element indices, innermost first.
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int c0, int c1, uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_u32(dst)), "l"(tmap), "r"(c0), "r"(c1), "r"(smem_u32(mbar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, int c0, int c1, int c2, int c3,
+                                            uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(smem_u32(dst)),
+        "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(mbar))
+        : "memory");
+}
+
 // 16-byte asynchronous global -> shared copy; src_bytes < 16 zero-fills the rest.
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t src_bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Arrive on the mbarrier (without raising its expected count) once all of this thread's prior
+// cp.async copies have landed.
+__device__ __forceinline__ void cp_async_mbar_arrive(uint64_t* mbar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
 // Close the group of this thread's outstanding cp.async; wait until at most N groups are pending.
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>

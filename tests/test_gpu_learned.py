@@ -51,12 +51,17 @@ def _w4(Wt, cin, cout):
     return Wt[:, :9 * cin].float().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2).contiguous()
 
 
-@pytest.mark.parametrize("B,H,W,cin,cout", [(2, 20, 20, 8, 32), (1, 37, 29, 32, 64), (2, 16, 24, 64, 256),
-                                            (1, 12, 12, 128, 128)])
+@pytest.mark.parametrize("B,H,W,cin,cout", [
+    # cp.async staging: 8 channels, or widths that do not tile 128 pixels
+    (2, 20, 20, 8, 32), (1, 37, 29, 32, 64), (2, 16, 24, 64, 256), (1, 12, 12, 128, 128),
+    # TMA staging: rows of 128 pixels, several rows per box, whole images per box; 32 / 64 channel stages
+    (1, 64, 128, 32, 32), (1, 16, 256, 64, 64), (2, 16, 16, 64, 128), (1, 8, 8, 32, 64), (3, 4, 4, 256, 256),
+    (2, 32, 32, 128, 256)])
 def test_conv3x3_forward_and_gradients(engine, B, H, W, cin, cout):
     """Implicit-GEMM convolution on tcgen05: forward (linear; GELU with a skip add), input
     gradient (plain; times gelu'(z) with an added gradient) and weight gradient, against
-    PyTorch fp32 conv2d / autograd of the same bf16 inputs."""
+    PyTorch fp32 conv2d / autograd of the same bf16 inputs.  Shapes cover both operand
+    stagings (cp.async gathers and TMA boxes with zero-filled halos)."""
     import torch
     import torch.nn.functional as F
     E = engine
