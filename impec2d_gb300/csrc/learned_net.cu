@@ -738,9 +738,9 @@ extern "C" impec_status impec_learned_attach(impec_ctx* ctx, impec_net* net, int
     learned_release(ctx);
     if (!net || mode == 0) return IMPEC_OK;
     const int N1 = ctx->P.N1, N2 = ctx->P.N2;
-    if ((mode != 1 && mode != 2) || (factor != 1 && factor != 2 && factor != 4 && factor != 8) ||
+    if ((mode != 1 && mode != 2) || (factor != 1 && factor != 2 && factor != 4 && factor != 8 && factor != 16) ||
         N1 % (8 * factor) != 0 || N2 % (8 * factor) != 0) {
-        set_error("impec_learned_attach: mode 1 or 2, factor 1, 2, 4 or 8 with N1 and N2 multiples of 8 * factor");
+        set_error("impec_learned_attach: mode 1 or 2, factor 1, 2, 4, 8 or 16 with N1 and N2 multiples of 8 * factor");
         return IMPEC_ERR_ARG;
     }
     if (!ctx->singular || !ctx->P.warm_start) {

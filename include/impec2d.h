@@ -241,7 +241,7 @@ impec_status impec_net_parameters(impec_net* net, float* host_out, const float* 
  * NULL or mode 0).  Needs warm_start (x0 = the previous pressure) and a well-driven pure-Neumann
  * system.  Each solve then computes r0 = f - A x0 and the features [mean 4 log(1-c+M^(1/4)c),
  * mean log K, sum q dA/I, centred x0 / RMS, r0 / RMS] over factor x factor cells (factor 1, 2,
- * 4 or 8; N1 and N2 multiples of 8 * factor).  Predicting, the network's output d (bilinear to
+ * 4, 8 or 16; N1 and N2 multiples of 8 * factor).  Predicting, the network's output d (bilinear to
  * the fine grid) moves the iterate: x0 += alpha d, alpha = (r0, d) / (d, A d); the solve still
  * converges to its tolerance.  The captured step graph is rebuilt at the next step. */
 impec_status impec_learned_attach(impec_ctx* ctx, impec_net* net, int factor, int mode);

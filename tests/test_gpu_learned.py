@@ -238,3 +238,37 @@ def test_learned_attach_rejections(engine):
         net.attach(ctx, factor=3, mode=1)
     ctx.close()
     net.close()
+
+
+def test_trained_network_saves_cycles_over_the_previous_step(engine):
+    """What the learned part gains: a network trained (AdamW, the engine's kernels) on pairs that
+    the solver wrote from 64^2 realisations starts held-out solves closer to the solution than
+    the previous pressure alone, so they need fewer V-cycles to the same 1e-10 (counted over the
+    same IMPES steps of three held-out realisations run side by side)."""
+    from impec2d_gb300 import learned as LW
+    from impec2d_gb300.workloads import realisation
+    E = engine
+    N, ell = 64, 4.0
+    X, T, _ = LW.generate_pairs(E, 16, 40, N=N, every=2, skip=2, ell=ell)
+    net = E.Net(seed=5)
+    v0 = LW.validation_mse(net, X[:40], T[:40])
+    LW.train(net, X[40:], T[40:], epochs=25, batch=32, lr=1e-3, weight_decay=1e-4, evals=1)
+    v1 = LW.validation_mse(net, X[:40], T[:40])
+    assert v1 < 0.5 * v0, (v0, v1)
+    its = {"previous": 0, "learned": 0}
+    for seed in (100, 101, 102):
+        runs = {k: realisation(E, N, seed, precision="mixed", ell=ell, warm_start=1) for k in its}
+        for cx in runs.values():
+            cx.run_steps(3)
+        net.attach(runs["learned"], factor=1, mode=1)
+        for _ in range(12):
+            for k, cx in runs.items():
+                info = cx.step()
+                assert info.relres <= 1e-10
+                its[k] += info.its
+        E.Net.detach(runs["learned"])
+        for cx in runs.values():
+            cx.close()
+    print(f"validation MSE {v0:.3f} -> {v1:.3f}; V-cycles over 36 solves: {its}")
+    assert its["learned"] < its["previous"], its
+    net.close()
