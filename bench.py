@@ -65,6 +65,11 @@ def parse():
     ap.add_argument("--eval-samples", type=int, default=8, help="learned study: timed solves per realisation")
     ap.add_argument("--eval-skip", type=int, default=20, help="learned study: IMPES steps before the first solve")
     ap.add_argument("--eval-every", type=int, default=10, help="learned study: IMPES steps between solves")
+    ap.add_argument("--eval-factor", type=int, default=0,
+                    help="learned study: feature averaging factor (default N / 256, the training grid)")
+    ap.add_argument("--eval-ell", type=float, default=0.0,
+                    help="learned study: permeability correlation length in cells (default 16 N / 256, the "
+                         "training fields' length relative to the domain)")
     return ap.parse_args()
 
 
@@ -459,8 +464,8 @@ def study_learned(args):
              ("fp64", "learned")]
     evals = {}
     for N in [int(x) for x in args.eval_sizes.split(",")]:
-        factor = max(1, N // 256)
-        ell = 16.0 * N / 256
+        factor = args.eval_factor or max(1, N // 256)
+        ell = args.eval_ell or 16.0 * N / 256
         res = {f"{p}/{g}": {"cycles": [], "ms": [], "alpha": [], "relres0": []} for p, g in modes}
         for si in range(args.eval_seeds):
             seed = 10000 + si

@@ -243,23 +243,26 @@ __global__ void __launch_bounds__(256) k_learn_pool(int n1, int n2, int f, const
     const size_t m = (size_t)h * w;
     double acc[3] = {0.0, 0.0, 0.0};
     const double inv = 1.0 / ((double)f * f);
+    const float m14f = (float)m14;
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x) {
         const int I = (int)(k / w), J = (int)(k % w);
-        double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        // the logarithms in FP32 (the features are stored in bf16; FP64 transcendentals are slow)
+        float lm = 0.0f, lk = 0.0f;
+        double s[3] = {0.0, 0.0, 0.0};
         for (int a = 0; a < f; ++a)
             for (int b = 0; b < f; ++b) {
                 const size_t g = (size_t)(I * f + a) * n2 + (size_t)J * f + b;
-                const double cg = c[g];
-                s[0] += 4.0 * log(1.0 - cg + m14 * cg);
-                s[1] += K ? log(K[g]) : 0.0;
-                s[2] += q[g];
-                s[3] += x[g];
-                s[4] += r[g];
+                const float cg = (float)c[g];
+                lm += 4.0f * logf(1.0f - cg + m14f * cg);
+                lk += K ? logf((float)K[g]) : 0.0f;
+                s[0] += q[g];
+                s[1] += x[g];
+                s[2] += r[g];
             }
-        const double xm = s[3] * inv, rm = s[4] * inv;
-        raw[k * 5 + 0] = (float)(s[0] * inv);
-        raw[k * 5 + 1] = (float)(s[1] * inv);
-        raw[k * 5 + 2] = (float)(s[2] * qnorm);
+        const double xm = s[1] * inv, rm = s[2] * inv;
+        raw[k * 5 + 0] = (float)(lm * inv);
+        raw[k * 5 + 1] = (float)(lk * inv);
+        raw[k * 5 + 2] = (float)(s[0] * qnorm);
         raw[k * 5 + 3] = (float)xm;
         raw[k * 5 + 4] = (float)rm;
         acc[0] += xm;
