@@ -323,10 +323,18 @@ __global__ void __launch_bounds__(CV_THREADS) k_conv3x3(ConvArgs a) {
 // TMA variant for cin a multiple of 32 and tiles of whole image rows (see conv_tma_plan): one
 // K stage is one tap's KS-channel slice (KS = 64: 128-byte swizzle; KS = 32: 64-byte swizzle).
 // The activation tile of a stage is one 4D box (KS channels x wbox x hbox x bbox pixels = the
-// CTA's 128 output pixels) at the tap's offset, zero-filled outside the image by the TMA; the
-// weight tile is one 2D box.  Lane 0 of warp 4 issues both loads per stage on the stage's "full"
-// mbarrier (expected bytes); lane 0 of warp 5 issues the MMAs and commits them to "empty";
-// warps 0-3 run the epilogue.  Stages: as many as fit in 200 KB (at most 8).
+// 128 output pixels of the tile) at the tap's offset, zero-filled outside the image by the
+// TMA; the weight tile is one 2D box.
+//
+// Persistent: each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ... with the
+// accumulator double-buffered in TMEM, so that the loads and MMAs of tile i+1 overlap the
+// epilogue of tile i.  Roles: lane 0 of warp 4 issues both loads of every stage on the
+// stage's "full" mbarrier (expected bytes); lane 0 of warp 5 waits for the accumulator buffer
+// to be free ("tmem_empty", one arrival per epilogue warp), issues the MMAs of each stage,
+// commits them to the stage's "empty" mbarrier and, after a tile's last stage, to the
+// buffer's "tmem_full"; warps 0-3 wait for "tmem_full", run the epilogue and release the
+// buffer.  Stages: as many as fit in 200 KB (at most 8).  Stage and buffer uses are counted
+// across tiles, which gives every wait its phase parity.
 constexpr int CT_THREADS = 192, CT_MAX_STAGES = 8;
 
 struct ConvTmaPlan {
@@ -339,19 +347,23 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
                                                             int stages) {
     extern __shared__ __align__(1024) unsigned char ct_smem[];
     constexpr int A_BYTES = GB_M * KS * 2, B_BYTES = BN * KS * 2, STAGE = A_BYTES + B_BYTES;
-    __shared__ uint64_t full[CT_MAX_STAGES], empty[CT_MAX_STAGES], done;
+    constexpr uint32_t TC = BN < 32 ? 32 : BN;  // TMEM columns of one accumulator buffer
+    __shared__ uint64_t full[CT_MAX_STAGES], empty[CT_MAX_STAGES], tfull[2], tempty[2], done;
     __shared__ uint32_t tslot;
     __shared__ volatile int fail, tma_issued;
-    constexpr uint32_t TCOLS = BN < 32 ? 32 : BN;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int M = a.B * a.H * a.W_;
-    const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * BN;
+    const int mt = (M + GB_M - 1) / GB_M, nt = (a.cout + BN - 1) / BN, tiles = mt * nt;
     unsigned char* base = ct_smem + ((1024 - (umma::smem_u32(ct_smem) & 1023)) & 1023);  // 1024-byte aligned
-    if (warp == 0) umma::tmem_alloc(&tslot, TCOLS);
+    if (warp == 0) umma::tmem_alloc(&tslot, 2 * TC);
     if (tid == 0) {
         for (int st = 0; st < stages; ++st) {
             umma::mbar_init(&full[st], 1);
             umma::mbar_init(&empty[st], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            umma::mbar_init(&tfull[b], 1);
+            umma::mbar_init(&tempty[b], 4);
         }
         umma::mbar_init(&done, 1);
         fail = 0;
@@ -361,63 +373,87 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
     __syncthreads();
     umma::fence_after();
     const uint32_t tmem = tslot;
-    const int cs = a.cin / KS, nk = 9 * cs;
+    const int cs = a.cin / KS, nk = 9 * cs, hw = a.H * a.W_;
     if (warp == 4) {
         if (lane == 0) {  // TMA producer
-            const int hw = a.H * a.W_, b0 = m0 / hw, rem = m0 - b0 * hw, y0 = rem / a.W_, x0 = rem - y0 * a.W_;
-            for (int kt = 0; kt < nk; ++kt) {
-                const int slot = kt % stages, use = kt / stages;
-                if (use > 0 && !umma::mbar_wait(&empty[slot], (uint32_t)((use - 1) & 1), GB_WAIT_TRIES)) {
-                    fail = 1;
-                    break;
+            int g = 0;
+            for (int t = blockIdx.x; t < tiles && !fail; t += gridDim.x) {
+                const int m0 = (t / nt) * GB_M, n0 = (t % nt) * BN;
+                const int b0 = m0 / hw, rem = m0 - b0 * hw, y0 = rem / a.W_, x0 = rem - y0 * a.W_;
+                for (int kt = 0; kt < nk; ++kt, ++g) {
+                    const int slot = g % stages, use = g / stages;
+                    if (use > 0 && !umma::mbar_wait(&empty[slot], (uint32_t)((use - 1) & 1), GB_WAIT_TRIES)) {
+                        fail = 1;
+                        break;
+                    }
+                    const int tap = kt / cs, c0 = (kt - tap * cs) * KS;
+                    const int dy = a.tapsign * (tap / 3 - 1), dx = a.tapsign * (tap % 3 - 1);
+                    unsigned char* sA = base + slot * STAGE;
+                    umma::mbar_expect_tx(&full[slot], (uint32_t)STAGE);
+                    umma::tma_load_4d(sA, &tx, c0, x0 + dx, y0 + dy, b0, &full[slot]);
+                    umma::tma_load_2d(sA + A_BYTES, &tw, tap * a.cin + c0, n0, &full[slot]);
+                    tma_issued = g + 1;
                 }
-                const int tap = kt / cs, c0 = (kt - tap * cs) * KS;
-                const int dy = a.tapsign * (tap / 3 - 1), dx = a.tapsign * (tap % 3 - 1);
-                unsigned char* sA = base + slot * STAGE;
-                umma::mbar_expect_tx(&full[slot], (uint32_t)STAGE);
-                umma::tma_load_4d(sA, &tx, c0, x0 + dx, y0 + dy, b0, &full[slot]);
-                umma::tma_load_2d(sA + A_BYTES, &tw, tap * a.cin + c0, n0, &full[slot]);
-                tma_issued = kt + 1;
             }
         }
         __syncwarp();
     } else if (warp == 5) {
         if (lane == 0) {  // MMA issuer
             const uint32_t idesc = umma::idesc_bf16_f32(GB_M, BN);
-            for (int kt = 0; kt < nk; ++kt) {
-                const int slot = kt % stages, use = kt / stages;
-                if (!umma::mbar_wait(&full[slot], (uint32_t)(use & 1), GB_WAIT_TRIES)) {
+            int g = 0, i = 0;
+            for (int t = blockIdx.x; t < tiles && !fail; t += gridDim.x, ++i) {
+                const int buf = i & 1, buse = i >> 1;
+                if (buse > 0 && !umma::mbar_wait(&tempty[buf], (uint32_t)((buse - 1) & 1), GB_WAIT_TRIES)) {
                     fail = 1;
-                    // let the loads already issued land before the CTA ends (bounded)
-                    for (int j = kt + 1; j < tma_issued; ++j)
-                        umma::mbar_wait(&full[j % stages], (uint32_t)((j / stages) & 1), GB_WAIT_TRIES >> 4);
                     break;
                 }
                 umma::fence_after();
-                const uint32_t sa = umma::smem_u32(base + slot * STAGE);
+                const uint32_t acc = tmem + (uint32_t)buf * TC;
+                for (int kt = 0; kt < nk; ++kt, ++g) {
+                    const int slot = g % stages, use = g / stages;
+                    if (!umma::mbar_wait(&full[slot], (uint32_t)(use & 1), GB_WAIT_TRIES)) {
+                        fail = 1;
+                        break;
+                    }
+                    umma::fence_after();
+                    const uint32_t sa = umma::smem_u32(base + slot * STAGE);
 #pragma unroll
-                for (int ks = 0; ks < KS / 16; ++ks) {
-                    const uint64_t ad = umma::smem_desc_sw(sa + ks * 32, KS * 2);
-                    const uint64_t bd = umma::smem_desc_sw(sa + A_BYTES + ks * 32, KS * 2);
-                    umma::mma_bf16(tmem, ad, bd, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+                    for (int ks = 0; ks < KS / 16; ++ks) {
+                        const uint64_t ad = umma::smem_desc_sw(sa + ks * 32, KS * 2);
+                        const uint64_t bd = umma::smem_desc_sw(sa + A_BYTES + ks * 32, KS * 2);
+                        umma::mma_bf16(acc, ad, bd, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+                    }
+                    umma::commit(&empty[slot]);
                 }
-                umma::commit(&empty[slot]);
+                if (fail) break;
+                umma::commit(&tfull[buf]);
             }
-            umma::commit(&done);
+            if (fail)  // let the loads already issued land before the CTA ends (bounded)
+                for (int j = g; j < tma_issued; ++j)
+                    umma::mbar_wait(&full[j % stages], (uint32_t)((j / stages) & 1), GB_WAIT_TRIES >> 4);
+            umma::commit(&done);  // completes once every MMA issued above has
+            umma::mbar_wait(&done, 0u, GB_WAIT_TRIES);
         }
         __syncwarp();
+    } else {  // warps 0-3: epilogue
+        int i = 0;
+        for (int t = blockIdx.x; t < tiles && !fail; t += gridDim.x, ++i) {
+            const int buf = i & 1, buse = i >> 1;
+            if (!umma::mbar_wait(&tfull[buf], (uint32_t)(buse & 1), GB_WAIT_TRIES)) {
+                fail = 1;
+                break;
+            }
+            umma::fence_after();
+            conv_epilogue<BN>(a, tmem + (uint32_t)buf * TC, (t / nt) * GB_M, (t % nt) * BN, warp, lane, M);
+            umma::fence_before();
+            __syncwarp();
+            if (lane == 0) umma::mbar_arrive(&tempty[buf]);
+        }
     }
-    const bool fin = warp < 4 ? umma::mbar_wait(&done, 0u, GB_WAIT_TRIES) : true;
-    const bool ok = __syncthreads_and(fin) != 0 && fail == 0;
-    if (ok && warp < 4) {
-        umma::fence_after();
-        conv_epilogue<BN>(a, tmem, m0, n0, warp, lane, M);
-    }
-    if (!ok && tid == 0) atomicExch(a.err, 1);
-    umma::fence_before();
     __syncthreads();
+    if (fail && tid == 0) atomicExch(a.err, 1);
     umma::fence_after();
-    if (warp == 0) umma::tmem_free(tmem, TCOLS);
+    if (warp == 0) umma::tmem_free(tmem, 2 * TC);
 }
 
 // Weights of the input-gradient convolution: Wd[ci][tap * cout + co] = W[co][tap * cin + ci],
@@ -668,8 +704,16 @@ static impec_status launch_conv_tma(const ConvArgs& a, const ConvTmaPlan& p, cud
     }
     const int M = a.B * a.H * a.W_;
     const int smem = p.stages * (GB_M + BN) * KS * 2 + 1024;
-    dim3 g((a.cout + BN - 1) / BN, (M + GB_M - 1) / GB_M);
-    k_conv3x3_tma<BN, KS><<<g, CT_THREADS, smem, s>>>(tx, tw, a, p.stages);
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const long long tiles = (long long)((M + GB_M - 1) / GB_M) * ((a.cout + BN - 1) / BN);
+    const int per_sm = smem <= 110 * 1024 ? 2 : 1;  // resident CTAs per SM (shared memory)
+    const int grid = (int)(tiles < (long long)sms * per_sm ? tiles : (long long)sms * per_sm);
+    k_conv3x3_tma<BN, KS><<<grid, CT_THREADS, smem, s>>>(tx, tw, a, p.stages);
     IMPEC_CUDA_TRY(cudaGetLastError());
     return IMPEC_OK;
 }

@@ -117,6 +117,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
     return false;
 }
 
+// Plain arrive of this thread on the mbarrier.
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
 // mbarrier arrive by this thread, announcing tx_bytes of TMA data for the current phase.
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t tx_bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(tx_bytes)
