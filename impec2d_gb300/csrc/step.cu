@@ -334,10 +334,9 @@ impec_status impec_launch_count(impec_ctx* ctx, long long* n) {
 impec_status impec_state_upload(impec_ctx* ctx, const double* c_host, const double* q_host, int g) {
     if (!ctx || g < 0) return IMPEC_ERR_ARG;
     const int N1 = ctx->P.N1, N2 = ctx->P.N2, w = N2 + 2 * g;
-    std::vector<double> buf((size_t)N1 * N2);
-    if (c_host) {
-        for (int i = 0; i < N1; ++i) std::memcpy(&buf[IX(i, 0, N2)], c_host + (size_t)(i + g) * w + g, N2 * 8);
-        IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->c, buf.data(), buf.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    if (c_host) {  // interior rows straight from the ghosted host array (one strided copy)
+        IMPEC_CUDA_TRY(cudaMemcpy2DAsync(ctx->c, (size_t)N2 * 8, c_host + (size_t)g * w + g, (size_t)w * 8,
+                                         (size_t)N2 * 8, N1, cudaMemcpyHostToDevice, ctx->stream));
         IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     }
     if (q_host) {
@@ -350,15 +349,14 @@ impec_status impec_state_upload(impec_ctx* ctx, const double* c_host, const doub
 impec_status impec_state_download(impec_ctx* ctx, double* c_host, double* p_host, double* v_host, int g) {
     if (!ctx || g < 0) return IMPEC_ERR_ARG;
     const int N1 = ctx->P.N1, N2 = ctx->P.N2, w = N2 + 2 * g;
-    std::vector<double> buf((size_t)N1 * N2);
-    auto get = [&](const double* dev, double* host) -> impec_status {
-        IMPEC_CUDA_TRY(cudaMemcpyAsync(buf.data(), dev, buf.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
-        IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-        for (int i = 0; i < N1; ++i) std::memcpy(host + (size_t)(i + g) * w + g, &buf[IX(i, 0, N2)], N2 * 8);
+    auto get = [&](const double* dev, double* host) -> impec_status {  // interior rows, one strided copy
+        IMPEC_CUDA_TRY(cudaMemcpy2DAsync(host + (size_t)g * w + g, (size_t)w * 8, dev, (size_t)N2 * 8, (size_t)N2 * 8,
+                                         N1, cudaMemcpyDeviceToHost, ctx->stream));
         return IMPEC_OK;
     };
     if (c_host) IMPEC_TRY(get(ctx->c, c_host));
     if (p_host) IMPEC_TRY(get(ctx->p, p_host));
+    if (c_host || p_host) IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     if (v_host) {
         const int wv = N2 + 1 + 2 * g;
         std::vector<double> hu((size_t)(N1 + 1) * N2), hv((size_t)N1 * (N2 + 1));
