@@ -74,7 +74,8 @@ def parse():
 
 
 def dist_info():
-    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+    from impec2d_gb300.replicas import dist_info as _d
+    return _d()
 
 
 def initial_state(N, seed=1234):
@@ -314,33 +315,45 @@ def study_ensemble(args):
             tuned[N] = {n: probe.get_tuning(n) for n in ("mg_pre", "mg_post", "cluster")}
             tuned[N]["report"] = rep.strip().splitlines()[-1]
             probe.close()
+    from impec2d_gb300.replicas import dist_info, max_over_ranks, shard
+    rank, world, local = dist_info()
+    if world > 1:  # members dealt to ranks by index; no exchange between ranks
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    listing = [(N, i) for N in sizes for i in range(k)]
     members = []
-    for N in sizes:
-        for i in range(k):
-            ctx = ensemble_member(E, N, i)
-            for name, v in tuned.get(N, {}).items():
-                if name != "report":
-                    ctx.set_tuning(name, v)
-            members.append((N, ctx))
-    cells = sum(N * N for N, _ in members)
+    for j in shard(len(listing), rank, world):
+        N, i = listing[j]
+        ctx = ensemble_member(E, N, i)
+        for name, v in tuned.get(N, {}).items():
+            if name != "report":
+                ctx.set_tuning(name, v)
+        members.append((N, ctx))
+    cells = sum(N * N for N, _ in listing)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
     t0 = time.perf_counter()
     ens = E.Ensemble([c for _, c in members])
     t_capture = time.perf_counter() - t0
     ens.step(args.warmup)
-    torch.cuda.synchronize()
+    barrier()
     t0 = time.perf_counter()
     ens.step(args.steps)
-    t_ens = time.perf_counter() - t0
+    barrier()
+    t_ens = max_over_ranks(time.perf_counter() - t0, device="cuda")
     # the same members one after another (each its own graph launch per step)
     for _, c in members:
         c.run_steps(1)
-    torch.cuda.synchronize()
+    barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         for _, c in members:
             c.run_steps(1)
-    torch.cuda.synchronize()
-    t_seq = time.perf_counter() - t0
+    barrier()
+    t_seq = max_over_ranks(time.perf_counter() - t0, device="cuda")
     out = {"study": "ensemble",
            "workload": f"{len(members)} realisations, {k} each at 128^2, 256^2, 384^2, 512^2; lognormal K "
                        f"(sigma 0.5), M in {{5,20,41,100}}, diagonal/parallel by seed; MUSCL + Peaceman; "
@@ -349,8 +362,10 @@ def study_ensemble(args):
            "ensemble": {"cell_steps_per_s": cells * args.steps / t_ens, "ms_per_step": 1e3 * t_ens / args.steps,
                         "capture_s": t_capture},
            "one_after_another": {"cell_steps_per_s": cells * args.steps / t_seq, "ms_per_step": 1e3 * t_seq / args.steps},
-           "speedup": t_seq / t_ens, "autotune": tuned or None, "data": "synthetic (seeded GRF permeability)"}
-    print(json.dumps(out))
+           "speedup": t_seq / t_ens, "autotune": tuned or None, "data": "synthetic (seeded GRF permeability)",
+           "n_gpus": world, "scaling": "strong (members dealt to ranks)"}
+    if rank == 0:
+        print(json.dumps(out))
     ens.close()
     for _, c in members:
         c.close()
@@ -595,13 +610,10 @@ def main():
     step_ms = [a.elapsed_time(b) for a, b in times]
     launches = E.launch_count(ctx) - launches0
     info = ctx.step()  # one more (untimed) step for the solver statistics
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    from impec2d_gb300.replicas import max_over_ranks, whole_job_rate
+    total_ms = max_over_ranks(sum(step_ms), device="cuda")
     ms = total_ms / args.steps
-    value = N * N * args.steps * world / (total_ms * 1e-3)
+    value = whole_job_rate(N * N * args.steps, total_ms * 1e-3, world)
 
     # end to end through the host-buffer C ABI: pinned host c in, c and p out, every step
     e2e = None
@@ -617,9 +629,9 @@ def main():
             ctx.run_steps(1)
             ctx.download(hc, hp, None, ghost=g)
         barrier()
-        te = time.perf_counter() - t0
-        e2e = {"value": N * N * args.steps * world / te, "unit": "cell-steps/s", "h2d_bytes_per_step": N * N * 8,
-               "d2h_bytes_per_step": 2 * N * N * 8}
+        te = max_over_ranks(time.perf_counter() - t0, device="cuda")
+        e2e = {"value": whole_job_rate(N * N * args.steps, te, world), "unit": "cell-steps/s",
+               "h2d_bytes_per_step": N * N * 8, "d2h_bytes_per_step": 2 * N * N * 8}
 
     # ms per pressure solve to 1e-10 on the current state: plain FP64 MG vs mixed precision
     pressure = {}
