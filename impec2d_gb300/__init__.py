@@ -374,7 +374,7 @@ class Context:
 
     def close(self):
         if self.h:
-            lib().impec_ctx_destroy(self.h)
+            _chk(lib().impec_ctx_destroy(self.h), "ctx_destroy")
             self.h = None
 
     def __del__(self):

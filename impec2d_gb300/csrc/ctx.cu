@@ -91,6 +91,15 @@ impec_status sync_scalars(impec_ctx* ctx) {
 
 using namespace impec;
 
+namespace impec {
+bool buffers_movable(const impec_ctx* ctx, const char* what) {
+    if (ctx->ensembles == 0) return true;
+    set_error(std::string(what) + ": the context belongs to a live ensemble whose graph holds its buffers "
+                                  "(destroy the ensemble first)");
+    return false;
+}
+}  // namespace impec
+
 extern "C" {
 
 const char* impec_last_error(void) { return g_err.c_str(); }
@@ -210,6 +219,7 @@ impec_status impec_ctx_create(const impec_params* P, void* stream, impec_ctx** o
 
 impec_status impec_ctx_destroy(impec_ctx* ctx) {
     if (!ctx) return IMPEC_OK;
+    if (!buffers_movable(ctx, "impec_ctx_destroy")) return IMPEC_ERR_ARG;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream); else cudaDeviceSynchronize();
     invalidate_step_graph(ctx);
     learned_release(ctx);
@@ -238,8 +248,16 @@ impec_status impec_ctx_params(const impec_ctx* ctx, impec_params* P) {
 
 impec_status impec_set_permeability(impec_ctx* ctx, const double* K11, const double* K22) {
     if (!ctx) return IMPEC_ERR_ARG;
-    invalidate_step_graph(ctx);
     const size_t n = (size_t)ctx->P.N1 * ctx->P.N2;
+    const bool aniso = K22 && K22 != K11, was_aniso = ctx->K22 && ctx->K22 != ctx->K11;
+    if (K11 && ctx->K11 && aniso == was_aniso) {  // same layout: new values in place (graphs stay valid)
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->K11, K11, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (aniso) IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->K22, K22, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        return IMPEC_OK;
+    }
+    if (!buffers_movable(ctx, "impec_set_permeability")) return IMPEC_ERR_ARG;
+    invalidate_step_graph(ctx);
     if (ctx->K22 && ctx->K22 != ctx->K11) cudaFree(ctx->K22);
     if (ctx->K11) cudaFree(ctx->K11);
     ctx->K11 = ctx->K22 = nullptr;
@@ -280,6 +298,7 @@ impec_status impec_set_source(impec_ctx* ctx, const double* q_dev) {
             IMPEC_CUDA_TRY(cudaMemcpy(ctx->well_q, val.data(), val.size() * 8, cudaMemcpyHostToDevice));
         return IMPEC_OK;
     }
+    if (!buffers_movable(ctx, "impec_set_source (new well cells)")) return IMPEC_ERR_ARG;
     invalidate_step_graph(ctx);
     ctx->well_idx_host = idx;
     if (ctx->well_idx) cudaFree(ctx->well_idx);

@@ -379,6 +379,7 @@ extern "C" impec_status impec_ensemble_create(impec_ctx* const* members, int n, 
         set_error(std::string("impec_ensemble_create: instantiation failed: ") + cudaGetErrorString(ce));
         return fail(IMPEC_ERR_CUDA);
     }
+    for (impec_ctx* c : e->m) ++c->ensembles;  // the graph now holds their buffers
     *out = e;
     return IMPEC_OK;
 }
@@ -399,6 +400,7 @@ extern "C" impec_status impec_ensemble_step(impec_ensemble* e, int nsteps, int s
 extern "C" impec_status impec_ensemble_destroy(impec_ensemble* e) {
     if (!e) return IMPEC_OK;
     cudaStreamSynchronize(e->stream);
+    for (impec_ctx* c : e->m) --c->ensembles;
     ensemble_free(e);
     return IMPEC_OK;
 }

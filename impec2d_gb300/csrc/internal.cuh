@@ -195,6 +195,9 @@ struct impec_ctx {
     // the previous pressure, the predicted direction, its image under A and the step length
     impec::LearnedHook* learned = nullptr;
     double *lrn_r0 = nullptr, *lrn_d = nullptr, *lrn_Ad = nullptr, *lrn_alpha = nullptr;
+    // live ensembles whose captured graph holds this context's buffers: calls that would free
+    // or move a buffer are refused while it is non-zero
+    int ensembles = 0;
 };
 
 namespace impec {
@@ -227,6 +230,8 @@ impec_status cn_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalH
 impec_status cn_iteration(impec_ctx* ctx, double* c);
 impec_status dispersion_cn_dev(impec_ctx* ctx, double* c, const double* u, const double* v, double dt_scale,
                                const double* dt_dev, double tol, int* its, double* relres);
+// ctx.cu: false (and the error set) when ctx belongs to a live ensemble
+bool buffers_movable(const impec_ctx* ctx, const char* what);
 // learned_net.cu
 bool learned_predicts(const impec_ctx* ctx);
 impec_status learned_predict(impec_ctx* ctx, const double* x, const double* r0, double* d);

@@ -736,6 +736,7 @@ void learned_release(impec_ctx* ctx) {
 
 extern "C" impec_status impec_learned_attach(impec_ctx* ctx, impec_net* net, int factor, int mode) {
     if (!ctx) return IMPEC_ERR_ARG;
+    if (!buffers_movable(ctx, "impec_learned_attach")) return IMPEC_ERR_ARG;
     if (ctx->stream) IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream)); else IMPEC_CUDA_TRY(cudaDeviceSynchronize());
     invalidate_step_graph(ctx);
     learned_release(ctx);

@@ -278,8 +278,11 @@ impec_status impec_advect_symmetric_noalloc(const impec_params* P, double* c_dev
 /* One CUDA graph holding each member's whole IMPES step as a parallel branch, so one launch
  * advances every member (BASELINE's batched-ensemble mode; no counterpart in the reference,
  * whose driver runs one realisation per process).  Members must not use alternating sweeps and
- * run without output-time clipping.  A member's later changes (source cells, tunables,
- * permeability) are not seen by an existing ensemble: create it again. */
+ * run without output-time clipping.  A member's later changes of tunables are not seen by an
+ * existing ensemble: create it again.  While an ensemble lives, calls that would free or move
+ * a member's buffers fail with IMPEC_ERR_ARG: impec_ctx_destroy, impec_learned_attach,
+ * impec_set_source with new well cells, impec_set_permeability changing between isotropic and
+ * anisotropic (new values in the same layout are copied in place and seen by the ensemble). */
 typedef struct impec_ensemble impec_ensemble;
 impec_status impec_ensemble_create(impec_ctx* const* members, int n, impec_ensemble** out);
 /* nsteps graph launches on the ensemble's stream, ordered after work already queued on the

@@ -78,3 +78,31 @@ def test_tuning_and_autotune(engine):
     p = torch.zeros((N, N), dtype=torch.float64, device="cuda")
     cyc, rr, _ = ctx.pressure_solve(c, p, 1e-10)
     assert rr <= 1e-10
+
+
+def test_ensemble_members_keep_their_buffers(engine):
+    """While an ensemble's graph holds a member's buffers, calls that would free or move them
+    are refused (the graph would read freed memory); in-place permeability updates pass."""
+    import numpy as np
+    import torch
+    from impec2d_gb300.workloads import realisation
+    E = engine
+    a, b = realisation(E, 64, 1), realisation(E, 64, 2)
+    ens = E.Ensemble([a, b])
+    net = E.Net(seed=0)
+    with pytest.raises(E.ImpecError):
+        a.close()
+    assert a.h is not None
+    with pytest.raises(E.ImpecError):
+        net.attach(a, factor=1, mode=2)
+    q = np.zeros(64 * 64)
+    q[5], q[-7] = 1.0, -1.0
+    with pytest.raises(E.ImpecError):
+        a.set_source(torch.from_numpy(q).cuda())
+    K = torch.full((64, 64), 2.0, dtype=torch.float64, device="cuda")
+    a.set_permeability(K, K)  # same layout: in place
+    ens.step(1)
+    ens.close()
+    a.close()
+    b.close()
+    net.close()
