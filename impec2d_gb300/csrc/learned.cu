@@ -577,6 +577,124 @@ __global__ void __launch_bounds__(GB_THREADS) k_conv_wgrad(const __nv_bfloat16* 
     if (warp == 0) umma::tmem_free(tmem, GB_TMEM_COLS);
 }
 
+// Weight gradient on TMA boxes, both operands MN-major (no transposing stores).  GEMM rows:
+// output channels (128 per CTA), columns: (tap, ci) pairs (128 per CTA), K: 64 pixels per
+// stage over the CTA's slice of the pixels (blockIdx.z), partial sums added to dW with fp32
+// atomics.  Per stage: A = 128 / CA boxes of dZ [pixels][cout] (CA channels x 64 pixels, rows =
+// pixels, CA-element MN blocks), B = 128 / CB boxes of the layer input at one tap's offset (CB
+// channels x the stage's 64 pixels as a 4D box, zero-filled outside the image; column blocks
+// beyond 9 cin point past the channels and load zeros).  CA, CB = 64 (128-byte swizzle) or 32
+// (64-byte).  Roles as in k_conv3x3_tma, one tile per CTA.
+constexpr int WG_THREADS = 192, WG_STAGES = 6, WG_PIX = 64;
+
+template <int CA, int CB>
+__global__ void __launch_bounds__(WG_THREADS) k_conv_wgrad_tma(const __grid_constant__ CUtensorMap tz,
+                                                               const __grid_constant__ CUtensorMap tx, int H, int W_,
+                                                               int cin, int cout, int Kp, int P, int pix_per_split,
+                                                               float* __restrict__ dW, int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char wt_smem[];
+    constexpr int A_BLK = WG_PIX * CA * 2, B_BLK = WG_PIX * CB * 2;  // bytes of one MN block
+    constexpr int A_BYTES = 128 / CA * A_BLK, STAGE = A_BYTES + 128 / CB * B_BLK;
+    __shared__ uint64_t full[WG_STAGES], empty[WG_STAGES], done;
+    __shared__ uint32_t tslot;
+    __shared__ volatile int fail, tma_issued;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int co0 = blockIdx.y * 128, k0 = blockIdx.x * 128;
+    const int p_begin = blockIdx.z * pix_per_split;
+    const int p_end = p_begin + pix_per_split < P ? p_begin + pix_per_split : P;
+    const int nk = p_end > p_begin ? (p_end - p_begin + WG_PIX - 1) / WG_PIX : 0;
+    unsigned char* base = wt_smem + ((1024 - (umma::smem_u32(wt_smem) & 1023)) & 1023);
+    if (warp == 0) umma::tmem_alloc(&tslot, 128);
+    if (tid == 0) {
+        for (int st = 0; st < WG_STAGES; ++st) {
+            umma::mbar_init(&full[st], 1);
+            umma::mbar_init(&empty[st], 1);
+        }
+        umma::mbar_init(&done, 1);
+        fail = 0;
+        tma_issued = 0;
+    }
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+    if (warp == 4) {
+        if (lane == 0) {  // TMA producer
+            const int hw = H * W_;
+            for (int kt = 0; kt < nk; ++kt) {
+                const int slot = kt % WG_STAGES, use = kt / WG_STAGES;
+                if (use > 0 && !umma::mbar_wait(&empty[slot], (uint32_t)((use - 1) & 1), GB_WAIT_TRIES)) {
+                    fail = 1;
+                    break;
+                }
+                const int p0 = p_begin + kt * WG_PIX, b0 = p0 / hw, rem = p0 - b0 * hw, y0 = rem / W_,
+                          x0 = rem - y0 * W_;
+                unsigned char* sA = base + slot * STAGE;
+                umma::mbar_expect_tx(&full[slot], (uint32_t)STAGE);
+#pragma unroll
+                for (int i = 0; i < 128 / CA; ++i) umma::tma_load_2d(sA + i * A_BLK, &tz, co0 + i * CA, p0, &full[slot]);
+#pragma unroll
+                for (int j = 0; j < 128 / CB; ++j) {
+                    const int k = k0 + j * CB, tap = k / cin;
+                    const int c0 = tap < 9 ? k - tap * cin : cin;  // past the taps: a box of zeros
+                    const int t = tap < 9 ? tap : 4;
+                    umma::tma_load_4d(sA + A_BYTES + j * B_BLK, &tx, c0, x0 + t % 3 - 1, y0 + t / 3 - 1, b0,
+                                      &full[slot]);
+                }
+                tma_issued = kt + 1;
+            }
+        }
+        __syncwarp();
+    } else if (warp == 5) {
+        if (lane == 0) {  // MMA issuer
+            const uint32_t idesc = umma::idesc_bf16_f32_mn(128, 128);
+            int kt = 0;
+            for (; kt < nk; ++kt) {
+                const int slot = kt % WG_STAGES, use = kt / WG_STAGES;
+                if (!umma::mbar_wait(&full[slot], (uint32_t)(use & 1), GB_WAIT_TRIES)) {
+                    fail = 1;
+                    for (int j = kt + 1; j < tma_issued; ++j)
+                        umma::mbar_wait(&full[j % WG_STAGES], (uint32_t)((j / WG_STAGES) & 1), GB_WAIT_TRIES >> 4);
+                    break;
+                }
+                umma::fence_after();
+                const uint32_t sa = umma::smem_u32(base + slot * STAGE), sb = sa + A_BYTES;
+#pragma unroll
+                for (int ks = 0; ks < WG_PIX / 16; ++ks) {  // 16 pixels = two 8-row K groups
+                    const uint64_t ad = umma::smem_desc_mn(sa + ks * 2 * 8 * CA * 2, A_BLK, 8 * CA * 2, CA * 2);
+                    const uint64_t bd = umma::smem_desc_mn(sb + ks * 2 * 8 * CB * 2, B_BLK, 8 * CB * 2, CB * 2);
+                    umma::mma_bf16(tmem, ad, bd, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+                }
+                umma::commit(&empty[slot]);
+            }
+            umma::commit(&done);
+        }
+        __syncwarp();
+    }
+    const bool fin = warp < 4 && nk > 0 ? umma::mbar_wait(&done, 0u, GB_WAIT_TRIES) : true;
+    const bool ok = __syncthreads_and(fin) != 0 && fail == 0;
+    if (ok && nk > 0 && warp < 4) {
+        umma::fence_after();
+        const int co = co0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int cb = 0; cb < 4; ++cb) {
+            float v[32];
+            umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
+            if (co >= cout) continue;
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                const int k = k0 + cb * 32 + q;
+                if (k < 9 * cin) atomicAdd(dW + (size_t)co * Kp + k, v[q]);
+            }
+        }
+    }
+    if (!ok && tid == 0) atomicExch(err, 1);
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    if (warp == 0) umma::tmem_free(tmem, 128);
+}
+
 void launch_wt_transpose(const __nv_bfloat16* W, int cin, int cout, __nv_bfloat16* Wd, cudaStream_t s) {
     k_conv_wt_transpose<<<128, 256, 0, s>>>(W, cin, cout, conv_kp(cin), Wd, conv_kp(cout));
 }
@@ -741,8 +859,86 @@ impec_status launch_conv(const ConvArgs& a, cudaStream_t s) {
     return launch_conv_any<32>(a, s);
 }
 
+// Boxes of 64 pixels: whole rows (W a multiple of 64) or whole-row groups of one image, as in
+// conv_tma_plan; cin and cout multiples of 32; P a multiple of 64.
+static bool wgrad_tma_plan(int B, int H, int W, int cin, int cout, int* wb, int* hb, int* bb) {
+    static const bool off = [] {
+        const char* e = getenv("IMPEC_CONV_TMA");
+        return e && e[0] == '0';
+    }();
+    if (off || cin % 32 || cout % 32 || ((long long)B * H * W) % WG_PIX || !tmap_encoder()) return false;
+    if (W >= WG_PIX) {
+        if (W % WG_PIX) return false;
+        *wb = WG_PIX, *hb = 1, *bb = 1;
+        return true;
+    }
+    if (WG_PIX % W) return false;
+    const int r = WG_PIX / W;
+    *wb = W;
+    if (r >= H) {
+        if (r % H) return false;
+        *hb = H, *bb = r / H;
+    } else {
+        if (H % r) return false;
+        *hb = r, *bb = 1;
+    }
+    return true;
+}
+
+template <int CA, int CB>
+static impec_status launch_wgrad_tma(const __nv_bfloat16* dZ, const __nv_bfloat16* X, int B, int H, int W_, int cin,
+                                     int cout, float* dW, int* err, int num_sms, int wb, int hb, int bb,
+                                     cudaStream_t s) {
+    constexpr int STAGE = 128 * WG_PIX * 2 * 2;
+    const int smem = WG_STAGES * STAGE + 1024;
+    static bool attr = false;
+    if (!attr) {
+        IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_conv_wgrad_tma<CA, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    TmapEncodeFn enc = tmap_encoder();
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    const int P = B * H * W_, Kp = conv_kp(cin);
+    CUtensorMap tz, tx;
+    const cuuint64_t zd[2] = {(cuuint64_t)cout, (cuuint64_t)P};
+    const cuuint64_t zs[1] = {(cuuint64_t)cout * 2};
+    const cuuint32_t zb[2] = {(cuuint32_t)CA, (cuuint32_t)WG_PIX};
+    if (enc(&tz, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)dZ, zd, zs, zb, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CA == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+        set_error("wgrad: cuTensorMapEncodeTiled (gradients) failed");
+        return IMPEC_ERR_CUDA;
+    }
+    const cuuint64_t xd[4] = {(cuuint64_t)cin, (cuuint64_t)W_, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t xs[3] = {(cuuint64_t)cin * 2, (cuuint64_t)W_ * cin * 2, (cuuint64_t)H * W_ * cin * 2};
+    const cuuint32_t xb[4] = {(cuuint32_t)CB, (cuuint32_t)wb, (cuuint32_t)hb, (cuuint32_t)bb};
+    if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)X, xd, xs, xb, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CB == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+        set_error("wgrad: cuTensorMapEncodeTiled (activations) failed");
+        return IMPEC_ERR_CUDA;
+    }
+    const int nt = (9 * cin + 127) / 128, mt = (cout + 127) / 128;
+    int splits = (2 * num_sms + nt * mt - 1) / (nt * mt);
+    int per = (P + splits - 1) / splits;
+    per = (per + WG_PIX - 1) / WG_PIX * WG_PIX;
+    splits = (P + per - 1) / per;
+    dim3 g(nt, mt, splits);
+    k_conv_wgrad_tma<CA, CB><<<g, WG_THREADS, smem, s>>>(tz, tx, H, W_, cin, cout, Kp, P, per, dW, err);
+    IMPEC_CUDA_TRY(cudaGetLastError());
+    return IMPEC_OK;
+}
+
 impec_status launch_wgrad(const __nv_bfloat16* dZ, const __nv_bfloat16* X, int B, int H, int W_, int cin, int cout,
                           float* dW, int* err, int num_sms, cudaStream_t s) {
+    int wb, hb, bb;
+    if (wgrad_tma_plan(B, H, W_, cin, cout, &wb, &hb, &bb)) {
+        const bool a64 = cout % 64 == 0, b64 = cin % 64 == 0;
+        if (a64 && b64) return launch_wgrad_tma<64, 64>(dZ, X, B, H, W_, cin, cout, dW, err, num_sms, wb, hb, bb, s);
+        if (a64) return launch_wgrad_tma<64, 32>(dZ, X, B, H, W_, cin, cout, dW, err, num_sms, wb, hb, bb, s);
+        if (b64) return launch_wgrad_tma<32, 64>(dZ, X, B, H, W_, cin, cout, dW, err, num_sms, wb, hb, bb, s);
+        return launch_wgrad_tma<32, 32>(dZ, X, B, H, W_, cin, cout, dW, err, num_sms, wb, hb, bb, s);
+    }
     static bool attr = false;
     const int smem = 2 * GB_TILE_BYTES + 1024;
     if (!attr) {

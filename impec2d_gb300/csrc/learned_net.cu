@@ -171,14 +171,31 @@ __global__ void k_pool2_bwd_add_gelu(const __nv_bfloat16* __restrict__ g, const 
     }
 }
 
-// gb[c] += sum over P pixels of dz[p][c]; each block folds a slab of pixels per channel.
-__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dz, size_t P, int C, float* __restrict__ gb) {
-    const int c = threadIdx.x % C, lanes = blockDim.x / C;
-    if ((int)threadIdx.x >= lanes * C) return;
-    const int l = threadIdx.x / C;
-    float s = 0.0f;
-    for (size_t p = blockIdx.x * (size_t)lanes + l; p < P; p += (size_t)gridDim.x * lanes) s += bf(dz[p * C + c]);
-    atomicAdd(gb + c, s);
+// gb[c] += sum over P pixels of dz[p][c].  Thread t of a block reads 8 channels (16 bytes) of
+// one pixel: channel group t % (C / 8), pixel lane t / (C / 8); the block folds its partial
+// sums per channel in shared memory and adds them with one atomic per channel.  C is a
+// multiple of 8 and divides 8 * blockDim.x (blockDim.x = 256).
+__global__ void __launch_bounds__(256) k_bias_grad(const __nv_bfloat16* __restrict__ dz, size_t P, int C,
+                                                   float* __restrict__ gb) {
+    __shared__ float part[256 * 8];
+    const int C8 = C >> 3, lanes = blockDim.x / C8;
+    const int cg = threadIdx.x % C8, pl = threadIdx.x / C8;
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (pl < lanes)
+        for (size_t p = blockIdx.x * (size_t)lanes + pl; p < P; p += (size_t)gridDim.x * lanes) {
+            __align__(16) __nv_bfloat16 v[8];
+            *reinterpret_cast<uint4*>(v) = *reinterpret_cast<const uint4*>(dz + p * C + 8 * cg);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) acc[k] += bf(v[k]);
+        }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) part[threadIdx.x * 8 + k] = acc[k];
+    __syncthreads();
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        float s = 0.0f;
+        for (int l = 0; l < lanes; ++l) s += part[(l * C8 + (c >> 3)) * 8 + (c & 7)];
+        atomicAdd(gb + c, s);
+    }
 }
 
 // MSE on channel 0: loss += sum (o - t)^2 / P; dz channel 0 = 2 (o - t) / P, other channels 0.
@@ -481,7 +498,10 @@ static impec_status net_backward(impec_net* net, const __nv_bfloat16* X, cudaStr
         const int h = H >> L.level, w = W >> L.level;
         IMPEC_TRY(launch_wgrad(nb.dz[l], layer_input(nb, X, l), B, h, w, L.cin, L.cout, L.gw, net->err, net->num_sms, s));
         const size_t P = level_pixels(nb, L.level);
-        k_bias_grad<<<256, 256, 0, s>>>(nb.dz[l], P, L.cout, L.gb);
+        {
+            const size_t want = (P * (size_t)(L.cout / 8) + 255) / 256, cap = (size_t)net->num_sms * 8;
+            k_bias_grad<<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(nb.dz[l], P, L.cout, L.gb);
+        }
         switch (l) {
             case 0: break;
             case 14: case 7: case 5: case 3: case 1:  // input is a plain GELU output

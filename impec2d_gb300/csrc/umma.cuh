@@ -41,10 +41,27 @@ __device__ __forceinline__ uint64_t smem_desc_sw(uint32_t saddr, int row_bytes) 
     return d;
 }
 
+// Descriptor of an MN-major tile written by TMA: blocks of `row_bytes` (128 or 64 bytes: 64 or
+// 32 elements along M/N) per K row, 128- or 64-byte swizzled, 8-row K groups `sbo` bytes apart
+// and M/N blocks `lbo` bytes apart.
+__device__ __forceinline__ uint64_t smem_desc_mn(uint32_t saddr, uint32_t lbo, uint32_t sbo, int row_bytes) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)(row_bytes == 128 ? 2 : 4) << 61;
+    return d;
+}
+
 // Instruction descriptor of kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9 and
 // 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// The same with both operands MN-major (bits 15 and 16: A and B transposed).
+__host__ __device__ constexpr uint32_t idesc_bf16_f32_mn(int M, int N) {
+    return idesc_bf16_f32(M, N) | (1u << 15) | (1u << 16);
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
