@@ -16,6 +16,10 @@
 
 #include "Solvers.h"
 
+namespace impec {
+void set_error(const std::string& msg);  // the library's last-error record (impec_last_error)
+}
+
 // ---------------------------------------------------------------- host ghost fills
 // Reflection form of FillGhostCellsNeumannScalar / FillGhostCellsPeriodicScalar /
 // FillGhostCellsNeumannVelocity (src/Util.cpp:215-438).
@@ -58,10 +62,69 @@ void FillGhostCellsNeumannVelocity(Array3d& v, int N1, int N2, int g) {
 Engine::Engine(const SimParams& sp) : N1(sp.N1), N2(sp.N2), g(sp.p_bounds) {
     impec_params P = sp.engine();
     check(impec_ctx_create(&P, nullptr, &ctx_), "impec_ctx_create");
-    check(impec_state(ctx_, &c, &p, &u, &v, &q), "impec_state");
-    check(impec_set_time(ctx_, sp.tstart), "impec_set_time");
+    try {
+        check(impec_state(ctx_, &c, &p, &u, &v, &q), "impec_state");
+        check(impec_set_time(ctx_, sp.tstart), "impec_set_time");
+        if (!sp.learned_weights.empty()) attach_learned(sp);
+    } catch (...) {
+        if (net_) impec_learned_attach(ctx_, nullptr, 1, 0), impec_net_destroy(net_);
+        impec_ctx_destroy(ctx_);
+        throw;
+    }
 }
-Engine::~Engine() { impec_ctx_destroy(ctx_); }
+Engine::~Engine() {
+    if (net_) {
+        impec_learned_attach(ctx_, nullptr, 1, 0);
+        impec_net_destroy(net_);
+    }
+    impec_ctx_destroy(ctx_);
+}
+
+// A 1-D little-endian float32 .npy array (format versions 1-3, C order).
+static std::vector<float> read_npy_f32(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw ConfigError("gb300.learned_weights: cannot open " + path);
+    char magic[6];
+    unsigned char ver[2];
+    f.read(magic, 6);
+    f.read(reinterpret_cast<char*>(ver), 2);
+    if (!f || std::string(magic, 6) != "\x93NUMPY") throw ConfigError(path + ": not an .npy file");
+    uint32_t hlen = 0;
+    unsigned char b[4] = {0, 0, 0, 0};
+    f.read(reinterpret_cast<char*>(b), ver[0] == 1 ? 2 : 4);
+    hlen = b[0] | (b[1] << 8) | (ver[0] == 1 ? 0u : ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24));
+    std::string h(hlen, ' ');
+    f.read(&h[0], hlen);
+    auto has = [&](const char* t) { return h.find(t) != std::string::npos; };
+    if (!f || !has("'descr': '<f4'") || !has("'fortran_order': False"))
+        throw ConfigError(path + ": expected a little-endian float32 array in C order");
+    const size_t lp = h.find("'shape': ("), rp = lp == std::string::npos ? lp : h.find(')', lp);
+    if (rp == std::string::npos) throw ConfigError(path + ": no shape in the .npy header");
+    const std::string shape = h.substr(lp + 10, rp - lp - 10);
+    if (shape.find(',') != shape.rfind(',') || shape.find_first_not_of("0123456789, ") != std::string::npos)
+        throw ConfigError(path + ": expected a 1-D array");
+    const size_t n = std::stoull(shape);
+    std::vector<float> w(n);
+    f.read(reinterpret_cast<char*>(w.data()), (std::streamsize)(n * sizeof(float)));
+    if (!f) throw ConfigError(path + ": truncated");
+    return w;
+}
+
+// gb300.learned_weights: the trained network as the initial guess of every pressure solve.
+void Engine::attach_learned(const SimParams& sp) {
+    std::vector<float> w = read_npy_f32(sp.learned_weights);
+    check(impec_net_create(0, &net_), "impec_net_create");
+    size_t count = 0;
+    check(impec_net_parameters(net_, nullptr, nullptr, &count, 0), "impec_net_parameters");
+    if (w.size() != count)
+        throw ConfigError(sp.learned_weights + ": " + std::to_string(w.size()) + " parameters, the network has " +
+                          std::to_string(count));
+    check(impec_net_parameters(net_, nullptr, w.data(), &count, 0), "impec_net_parameters");
+    int f = sp.learned_factor;
+    if (f == 0)
+        for (f = 16; f > 1 && (N1 / f < 256 || N1 % (8 * f) || N2 % (8 * f)); f /= 2) {}
+    check(impec_learned_attach(ctx_, net_, f, 1), "impec_learned_attach");
+}
 void Engine::check(impec_status s, const char* what) const {
     if (s != IMPEC_OK) throw EngineError(s, std::string(what) + ": " + impec_last_error());
 }
@@ -678,6 +741,7 @@ impec_status impec_cfg_load(const char* path, impec_params* P, double* tstart, d
         return IMPEC_OK;
     } catch (const std::exception& e) {
         fprintf(stderr, "%s\n", e.what());
+        impec::set_error(e.what());
         return IMPEC_ERR_CONFIG;
     }
 }
@@ -690,6 +754,7 @@ impec_status impec_cfg_source(const char* path, double* q_host) {
         return IMPEC_OK;
     } catch (const std::exception& e) {
         fprintf(stderr, "%s\n", e.what());
+        impec::set_error(e.what());
         return IMPEC_ERR_CONFIG;
     }
 }
@@ -702,12 +767,15 @@ impec_status impec_run_cfg(const char* path, int quiet) {
         return s.Run() ? IMPEC_OK : IMPEC_ERR_NOT_CONVERGED;
     } catch (const ConfigError& e) {
         fprintf(stderr, "%s\n", e.what());
+        impec::set_error(e.what());
         return IMPEC_ERR_CONFIG;
     } catch (const EngineError& e) {
         fprintf(stderr, "%s\n", e.what());
+        impec::set_error(e.what());
         return e.status;
     } catch (const std::exception& e) {
         fprintf(stderr, "%s\n", e.what());
+        impec::set_error(e.what());
         return IMPEC_ERR_ARG;
     }
 }

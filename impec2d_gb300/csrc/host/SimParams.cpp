@@ -361,6 +361,12 @@ void SimParams::load(std::shared_ptr<CfgNode> root) {
         if (e->lookup("warm_start", b)) warm_start = b;
         if (e->lookup("peaceman_guard", b)) peaceman_guard = b;
         if (e->lookup("cfl_porosity", b)) cfl_porosity = b;
+        if (e->lookup("learned_weights", learned_weights) && !learned_weights.empty())
+            warm_start = 1;  // the network moves the previous pressure
+        if (e->lookup("learned_factor", learned_factor) &&
+            !(learned_factor == 1 || learned_factor == 2 || learned_factor == 4 || learned_factor == 8 ||
+              learned_factor == 16))
+            throw ConfigError("gb300.learned_factor must be 1, 2, 4, 8 or 16");
     }
     v_bounds = p_bounds;  // src/SimParams.cpp:448
     dx = (x_ub - x_lb) / N1;

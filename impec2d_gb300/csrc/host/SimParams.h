@@ -106,6 +106,10 @@ public:
     // engine options (optional group application.gb300; absent = reference behaviour)
     double Dm = 0.0;
     int precision = IMPEC_PREC_FP64, max_cycles = 100, warm_start = 0, peaceman_guard = 1, cfl_porosity = 0;
+    // learned warm start: trained parameters (.npy of float32, impec_net_parameters order) and
+    // the feature averaging factor (0: N1 / 256 rounded down to 1, 2, 4, 8 or 16)
+    std::string learned_weights;
+    int learned_factor = 0;
 
     explicit SimParams(const std::string& configfile);
     SimParams(const std::string& text, bool from_text);

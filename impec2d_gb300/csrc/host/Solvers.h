@@ -44,7 +44,9 @@ public:
     int N1, N2, g;
 
 private:
+    void attach_learned(const SimParams& sp);
     impec_ctx* ctx_ = nullptr;
+    impec_net* net_ = nullptr;  // learned warm start (gb300.learned_weights), or none
 };
 
 class EllipticSolver {

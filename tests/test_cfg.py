@@ -105,3 +105,36 @@ def test_comments_lists_and_unknown_keys(tmp_path):
     txt = base.replace("log_time_list = [];", "log_time_list = [0.01, 0.02, 3e-2]; /* block */ extra_key = \"x\";")
     P, t0, t1 = E.load_cfg(_write(tmp_path, txt))
     assert P.N1 == 128
+
+
+def _learned_cfg(tmp_path, weights, extra=""):
+    base = open(os.path.join(HERE, "golden", "quarter_five_spot_128_upwind.cfg")).read()
+    txt = base.replace("cfl_porosity = true;", f"cfl_porosity = true;  learned_weights = \"{weights}\"; {extra}")
+    txt = txt.replace("endtime = 0.06;", "endtime = 0.0005;").replace("/tmp/impec2d_c1", str(tmp_path / "out"))
+    return _write(tmp_path, txt)
+
+
+def test_learned_keys(tmp_path):
+    """gb300.learned_weights turns the previous-pressure start on (the network moves it);
+    gb300.learned_factor accepts the supported averaging factors only."""
+    P, _, _ = E.load_cfg(_learned_cfg(tmp_path, tmp_path / "w.npy"))
+    assert P.warm_start == 1
+    P, _, _ = E.load_cfg(_learned_cfg(tmp_path, tmp_path / "w.npy", "learned_factor = 2;"))
+    with pytest.raises(E.ImpecError):
+        E.load_cfg(_learned_cfg(tmp_path, tmp_path / "w.npy", "learned_factor = 3;"))
+
+
+@pytest.mark.gpu
+def test_run_cfg_with_learned_weights(tmp_path):
+    """The executable's entry point loads trained parameters from the .npy that
+    `bench.py --study learned --net-out` writes and runs with the network attached; a file of
+    the wrong size is a status, not a crash."""
+    import numpy as np
+    net = E.Net(seed=4)
+    w = net.parameters()
+    net.close()
+    np.save(tmp_path / "w.npy", w)
+    assert E.lib().impec_run_cfg(str(_learned_cfg(tmp_path, tmp_path / "w.npy")).encode(), 1) == 0, E.last_error()
+    np.save(tmp_path / "short.npy", w[:100])
+    assert E.lib().impec_run_cfg(str(_learned_cfg(tmp_path, tmp_path / "short.npy")).encode(), 1) != 0
+    assert "parameters" in E.last_error()
