@@ -106,3 +106,36 @@ def test_ensemble_members_keep_their_buffers(engine):
     a.close()
     b.close()
     net.close()
+
+
+def test_ensemble_with_learned_members_matches_solo(engine):
+    """Members with the learned initial guess attached (one shared network) run their hooks
+    (features, forward pass, step along the prediction) inside the ensemble graph's parallel
+    branches and end bit-identical to the same members stepped alone."""
+    from impec2d_gb300.workloads import realisation
+    E = engine
+    net = E.Net(seed=11)
+    specs = [(64, 3), (128, 4), (64, 5)]
+    ens_members = [realisation(E, N, s, warm_start=1) for N, s in specs]
+    solo = [realisation(E, N, s, warm_start=1) for N, s in specs]
+    for cx in ens_members + solo:
+        cx.run_steps(2)
+        net.attach(cx, factor=1, mode=1)
+    ens = E.Ensemble(ens_members)
+    ens.step(4)
+    for cx in solo:
+        for _ in range(4):
+            info = cx.step()
+            assert info.relres <= 1e-10
+    for (N, _), a, b in zip(specs, ens_members, solo):
+        ca, pa = np.zeros((N + 4, N + 4)), np.zeros((N + 4, N + 4))
+        cb, pb = np.zeros_like(ca), np.zeros_like(pa)
+        a.download(ca, pa, None, ghost=2)
+        b.download(cb, pb, None, ghost=2)
+        assert np.array_equal(ca, cb) and np.array_equal(pa, pb)
+        assert E.Net.last_alpha(a) == E.Net.last_alpha(b)
+    ens.close()
+    for cx in ens_members + solo:
+        E.Net.detach(cx)
+        cx.close()
+    net.close()
