@@ -117,8 +117,7 @@ static impec_status capture_step_into(impec_ctx* ctx, int pfs_in) {
         IMPEC_TRY(capture_while(
             ctx, [&](cudaGraphConditionalHandle h) { return pressure_check(ctx, P.eps, 0, h, 1); },
             [&](cudaGraphConditionalHandle h) {
-                IMPEC_TRY(pressure_iteration(ctx));
-                return pressure_check(ctx, P.eps, 1, h, 1);
+                return pressure_step(ctx, P.eps, h, 1);
             },
             mg_body));
         IMPEC_TRY(pressure_finish(ctx, ctx->p));
@@ -185,8 +184,7 @@ static impec_status capture_pressure(impec_ctx* ctx, cudaGraph_t* out) {
         IMPEC_TRY(capture_while(
             ctx, [&](cudaGraphConditionalHandle h) { return pressure_check(ctx, P.eps, 0, h, 1); },
             [&](cudaGraphConditionalHandle h) {
-                IMPEC_TRY(pressure_iteration(ctx));
-                return pressure_check(ctx, P.eps, 1, h, 1);
+                return pressure_step(ctx, P.eps, h, 1);
             },
             mg_body));
         return pressure_finish(ctx, ctx->p);

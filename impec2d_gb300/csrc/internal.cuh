@@ -211,7 +211,8 @@ impec_status pressure_apply_ref(impec_ctx* ctx, const double* x, double* y);
 impec_status pressure_prepare(impec_ctx* ctx, const double* c, const double* p);
 impec_status pressure_residual(impec_ctx* ctx);
 impec_status pressure_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h);
-impec_status pressure_iteration(impec_ctx* ctx);
+impec_status pressure_iteration(impec_ctx* ctx, double tol, cudaGraphConditionalHandle h, int use_h);
+impec_status pressure_step(impec_ctx* ctx, double tol, cudaGraphConditionalHandle h, int use_h);
 impec_status pressure_finish(impec_ctx* ctx, double* p);
 // elliptic velocity
 impec_status velocity(impec_ctx* ctx, const double* p, const double* c, double* u, double* v);

@@ -1099,9 +1099,8 @@ static void vcycle(impec_ctx* ctx, size_t l) {
 // another cycle runs and, inside a graph, sets the WHILE node's condition.  With CG
 // (krylov) and after an iteration, it also keeps the iteration's alpha and (r, z) for the
 // next search direction, and stops on a breakdown ((p, Ap) <= 0).
-__global__ void k_mg_check(DevScalars* S, double tol, int max_cycles, int inc, cudaGraphConditionalHandle h,
-                           int use_h, int krylov) {
-    pdl_enter();
+__device__ __forceinline__ void mg_check(DevScalars* S, double tol, int max_cycles, int inc,
+                                         cudaGraphConditionalHandle h, int use_h, int krylov) {
     bool breakdown = false;
     if (inc) {
         S->mg_cycles++;
@@ -1121,6 +1120,12 @@ __global__ void k_mg_check(DevScalars* S, double tol, int max_cycles, int inc, c
     else if (!go && rr > tol) S->flags |= FLAG_MG_NOT_CONVERGED;
     S->go = go ? 1 : 0;
     if (use_h) cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+__global__ void k_mg_check(DevScalars* S, double tol, int max_cycles, int inc, cudaGraphConditionalHandle h,
+                           int use_h, int krylov) {
+    pdl_enter();
+    mg_check(S, tol, max_cycles, inc, h, use_h, krylov);
 }
 
 // ---------------------------------------------------------------- V-cycle preconditioned CG
@@ -1191,12 +1196,14 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_apply(Level F, const double*
 }
 
 // alpha = (r, z) / (p, Ap); x += alpha p; r -= alpha Ap (and its FP32 copy); ||r||^2 over the
-// cells other than the pinned one.
+// cells other than the pinned one.  The last block of the reduction then runs the iteration's
+// convergence check (k_mg_check's work, one launch fewer per iteration).
 __global__ void __launch_bounds__(RED_THREADS) k_cg_update(int n1, int n2, double* __restrict__ x,
                                                            double* __restrict__ r, float* __restrict__ r32,
                                                            const double* __restrict__ p, const double* __restrict__ q,
-                                                           int pin, const DevScalars* __restrict__ S,
-                                                           double* partials, int mb, unsigned* counter, double* out) {
+                                                           int pin, DevScalars* S, double* partials, int mb,
+                                                           unsigned* counter, double* out, double tol, int max_cycles,
+                                                           cudaGraphConditionalHandle h, int use_h) {
     pdl_enter();
     const double pq = S->pcg_pq;
     const double alpha = pq > 0.0 ? S->pcg_rz / pq : 0.0;
@@ -1208,7 +1215,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_update(int n1, int n2, doubl
         if (r32) r32[k] = (float)rr;
         if ((int)k != pin) acc[0] += rr * rr;
     });
-    grid_reduce<1>(acc, 0u, partials, mb, counter, out);
+    if (grid_reduce<1>(acc, 0u, partials, mb, counter, out) && threadIdx.x == 0) {
+        __threadfence();
+        mg_check(S, tol, max_cycles, 1, h, use_h, 1);
+    }
 }
 
 // Relative residual of the returned iterate (true residual, recomputed after the loop).
@@ -1326,9 +1336,19 @@ impec_status pressure_check(impec_ctx* ctx, double tol, int inc, cudaGraphCondit
     return IMPEC_OK;
 }
 
-// One iteration on the current iterate followed by the new residual (launch only): a
-// stationary V-cycle, or a CG step preconditioned by one V-cycle.
-impec_status pressure_iteration(impec_ctx* ctx) {
+// One iteration on the current iterate, the new residual and the convergence check (launch
+// only): a stationary V-cycle, or a CG step preconditioned by one V-cycle (whose residual
+// kernel also runs the check).  h / use_h: the graph's WHILE condition, as pressure_check.
+impec_status pressure_step(impec_ctx* ctx, double tol, cudaGraphConditionalHandle h, int use_h) {
+    ctx->solve_tol = tol;
+    if (!ctx->krylov) {
+        IMPEC_TRY(pressure_iteration(ctx, tol, h, use_h));
+        return pressure_check(ctx, tol, 1, h, use_h);
+    }
+    return pressure_iteration(ctx, tol, h, use_h);
+}
+
+impec_status pressure_iteration(impec_ctx* ctx, double tol, cudaGraphConditionalHandle h, int use_h) {
     Level& F = ctx->L[0];
     const size_t n = F.n();
     const bool mixed = ctx->P.precision == IMPEC_PREC_MIXED;
@@ -1367,7 +1387,8 @@ impec_status pressure_iteration(impec_ctx* ctx) {
              ctx->max_blocks, ctx->counter, &S->pcg_pq);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_cg_update, blocks, RED_THREADS, 0, F.n1, F.n2, ctx->cg_x, r, mixed ? F.b32 : nullptr,
-             ctx->cg_p, ctx->cg_q, pin_index(ctx), S, ctx->partials, ctx->max_blocks, ctx->counter, &S->rnorm2);
+             (const double*)ctx->cg_p, (const double*)ctx->cg_q, pin_index(ctx), S, ctx->partials, ctx->max_blocks,
+             ctx->counter, &S->rnorm2, tol, ctx->P.max_cycles, h, use_h);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -1400,8 +1421,7 @@ impec_status pressure_solve(impec_ctx* ctx, const double* c, double* p, double t
     for (;;) {
         IMPEC_TRY(sync_scalars(ctx));
         if (!ctx->hscal->go) break;
-        IMPEC_TRY(pressure_iteration(ctx));
-        IMPEC_TRY(pressure_check(ctx, tol, 1, 0, 0));
+        IMPEC_TRY(pressure_step(ctx, tol, 0, 0));
     }
     IMPEC_TRY(pressure_finish(ctx, p));
     IMPEC_TRY(sync_scalars(ctx));

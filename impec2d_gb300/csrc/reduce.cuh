@@ -69,9 +69,10 @@ __device__ __forceinline__ void for_cells(int n1, int n2, F&& f) {
 }
 
 // Grid-level reduction with last-block finalisation.  Requires blockDim.x == RED_THREADS,
-// 1-D grid with gridDim.x <= max_blocks.  out[k] receives the reduced values.
+// 1-D grid with gridDim.x <= max_blocks.  out[k] receives the reduced values.  Returns true in
+// every thread of the last block (thread 0 of which wrote out[]).
 template <int K>
-__device__ void grid_reduce(double (&v)[K], unsigned maxmask, double* partials, int max_blocks,
+__device__ bool grid_reduce(double (&v)[K], unsigned maxmask, double* partials, int max_blocks,
                             unsigned* counter, double* out) {
     __shared__ bool last;
     block_reduce<K>(v, maxmask);
@@ -83,7 +84,7 @@ __device__ void grid_reduce(double (&v)[K], unsigned maxmask, double* partials, 
         last = (ticket == gridDim.x - 1);
     }
     __syncthreads();
-    if (!last) return;
+    if (!last) return false;
     __threadfence();
     double w[K];
 #pragma unroll
@@ -102,6 +103,7 @@ __device__ void grid_reduce(double (&v)[K], unsigned maxmask, double* partials, 
         for (int k = 0; k < K; ++k) out[k] = w[k];
         *counter = 0u;
     }
+    return true;
 }
 
 }  // namespace impec
