@@ -456,6 +456,136 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
     if (warp == 0) umma::tmem_free(tmem, 2 * TC);
 }
 
+// Halo variant for cin = 32 or 64 and W a multiple of 128 (a tile is 128 pixels of one image
+// row).  Per tile, one 4D TMA box brings the halo: CIN channels x 130 pixels (x0 - 1 .. x0 + 128)
+// x 3 rows (y0 - 1 .. y0 + 1), zero-filled outside the image, as 390 swizzled rows of CIN * 2
+// bytes.  The A operand of tap (dy, dx) is the 128 rows starting at row (1 + dy) * 130 + 1 + dx
+// of that box: the descriptor's start moves there, and since the hardware applies the swizzle
+// on absolute shared-memory addresses (base offset 0), no copy or realignment is needed.  One
+// load serves all 9 taps: 390 instead of 9 x 128 TMA rows per tile.  Each CTA keeps the weights
+// of its BN output channels for all 9 taps resident (loaded once) and walks the tiles
+// blockIdx.x / nt, + gridDim.x / nt, ...; the halo and the TMEM accumulator are
+// double-buffered so that the next tile's load and MMAs overlap the epilogue.  Roles as in
+// k_conv3x3_tma (lane 0 of warp 4: TMA, lane 0 of warp 5: MMA, warps 0-3: epilogue).
+constexpr int CH_THREADS = 192, CH_PIX = 130, CH_ROWS = 3 * CH_PIX;
+
+template <int CIN>
+__host__ __device__ constexpr int halo_bytes() { return (CH_ROWS * CIN * 2 + 1023) / 1024 * 1024; }
+template <int BN, int CIN>
+__host__ __device__ constexpr int halo_smem() { return 9 * BN * CIN * 2 + 2 * halo_bytes<CIN>() + 1024; }
+
+template <int BN, int CIN>
+__global__ void __launch_bounds__(CH_THREADS) k_conv3x3_halo(const __grid_constant__ CUtensorMap tx,
+                                                             const __grid_constant__ CUtensorMap tw, ConvArgs a) {
+    extern __shared__ __align__(1024) unsigned char ch_smem[];
+    constexpr int ROWB = CIN * 2, W_TAP = BN * ROWB, HALO = halo_bytes<CIN>();
+    constexpr uint32_t TC = BN < 32 ? 32 : BN;
+    __shared__ uint64_t wfull, hfull[2], hempty[2], tfull[2], tempty[2], done;
+    __shared__ uint32_t tslot;
+    __shared__ volatile int fail, halo_issued;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int M = a.B * a.H * a.W_, mt = M / GB_M, nt = (a.cout + BN - 1) / BN;
+    const int n_tile = blockIdx.x % nt, g0 = blockIdx.x / nt, G = gridDim.x / nt, n0 = n_tile * BN;
+    unsigned char* base = ch_smem + ((1024 - (umma::smem_u32(ch_smem) & 1023)) & 1023);
+    unsigned char* sW = base;                       // 9 taps x BN rows x ROWB
+    unsigned char* sH = base + 9 * W_TAP;           // 2 halo buffers (9 * W_TAP is a multiple of 1024)
+    if (warp == 0) umma::tmem_alloc(&tslot, 2 * TC);
+    if (tid == 0) {
+        umma::mbar_init(&wfull, 1);
+        for (int b = 0; b < 2; ++b) {
+            umma::mbar_init(&hfull[b], 1);
+            umma::mbar_init(&hempty[b], 1);
+            umma::mbar_init(&tfull[b], 1);
+            umma::mbar_init(&tempty[b], 4);
+        }
+        umma::mbar_init(&done, 1);
+        fail = 0;
+        halo_issued = 0;
+    }
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+    const int hw = a.H * a.W_;
+    if (warp == 4) {
+        if (lane == 0) {  // TMA producer: weights once, then one halo box per tile
+            umma::mbar_expect_tx(&wfull, (uint32_t)(9 * W_TAP));
+            for (int tap = 0; tap < 9; ++tap)
+                umma::tma_load_2d(sW + tap * W_TAP, &tw, tap * a.cin, n0, &wfull);
+            int i = 0;
+            for (int t = g0; t < mt && !fail; t += G, ++i) {
+                const int buf = i & 1, use = i >> 1;
+                if (use > 0 && !umma::mbar_wait(&hempty[buf], (uint32_t)((use - 1) & 1), GB_WAIT_TRIES)) {
+                    fail = 1;
+                    break;
+                }
+                const int m0 = t * GB_M, b0 = m0 / hw, rem = m0 - b0 * hw, y0 = rem / a.W_, x0 = rem - y0 * a.W_;
+                umma::mbar_expect_tx(&hfull[buf], (uint32_t)(CH_ROWS * ROWB));
+                umma::tma_load_4d(sH + buf * HALO, &tx, 0, x0 - 1, y0 - 1, b0, &hfull[buf]);
+                halo_issued = i + 1;
+            }
+        }
+        __syncwarp();
+    } else if (warp == 5) {
+        if (lane == 0) {  // MMA issuer
+            const uint32_t idesc = umma::idesc_bf16_f32(GB_M, BN);
+            bool wok = umma::mbar_wait(&wfull, 0u, GB_WAIT_TRIES);
+            if (!wok) fail = 1;
+            int i = 0;
+            for (int t = g0; t < mt && !fail; t += G, ++i) {
+                const int buf = i & 1, use = i >> 1;
+                if (!umma::mbar_wait(&hfull[buf], (uint32_t)(use & 1), GB_WAIT_TRIES) ||
+                    (use > 0 && !umma::mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), GB_WAIT_TRIES))) {
+                    fail = 1;
+                    break;
+                }
+                umma::fence_after();
+                const uint32_t acc = tmem + (uint32_t)buf * TC;
+                const uint32_t h0 = umma::smem_u32(sH + buf * HALO), w0 = umma::smem_u32(sW);
+#pragma unroll 1
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int dy = a.tapsign * (tap / 3 - 1), dx = a.tapsign * (tap % 3 - 1);
+                    const uint32_t row0 = (uint32_t)((1 + dy) * CH_PIX + 1 + dx);
+#pragma unroll
+                    for (int ks = 0; ks < CIN / 16; ++ks) {
+                        const uint64_t ad = umma::smem_desc_sw(h0 + row0 * ROWB + ks * 32, ROWB);
+                        const uint64_t bd = umma::smem_desc_sw(w0 + tap * W_TAP + ks * 32, ROWB);
+                        umma::mma_bf16(acc, ad, bd, idesc, (tap > 0 || ks > 0) ? 1u : 0u);
+                    }
+                }
+                umma::commit(&hempty[buf]);
+                umma::commit(&tfull[buf]);
+            }
+            if (fail) {  // let the halo loads already issued land (bounded)
+                for (int j = i; j < halo_issued; ++j)
+                    umma::mbar_wait(&hfull[j & 1], (uint32_t)((j >> 1) & 1), GB_WAIT_TRIES >> 4);
+                if (!wok) umma::mbar_wait(&wfull, 0u, GB_WAIT_TRIES >> 4);
+            }
+            umma::commit(&done);
+            umma::mbar_wait(&done, 0u, GB_WAIT_TRIES);
+        }
+        __syncwarp();
+    } else {  // warps 0-3: epilogue
+        int i = 0;
+        for (int t = g0; t < mt && !fail; t += G, ++i) {
+            const int buf = i & 1, use = i >> 1;
+            if (!umma::mbar_wait(&tfull[buf], (uint32_t)(use & 1), GB_WAIT_TRIES)) {
+                fail = 1;
+                break;
+            }
+            umma::fence_after();
+            conv_epilogue<BN>(a, tmem + (uint32_t)buf * TC, t * GB_M, n0, warp, lane, M);
+            umma::fence_before();
+            __syncwarp();
+            if (lane == 0) umma::mbar_arrive(&tempty[buf]);
+        }
+    }
+    __syncthreads();
+    if (fail && tid == 0) atomicExch(a.err, 1);
+    umma::fence_after();
+    if (warp == 0) umma::tmem_free(tmem, 2 * TC);
+}
+
 // Weights of the input-gradient convolution: Wd[ci][tap * cout + co] = W[co][tap * cin + ci],
 // Kd = 9 cout rounded up to 64.  The taps keep their index: k_conv3x3 with tapsign = -1 reads
 // the neighbour at -d, which is the transposed convolution.
@@ -836,8 +966,64 @@ static impec_status launch_conv_tma(const ConvArgs& a, const ConvTmaPlan& p, cud
     return IMPEC_OK;
 }
 
+template <int BN, int CIN>
+static impec_status launch_conv_halo(const ConvArgs& a, cudaStream_t s) {
+    constexpr int smem = halo_smem<BN, CIN>();
+    static bool attr = false;
+    if (!attr) {
+        IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_conv3x3_halo<BN, CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    TmapEncodeFn enc = tmap_encoder();
+    const CUtensorMapSwizzle sw = CIN == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+    CUtensorMap tx, tw;
+    const cuuint64_t xd[4] = {(cuuint64_t)a.cin, (cuuint64_t)a.W_, (cuuint64_t)a.H, (cuuint64_t)a.B};
+    const cuuint64_t xs[3] = {(cuuint64_t)a.cin * 2, (cuuint64_t)a.W_ * a.cin * 2, (cuuint64_t)a.H * a.W_ * a.cin * 2};
+    const cuuint32_t xb[4] = {(cuuint32_t)CIN, (cuuint32_t)CH_PIX, 3, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.X, xd, xs, xb, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+        set_error("conv: cuTensorMapEncodeTiled (halo) failed");
+        return IMPEC_ERR_CUDA;
+    }
+    const cuuint64_t wd[2] = {(cuuint64_t)a.Kp, (cuuint64_t)a.cout};
+    const cuuint64_t ws[1] = {(cuuint64_t)a.Kp * 2};
+    const cuuint32_t wb[2] = {(cuuint32_t)CIN, (cuuint32_t)BN};
+    if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)a.W, wd, ws, wb, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+        set_error("conv: cuTensorMapEncodeTiled (halo weights) failed");
+        return IMPEC_ERR_CUDA;
+    }
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const int M = a.B * a.H * a.W_, mt = M / GB_M, nt = (a.cout + BN - 1) / BN;
+    const int per_sm = smem <= 110 * 1024 ? 2 : 1;
+    int G = (sms * per_sm) / nt;
+    if (G < 1) G = 1;
+    if (G > mt) G = mt;
+    k_conv3x3_halo<BN, CIN><<<nt * G, CH_THREADS, smem, s>>>(tx, tw, a);
+    IMPEC_CUDA_TRY(cudaGetLastError());
+    return IMPEC_OK;
+}
+
+// The halo kernel: cin 32 or 64, tiles of 128 pixels of one image row, output-channel tiles
+// of at most 64 (the weights of all taps stay in shared memory).
+static bool conv_halo_ok(const ConvArgs& a) {
+    static const bool off = [] {
+        const char* e = getenv("IMPEC_CONV_HALO");
+        return e && e[0] == '0';
+    }();
+    return !off && (a.cin == 32 || a.cin == 64) && a.W_ % GB_M == 0 && tmap_encoder();
+}
+
 template <int BN>
 static impec_status launch_conv_any(const ConvArgs& a, cudaStream_t s) {
+    if (BN <= 64 && conv_halo_ok(a))
+        return a.cin == 64 ? launch_conv_halo<BN <= 64 ? BN : 64, 64>(a, s) : launch_conv_halo<BN <= 64 ? BN : 64, 32>(a, s);
     ConvTmaPlan p;
     if (conv_tma_plan(a, BN, p)) return p.ks == 64 ? launch_conv_tma<BN, 64>(a, p, s) : launch_conv_tma<BN, 32>(a, p, s);
     return launch_conv_bn<BN>(a, s);
@@ -854,6 +1040,7 @@ impec_status launch_conv(const ConvArgs& a, cudaStream_t s) {
     }
     const long long mt = ((long long)a.B * a.H * a.W_ + GB_M - 1) / GB_M;
     auto ctas = [&](int bn) { return mt * ((a.cout + bn - 1) / bn); };
+    if (conv_halo_ok(a)) return a.cout >= 64 ? launch_conv_any<64>(a, s) : launch_conv_any<32>(a, s);
     if (a.cout >= 128 && ctas(128) >= sms) return launch_conv_any<128>(a, s);
     if (a.cout >= 64 && ctas(64) >= sms) return launch_conv_any<64>(a, s);
     return launch_conv_any<32>(a, s);

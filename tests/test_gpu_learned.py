@@ -56,7 +56,10 @@ def _w4(Wt, cin, cout):
     (2, 20, 20, 8, 32), (1, 37, 29, 32, 64), (2, 16, 24, 64, 256), (1, 12, 12, 128, 128),
     # TMA staging: rows of 128 pixels, several rows per box, whole images per box; 32 / 64 channel stages
     (1, 64, 128, 32, 32), (1, 16, 256, 64, 64), (2, 16, 16, 64, 128), (1, 8, 8, 32, 64), (3, 4, 4, 256, 256),
-    (2, 32, 32, 128, 256)])
+    (2, 32, 32, 128, 256),
+    # one halo box for the 9 taps (cin 32 / 64, rows of 128 pixels): 8 outputs, two channel tiles,
+    # several images of two rows
+    (2, 8, 128, 32, 8), (1, 4, 256, 64, 128), (3, 2, 128, 64, 32)])
 def test_conv3x3_forward_and_gradients(engine, B, H, W, cin, cout):
     """Implicit-GEMM convolution on tcgen05: forward (linear; GELU with a skip add), input
     gradient (plain; times gelu'(z) with an added gradient) and weight gradient, against
