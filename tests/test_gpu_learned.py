@@ -275,3 +275,45 @@ def test_trained_network_saves_cycles_over_the_previous_step(engine):
     print(f"validation MSE {v0:.3f} -> {v1:.3f}; V-cycles over 36 solves: {its}")
     assert its["learned"] < its["previous"], its
     net.close()
+
+
+@pytest.mark.parametrize("factor", [1, 2])
+def test_learned_features_match_a_recomputation(engine, factor):
+    """The features a solve records equal a recomputation from the state it started from
+    (bf16 rounding): mean 4 log(1 - c + M^(1/4) c), mean log K, the summed well rates q dA / I,
+    and the centred previous pressure over its RMS, each over factor x factor cells."""
+    import math
+    import torch
+    from impec2d_gb300.workloads import device_view, realisation
+    E = engine
+    N = 64
+    ctx = realisation(E, N, 6, ell=8.0, warm_start=1)  # lognormal K, M from the seed
+    rec = E.Net(seed=0)
+    ctx.run_steps(3)
+    rec.attach(ctx, factor=factor, mode=2)
+    cptr, pptr, _, _, qptr = ctx.state_ptrs()
+    c0 = device_view(cptr, (N, N)).clone()
+    p0 = device_view(pptr, (N, N)).clone()
+    q = device_view(qptr, (N, N)).clone()
+    ctx.step()
+    h = N // factor
+    X = torch.empty((h, h, 8), dtype=torch.bfloat16, device="cuda")
+    E.Net.last_features(ctx, X)
+    P = ctx.P
+    m14 = (P.mu_res / P.mu_inj) ** 0.25
+    dA = (P.x_ub - P.x_lb) / N * (P.y_ub - P.y_lb) / N
+    from impec2d_gb300.workloads import grf
+    K = torch.exp(0.5 * grf(N, 8.0, 5000 + 6))
+    pool = lambda a: a.reshape(h, factor, h, factor).mean(dim=(1, 3))
+    ref = [pool(4.0 * torch.log(1.0 - c0 + m14 * c0)), pool(torch.log(K)),
+           (q * dA / P.I).reshape(h, factor, h, factor).sum(dim=(1, 3))]
+    xm = pool(p0)
+    ref.append((xm - xm.mean()) / xm.std(unbiased=False))
+    for ch, r in enumerate(ref):
+        got = X[..., ch].double()
+        scale = max(r.abs().max().item(), 1e-30)
+        assert (got - r).abs().max().item() <= 8e-3 * scale + 1e-6, (ch, (got - r).abs().max().item(), scale)
+    assert math.isclose(X[..., 4].double().pow(2).mean().sqrt().item(), 1.0, rel_tol=2e-2)
+    E.Net.detach(ctx)
+    rec.close()
+    ctx.close()
