@@ -456,8 +456,10 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
     if (warp == 0) umma::tmem_free(tmem, 2 * TC);
 }
 
-// Halo variant for cin = 32 or 64 and W a multiple of 128 (a tile is 128 pixels of one image
-// row).  Per tile, one 4D TMA box brings the halo: CIN channels x 130 pixels (x0 - 1 .. x0 + 128)
+// Halo variant for cin = 8, 32 or 64 and W a multiple of 128 (a tile is 128 pixels of one image
+// row).  CIN is the channel width of the boxes: 64, 32, or 16 for 8-channel inputs, whose box
+// channels 8..15 lie outside the tensor and load as zeros (they meet the next tap's weights in
+// the MMA, which therefore add nothing).  Per tile, one 4D TMA box brings the halo: CIN channels x 130 pixels (x0 - 1 .. x0 + 128)
 // x 3 rows (y0 - 1 .. y0 + 1), zero-filled outside the image, as 390 swizzled rows of CIN * 2
 // bytes.  The A operand of tap (dy, dx) is the 128 rows starting at row (1 + dy) * 130 + 1 + dx
 // of that box: the descriptor's start moves there, and since the hardware applies the swizzle
@@ -714,7 +716,10 @@ __global__ void __launch_bounds__(GB_THREADS) k_conv_wgrad(const __nv_bfloat16* 
 // pixels, CA-element MN blocks), B = 128 / CB boxes of the layer input at one tap's offset (CB
 // channels x the stage's 64 pixels as a 4D box, zero-filled outside the image; column blocks
 // beyond 9 cin point past the channels and load zeros).  CA, CB = 64 (128-byte swizzle) or 32
-// (64-byte).  Roles as in k_conv3x3_tma, one tile per CTA.
+// (64-byte).  8-channel operands use 32-channel boxes, whose channels 8..31 lie outside the
+// tensor and load as zeros: for cout = 8 these are rows of zeros, for cin = 8 each column block
+// holds one tap (columns c >= cin of a block are discarded).  Roles as in k_conv3x3_tma, one
+// tile per CTA.
 constexpr int WG_THREADS = 192, WG_STAGES = 6, WG_PIX = 64;
 
 template <int CA, int CB>
@@ -765,8 +770,16 @@ __global__ void __launch_bounds__(WG_THREADS) k_conv_wgrad_tma(const __grid_cons
                 for (int i = 0; i < 128 / CA; ++i) umma::tma_load_2d(sA + i * A_BLK, &tz, co0 + i * CA, p0, &full[slot]);
 #pragma unroll
                 for (int j = 0; j < 128 / CB; ++j) {
-                    const int k = k0 + j * CB, tap = k / cin;
-                    const int c0 = tap < 9 ? k - tap * cin : cin;  // past the taps: a box of zeros
+                    int tap, c0;
+                    if (cin >= CB) {
+                        const int k = k0 + j * CB;
+                        tap = k / cin;
+                        c0 = k - tap * cin;
+                    } else {  // one tap per block
+                        tap = blockIdx.x * (128 / CB) + j;
+                        c0 = 0;
+                    }
+                    if (tap >= 9) c0 = cin;  // past the taps: a box of zeros
                     const int t = tap < 9 ? tap : 4;
                     umma::tma_load_4d(sA + A_BYTES + j * B_BLK, &tx, c0, x0 + t % 3 - 1, y0 + t / 3 - 1, b0,
                                       &full[slot]);
@@ -813,7 +826,14 @@ __global__ void __launch_bounds__(WG_THREADS) k_conv_wgrad_tma(const __grid_cons
             if (co >= cout) continue;
 #pragma unroll
             for (int q = 0; q < 32; ++q) {
-                const int k = k0 + cb * 32 + q;
+                const int col = cb * 32 + q;
+                int k;
+                if (cin >= CB) {
+                    k = k0 + col;
+                } else {  // column block col / CB is tap blockIdx.x * (128 / CB) + col / CB
+                    const int tap = blockIdx.x * (128 / CB) + col / CB, c = col % CB;
+                    k = tap < 9 && c < cin ? tap * cin + c : 9 * cin;
+                }
                 if (k < 9 * cin) atomicAdd(dW + (size_t)co * Kp + k, v[q]);
             }
         }
@@ -975,7 +995,8 @@ static impec_status launch_conv_halo(const ConvArgs& a, cudaStream_t s) {
         attr = true;
     }
     TmapEncodeFn enc = tmap_encoder();
-    const CUtensorMapSwizzle sw = CIN == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+    const CUtensorMapSwizzle sw = CIN == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                            : (CIN == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
     CUtensorMap tx, tw;
     const cuuint64_t xd[4] = {(cuuint64_t)a.cin, (cuuint64_t)a.W_, (cuuint64_t)a.H, (cuuint64_t)a.B};
     const cuuint64_t xs[3] = {(cuuint64_t)a.cin * 2, (cuuint64_t)a.W_ * a.cin * 2, (cuuint64_t)a.H * a.W_ * a.cin * 2};
@@ -1010,20 +1031,22 @@ static impec_status launch_conv_halo(const ConvArgs& a, cudaStream_t s) {
     return IMPEC_OK;
 }
 
-// The halo kernel: cin 32 or 64, tiles of 128 pixels of one image row, output-channel tiles
+// The halo kernel: cin 8, 32 or 64, tiles of 128 pixels of one image row, output-channel tiles
 // of at most 64 (the weights of all taps stay in shared memory).
 static bool conv_halo_ok(const ConvArgs& a) {
     static const bool off = [] {
         const char* e = getenv("IMPEC_CONV_HALO");
         return e && e[0] == '0';
     }();
-    return !off && (a.cin == 32 || a.cin == 64) && a.W_ % GB_M == 0 && tmap_encoder();
+    return !off && (a.cin == 8 || a.cin == 32 || a.cin == 64) && a.W_ % GB_M == 0 && tmap_encoder();
 }
 
 template <int BN>
 static impec_status launch_conv_any(const ConvArgs& a, cudaStream_t s) {
+    constexpr int HB = BN <= 64 ? BN : 64;
     if (BN <= 64 && conv_halo_ok(a))
-        return a.cin == 64 ? launch_conv_halo<BN <= 64 ? BN : 64, 64>(a, s) : launch_conv_halo<BN <= 64 ? BN : 64, 32>(a, s);
+        return a.cin == 64 ? launch_conv_halo<HB, 64>(a, s)
+                           : (a.cin == 32 ? launch_conv_halo<HB, 32>(a, s) : launch_conv_halo<HB, 16>(a, s));
     ConvTmaPlan p;
     if (conv_tma_plan(a, BN, p)) return p.ks == 64 ? launch_conv_tma<BN, 64>(a, p, s) : launch_conv_tma<BN, 32>(a, p, s);
     return launch_conv_bn<BN>(a, s);
@@ -1053,7 +1076,9 @@ static bool wgrad_tma_plan(int B, int H, int W, int cin, int cout, int* wb, int*
         const char* e = getenv("IMPEC_CONV_TMA");
         return e && e[0] == '0';
     }();
-    if (off || cin % 32 || cout % 32 || ((long long)B * H * W) % WG_PIX || !tmap_encoder()) return false;
+    if (off || (cin % 32 && cin != 8) || (cout % 32 && cout != 8) || ((long long)B * H * W) % WG_PIX ||
+        !tmap_encoder())
+        return false;
     if (W >= WG_PIX) {
         if (W % WG_PIX) return false;
         *wb = WG_PIX, *hb = 1, *bb = 1;
@@ -1105,7 +1130,7 @@ static impec_status launch_wgrad_tma(const __nv_bfloat16* dZ, const __nv_bfloat1
         set_error("wgrad: cuTensorMapEncodeTiled (activations) failed");
         return IMPEC_ERR_CUDA;
     }
-    const int nt = (9 * cin + 127) / 128, mt = (cout + 127) / 128;
+    const int nt = cin >= CB ? (9 * cin + 127) / 128 : (9 + 128 / CB - 1) / (128 / CB), mt = (cout + 127) / 128;
     int splits = (2 * num_sms + nt * mt - 1) / (nt * mt);
     int per = (P + splits - 1) / splits;
     per = (per + WG_PIX - 1) / WG_PIX * WG_PIX;
@@ -1120,7 +1145,7 @@ impec_status launch_wgrad(const __nv_bfloat16* dZ, const __nv_bfloat16* X, int B
                           float* dW, int* err, int num_sms, cudaStream_t s) {
     int wb, hb, bb;
     if (wgrad_tma_plan(B, H, W_, cin, cout, &wb, &hb, &bb)) {
-        const bool a64 = cout % 64 == 0, b64 = cin % 64 == 0;
+        const bool a64 = cout % 64 == 0, b64 = cin % 64 == 0;  // 8-channel operands take 32-channel boxes
         if (a64 && b64) return launch_wgrad_tma<64, 64>(dZ, X, B, H, W_, cin, cout, dW, err, num_sms, wb, hb, bb, s);
         if (a64) return launch_wgrad_tma<64, 32>(dZ, X, B, H, W_, cin, cout, dW, err, num_sms, wb, hb, bb, s);
         if (b64) return launch_wgrad_tma<32, 64>(dZ, X, B, H, W_, cin, cout, dW, err, num_sms, wb, hb, bb, s);

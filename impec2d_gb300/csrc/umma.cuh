@@ -27,17 +27,23 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes
     return d;
 }
 
-// Descriptor of a K-major tile written by TMA with 128- or 64-byte swizzling: rows of 128
-// (64) bytes, 8-row atoms of 1024 (512) bytes stacked along M/N (stride byte offset), layout
-// code 2 (128B) or 4 (64B) in bits 61-63.  A K step of 16 bf16 inside the atom advances the
-// start address by 32 bytes.
+// Layout code (bits 61-63) of the 128-, 64- and 32-byte swizzles.
+__host__ __device__ constexpr uint32_t swizzle_code(int row_bytes) {
+    return row_bytes == 128 ? 2u : (row_bytes == 64 ? 4u : 6u);
+}
+
+// Descriptor of a K-major tile written by TMA with 128-, 64- or 32-byte swizzling: rows of
+// row_bytes, 8-row atoms stacked along M/N (stride byte offset 8 * row_bytes).  A K step of 16
+// bf16 inside the row advances the start address by 32 bytes.  The swizzle is applied on
+// absolute shared-memory addresses (base offset 0), so a start that moves by whole rows inside
+// an atom (a shifted operand) needs nothing else.
 __device__ __forceinline__ uint64_t smem_desc_sw(uint32_t saddr, int row_bytes) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
     d |= (uint64_t)1 << 16;                                   // leading byte offset: unused for swizzled K-major
     d |= (uint64_t)(((uint32_t)(8 * row_bytes) >> 4) & 0x3FFFu) << 32;
     d |= (uint64_t)1 << 46;
-    d |= (uint64_t)(row_bytes == 128 ? 2 : 4) << 61;
+    d |= (uint64_t)swizzle_code(row_bytes) << 61;
     return d;
 }
 
@@ -50,7 +56,7 @@ __device__ __forceinline__ uint64_t smem_desc_mn(uint32_t saddr, uint32_t lbo, u
     d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
     d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
     d |= (uint64_t)1 << 46;
-    d |= (uint64_t)(row_bytes == 128 ? 2 : 4) << 61;
+    d |= (uint64_t)swizzle_code(row_bytes) << 61;
     return d;
 }
 

@@ -59,7 +59,9 @@ def _w4(Wt, cin, cout):
     (2, 32, 32, 128, 256),
     # one halo box for the 9 taps (cin 32 / 64, rows of 128 pixels): 8 outputs, two channel tiles,
     # several images of two rows
-    (2, 8, 128, 32, 8), (1, 4, 256, 64, 128), (3, 2, 128, 64, 32)])
+    (2, 8, 128, 32, 8), (1, 4, 256, 64, 128), (3, 2, 128, 64, 32),
+    # 8 input channels: halo boxes padded to 16 channels; weight gradients on 32-channel boxes
+    (2, 4, 128, 8, 32), (1, 8, 256, 8, 64)])
 def test_conv3x3_forward_and_gradients(engine, B, H, W, cin, cout):
     """Implicit-GEMM convolution on tcgen05: forward (linear; GELU with a skip add), input
     gradient (plain; times gelu'(z) with an added gradient) and weight gradient, against
