@@ -118,22 +118,24 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 
-// Epilogue of both convolution kernels: warp w (0-3) reads TMEM lanes 32w .. 32w + 31 (one
-// output pixel per thread) in blocks of 32 accumulator columns.
-template <int BN>
+// Epilogue of the convolution kernels, on NW (4 or 8) warps: warp w reads TMEM lanes
+// 32 (w % 4) .. + 31 (one output pixel per thread) and the 16-column groups w / 4,
+// w / 4 + NW / 4, ... of the accumulator.
+template <int BN, int NW>
 __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t tmem, int m0, int n0, int warp, int lane,
                                               int M) {
-        const int m = m0 + warp * 32 + lane;
+    const int quarter = warp & 3, part = warp >> 2;
+    const int m = m0 + quarter * 32 + lane;
 #pragma unroll 1
-    for (int cb = 0; cb < (BN + 31) / 32; ++cb) {
-        float v[32];
-        umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
+    for (int g = part; g < (BN + 15) / 16; g += NW / 4) {
+        float v[16];
+        umma::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(g * 16), v);
         if (m >= M) continue;
         const size_t row = (size_t)m * a.cout;
-        const int nb = n0 + cb * 32;
-        if (nb + 32 <= a.cout && (a.cout & 7) == 0) {  // 32 whole channels: 16-byte accesses
+        const int nb = n0 + g * 16;
+        if (nb + 16 <= a.cout && (a.cout & 7) == 0) {  // 16 whole channels: 16-byte accesses
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < 2; ++q) {
                 float z[8], y[8];
                 const size_t o = row + nb + 8 * q;
 #pragma unroll
@@ -182,9 +184,9 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t tmem, 
             continue;
         }
 #pragma unroll
-        for (int k = 0; k < 32; ++k) {
+        for (int k = 0; k < 16; ++k) {
             const int n = nb + k;
-            if (n >= a.cout || cb * 32 + k >= BN) continue;
+            if (n >= a.cout || g * 16 + k >= BN) continue;
             float z = v[k] + (a.bias ? a.bias[n] : 0.0f);
             if (a.gz) {  // input gradient: (acc + add) * gelu'(gz)
                 if (a.R) a.R[row + n] = __float2bfloat16(z);
@@ -311,7 +313,7 @@ __global__ void __launch_bounds__(CV_THREADS) k_conv3x3(ConvArgs a) {
     const bool ok = __syncthreads_and(fin) != 0 && fail == 0;
     if (ok && warp < 4) {
         umma::fence_after();
-        conv_epilogue<BN>(a, tmem, m0, n0, warp, lane, M);
+        conv_epilogue<BN, 4>(a, tmem, m0, n0, warp, lane, M);
     }
     if (!ok && tid == 0) atomicExch(a.err, 1);
     umma::fence_before();
@@ -328,14 +330,16 @@ __global__ void __launch_bounds__(CV_THREADS) k_conv3x3(ConvArgs a) {
 //
 // Persistent: each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ... with the
 // accumulator double-buffered in TMEM, so that the loads and MMAs of tile i+1 overlap the
-// epilogue of tile i.  Roles: lane 0 of warp 4 issues both loads of every stage on the
-// stage's "full" mbarrier (expected bytes); lane 0 of warp 5 waits for the accumulator buffer
+// epilogue of tile i.  Roles: lane 0 of the producer warp issues both loads of every stage on
+// the stage's "full" mbarrier (expected bytes); lane 0 of the MMA warp waits for the accumulator buffer
 // to be free ("tmem_empty", one arrival per epilogue warp), issues the MMAs of each stage,
 // commits them to the stage's "empty" mbarrier and, after a tile's last stage, to the
-// buffer's "tmem_full"; warps 0-3 wait for "tmem_full", run the epilogue and release the
+// buffer's "tmem_full"; the epilogue warps wait for "tmem_full", run the epilogue and release the
 // buffer.  Stages: as many as fit in 200 KB (at most 8).  Stage and buffer uses are counted
-// across tiles, which gives every wait its phase parity.
-constexpr int CT_THREADS = 192, CT_MAX_STAGES = 8;
+// across tiles, which gives every wait its phase parity.  (Warp numbers: the epilogue runs on
+// warps 0 .. EPI_WARPS - 1, two per TMEM lane quarter; the producer is warp EPI_WARPS and the
+// MMA issuer warp EPI_WARPS + 1.)
+constexpr int CT_THREADS = 320, CT_MAX_STAGES = 8, EPI_WARPS = 8;
 
 struct ConvTmaPlan {
     int ks, stages, wbox, hbox, bbox;
@@ -363,7 +367,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
         }
         for (int b = 0; b < 2; ++b) {
             umma::mbar_init(&tfull[b], 1);
-            umma::mbar_init(&tempty[b], 4);
+            umma::mbar_init(&tempty[b], EPI_WARPS);
         }
         umma::mbar_init(&done, 1);
         fail = 0;
@@ -374,7 +378,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
     umma::fence_after();
     const uint32_t tmem = tslot;
     const int cs = a.cin / KS, nk = 9 * cs, hw = a.H * a.W_;
-    if (warp == 4) {
+    if (warp == EPI_WARPS) {
         if (lane == 0) {  // TMA producer
             int g = 0;
             for (int t = blockIdx.x; t < tiles && !fail; t += gridDim.x) {
@@ -397,7 +401,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
             }
         }
         __syncwarp();
-    } else if (warp == 5) {
+    } else if (warp == EPI_WARPS + 1) {
         if (lane == 0) {  // MMA issuer
             const uint32_t idesc = umma::idesc_bf16_f32(GB_M, BN);
             int g = 0, i = 0;
@@ -435,7 +439,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
             umma::mbar_wait(&done, 0u, GB_WAIT_TRIES);
         }
         __syncwarp();
-    } else {  // warps 0-3: epilogue
+    } else {  // warps 0 .. EPI_WARPS - 1: epilogue
         int i = 0;
         for (int t = blockIdx.x; t < tiles && !fail; t += gridDim.x, ++i) {
             const int buf = i & 1, buse = i >> 1;
@@ -444,7 +448,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
                 break;
             }
             umma::fence_after();
-            conv_epilogue<BN>(a, tmem + (uint32_t)buf * TC, (t / nt) * GB_M, (t % nt) * BN, warp, lane, M);
+            conv_epilogue<BN, EPI_WARPS>(a, tmem + (uint32_t)buf * TC, (t / nt) * GB_M, (t % nt) * BN, warp, lane, M);
             umma::fence_before();
             __syncwarp();
             if (lane == 0) umma::mbar_arrive(&tempty[buf]);
@@ -468,8 +472,8 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv3x3_tma(const __grid_constan
 // of its BN output channels for all 9 taps resident (loaded once) and walks the tiles
 // blockIdx.x / nt, + gridDim.x / nt, ...; the halo and the TMEM accumulator are
 // double-buffered so that the next tile's load and MMAs overlap the epilogue.  Roles as in
-// k_conv3x3_tma (lane 0 of warp 4: TMA, lane 0 of warp 5: MMA, warps 0-3: epilogue).
-constexpr int CH_THREADS = 192, CH_PIX = 130, CH_ROWS = 3 * CH_PIX;
+// k_conv3x3_tma (producer, MMA issuer and EPI_WARPS epilogue warps).
+constexpr int CH_THREADS = 320, CH_PIX = 130, CH_ROWS = 3 * CH_PIX;
 
 template <int CIN>
 __host__ __device__ constexpr int halo_bytes() { return (CH_ROWS * CIN * 2 + 1023) / 1024 * 1024; }
@@ -498,7 +502,7 @@ __global__ void __launch_bounds__(CH_THREADS) k_conv3x3_halo(const __grid_consta
             umma::mbar_init(&hfull[b], 1);
             umma::mbar_init(&hempty[b], 1);
             umma::mbar_init(&tfull[b], 1);
-            umma::mbar_init(&tempty[b], 4);
+            umma::mbar_init(&tempty[b], EPI_WARPS);
         }
         umma::mbar_init(&done, 1);
         fail = 0;
@@ -509,7 +513,7 @@ __global__ void __launch_bounds__(CH_THREADS) k_conv3x3_halo(const __grid_consta
     umma::fence_after();
     const uint32_t tmem = tslot;
     const int hw = a.H * a.W_;
-    if (warp == 4) {
+    if (warp == EPI_WARPS) {
         if (lane == 0) {  // TMA producer: weights once, then one halo box per tile
             umma::mbar_expect_tx(&wfull, (uint32_t)(9 * W_TAP));
             for (int tap = 0; tap < 9; ++tap)
@@ -528,7 +532,7 @@ __global__ void __launch_bounds__(CH_THREADS) k_conv3x3_halo(const __grid_consta
             }
         }
         __syncwarp();
-    } else if (warp == 5) {
+    } else if (warp == EPI_WARPS + 1) {
         if (lane == 0) {  // MMA issuer
             const uint32_t idesc = umma::idesc_bf16_f32(GB_M, BN);
             bool wok = umma::mbar_wait(&wfull, 0u, GB_WAIT_TRIES);
@@ -567,7 +571,7 @@ __global__ void __launch_bounds__(CH_THREADS) k_conv3x3_halo(const __grid_consta
             umma::mbar_wait(&done, 0u, GB_WAIT_TRIES);
         }
         __syncwarp();
-    } else {  // warps 0-3: epilogue
+    } else {  // warps 0 .. EPI_WARPS - 1: epilogue
         int i = 0;
         for (int t = g0; t < mt && !fail; t += G, ++i) {
             const int buf = i & 1, use = i >> 1;
@@ -576,7 +580,7 @@ __global__ void __launch_bounds__(CH_THREADS) k_conv3x3_halo(const __grid_consta
                 break;
             }
             umma::fence_after();
-            conv_epilogue<BN>(a, tmem + (uint32_t)buf * TC, t * GB_M, n0, warp, lane, M);
+            conv_epilogue<BN, EPI_WARPS>(a, tmem + (uint32_t)buf * TC, t * GB_M, n0, warp, lane, M);
             umma::fence_before();
             __syncwarp();
             if (lane == 0) umma::mbar_arrive(&tempty[buf]);
