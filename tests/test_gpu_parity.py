@@ -502,3 +502,46 @@ def test_horizontal_source_rate_update_in_place(engine):
     ctx.download(ca, None, None, ghost=2)
     ref.download(cb, None, None, ghost=2)
     assert np.array_equal(ca, cb)
+
+
+def test_quarter_five_spot_integrated_quantities(engine, oracle_lib):
+    """A whole displacement, quarter-five-spot on the diagonal grid (the reference's CPU case
+    at 32 x 32, first-order upwind, M = 41, porosity 1), to 1 pore volume injected (~780
+    steps), engine and oracle in lockstep.  Past breakthrough the unstable displacement lets
+    round-off grow, so the comparison is by integrated quantities: the time step of every
+    step, the breakthrough step and time (produced volume above 1e-3), the produced volume
+    at the end, and mass balance."""
+    E = engine
+    N = 32
+    P, ctx = _ctx(E, N, N, stype=1, hmtype=0, nu=1.0, cfl=0.5, mu_res=41.0, mu_inj=1.0, eps=1e-10, para_eps=1e-10)
+    OP = oparams(P)
+    q = source(OP)
+    ctx.upload(cell_ghost(OP, np.zeros((N, N))), q, ghost=2)
+    ctx.set_time(0.0)
+    c = cell_ghost(OP, np.zeros((N, N)))
+    p, vv = np.zeros(O.scalar_shape(OP)), np.zeros(O.vel_shape(OP))
+    S = O.State()
+    S.prev_first_sweep = 1
+    tidx = C.c_int(0)
+    bt_e = bt_o = None
+    worst_dt = 0.0
+    n = 0
+    while S.t < 1.0:
+        oracle_lib.or_impes_step(C.byref(OP), C.byref(S), O.ptr(c), O.ptr(p), O.ptr(vv), O.ptr(q), None, 0,
+                                 C.byref(tidx), 0, 1e-13)
+        info = ctx.step()
+        n += 1
+        worst_dt = max(worst_dt, abs(info.dt - S.dt) / S.dt)
+        if bt_o is None and S.total_outflux > 1e-3:
+            bt_o = (n, S.t)
+        if bt_e is None and info.total_outflux > 1e-3:
+            bt_e = (n, info.t)
+        assert info.mass_err < 1e-12 and S.mass_err < 1e-12
+    rel_out = abs(info.total_outflux - S.total_outflux) / S.total_outflux
+    print(f"{n} steps to t = {S.t:.4f}: worst dt deviation {worst_dt:.2e}; breakthrough engine {bt_e}, "
+          f"oracle {bt_o}; produced {info.total_outflux:.6f} vs {S.total_outflux:.6f} (rel {rel_out:.2e})")
+    assert worst_dt <= 1e-8
+    assert bt_e is not None and bt_o is not None and abs(bt_e[0] - bt_o[0]) <= 1
+    assert abs(bt_e[1] - bt_o[1]) <= 1e-9 * bt_o[1]
+    assert rel_out <= 1e-9  # measured: 3e-12
+    ctx.close()
