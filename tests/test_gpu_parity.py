@@ -504,16 +504,20 @@ def test_horizontal_source_rate_update_in_place(engine):
     assert np.array_equal(ca, cb)
 
 
-def test_quarter_five_spot_integrated_quantities(engine, oracle_lib):
-    """A whole displacement, quarter-five-spot on the diagonal grid (the reference's CPU case
-    at 32 x 32, first-order upwind, M = 41, porosity 1), to 1 pore volume injected (~780
-    steps), engine and oracle in lockstep.  Past breakthrough the unstable displacement lets
-    round-off grow, so the comparison is by integrated quantities: the time step of every
-    step, the breakthrough step and time (produced volume above 1e-3), the produced volume
-    at the end, and mass balance."""
+@pytest.mark.parametrize("cfg", ["diag_upwind", "par_muscl_disp"])
+def test_quarter_five_spot_integrated_quantities(engine, oracle_lib, cfg):
+    """A whole displacement at 32 x 32, M = 41, porosity 1, to 1 pore volume injected, engine
+    and oracle in lockstep: the reference's CPU case (diagonal grid, first-order upwind) and
+    the benchmark's method (parallel grid with four corner wells, MUSCL, Crank-Nicolson
+    Peaceman dispersion).  Past breakthrough the unstable displacement lets round-off grow,
+    so the comparison is by integrated quantities: the time step of every step, the
+    breakthrough step and time (produced volume above 1e-3), the produced volume at the end,
+    and mass balance."""
     E = engine
     N = 32
-    P, ctx = _ctx(E, N, N, stype=1, hmtype=0, nu=1.0, cfl=0.5, mu_res=41.0, mu_inj=1.0, eps=1e-10, para_eps=1e-10)
+    kw = dict(diag_upwind=dict(stype=1, hmtype=0),
+              par_muscl_disp=dict(stype=0, hmtype=4, diffusion=1, alpha_l=1e-3, alpha_t=1e-4))[cfg]
+    P, ctx = _ctx(E, N, N, nu=1.0, cfl=0.5, mu_res=41.0, mu_inj=1.0, eps=1e-10, para_eps=1e-10, **kw)
     OP = oparams(P)
     q = source(OP)
     ctx.upload(cell_ghost(OP, np.zeros((N, N))), q, ghost=2)
@@ -524,9 +528,10 @@ def test_quarter_five_spot_integrated_quantities(engine, oracle_lib):
     S.prev_first_sweep = 1
     tidx = C.c_int(0)
     bt_e = bt_o = None
-    worst_dt = 0.0
+    worst_dt = mass_e = mass_o = 0.0
     n = 0
-    while S.t < 1.0:
+    t_end = 1.0 * (P.x_ub - P.x_lb) * (P.y_ub - P.y_lb) / (2.0 if P.stype == 0 else 1.0)  # 1 PV
+    while S.t < t_end:
         oracle_lib.or_impes_step(C.byref(OP), C.byref(S), O.ptr(c), O.ptr(p), O.ptr(vv), O.ptr(q), None, 0,
                                  C.byref(tidx), 0, 1e-13)
         info = ctx.step()
@@ -536,10 +541,13 @@ def test_quarter_five_spot_integrated_quantities(engine, oracle_lib):
             bt_o = (n, S.t)
         if bt_e is None and info.total_outflux > 1e-3:
             bt_e = (n, info.t)
-        assert info.mass_err < 1e-12 and S.mass_err < 1e-12
+        mass_e, mass_o = max(mass_e, info.mass_err), max(mass_o, S.mass_err)
     rel_out = abs(info.total_outflux - S.total_outflux) / S.total_outflux
     print(f"{n} steps to t = {S.t:.4f}: worst dt deviation {worst_dt:.2e}; breakthrough engine {bt_e}, "
-          f"oracle {bt_o}; produced {info.total_outflux:.6f} vs {S.total_outflux:.6f} (rel {rel_out:.2e})")
+          f"oracle {bt_o}; produced {info.total_outflux:.6f} vs {S.total_outflux:.6f} (rel {rel_out:.2e}); "
+          f"max mass error engine {mass_e:.1e}, oracle {mass_o:.1e}")
+    # mass balance: the CN solves stop at a 1e-10 relative residual, which is not exactly conservative
+    assert mass_e <= 1e-9 and mass_o <= 1e-9
     assert worst_dt <= 1e-8
     assert bt_e is not None and bt_o is not None and abs(bt_e[0] - bt_o[0]) <= 1
     assert abs(bt_e[1] - bt_o[1]) <= 1e-9 * bt_o[1]
