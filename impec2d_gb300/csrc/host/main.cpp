@@ -1,5 +1,5 @@
 // Impec2D command-line driver: `Impec2D [config.cfg]`, as the reference's main
-// (src/Driver.cpp:58-87) but single-process: every GPU machine runs one engine.
+// (src/Driver.cpp:58-87) but single-process: one engine per GPU.
 #include <cstdio>
 #include <string>
 

@@ -894,7 +894,7 @@ static impec_status launch_conv_bn(const ConvArgs& a, cudaStream_t s) {
     return IMPEC_OK;
 }
 
-// ---- TMA path: tensor maps through the driver's cuTensorMapEncodeTiled (runtime entry point).
+// ---- TMA path: tensor maps through the CUDA driver API's cuTensorMapEncodeTiled (runtime entry point).
 typedef CUresult (*TmapEncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);

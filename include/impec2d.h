@@ -276,7 +276,7 @@ impec_status impec_advect_symmetric_noalloc(const impec_params* P, double* c_dev
 
 /* ---- ensembles of independent realisations ---- */
 /* One CUDA graph holding each member's whole IMPES step as a parallel branch, so one launch
- * advances every member (BASELINE's batched-ensemble mode; no counterpart in the reference,
+ * advances every member (the batched-ensemble mode; no counterpart in the reference,
  * whose driver runs one realisation per process).  Members must not use alternating sweeps and
  * run without output-time clipping.  A member's later changes of tunables are not seen by an
  * existing ensemble: create it again.  While an ensemble lives, calls that would free or move
