@@ -41,6 +41,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--n", type=int, default=None, help="grid side (default 1024; 4096 for --study pressure)")
+    ap.add_argument("--nu", type=float, default=1.0,
+                    help="stencil weight: 1 = five-point (the default workload), 2/3 = the reference examples' "
+                         "weighted nine-point operator")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
@@ -101,9 +104,9 @@ def initial_state(N, seed=1234):
     return c, q
 
 
-def workload_params(E, N, precision):
+def workload_params(E, N, precision, nu=1.0):
     L = math.sqrt(2.0)
-    return E.default_params(N, N, x_ub=L, y_ub=L, stype=E.PARALLEL, hmtype=E.MUSCL, nu=1.0, diffusion=1,
+    return E.default_params(N, N, x_ub=L, y_ub=L, stype=E.PARALLEL, hmtype=E.MUSCL, nu=nu, diffusion=1,
                             alpha_l=1e-3, alpha_t=1e-4, Dm=1e-6, cfl=0.5, porosity=1.0, eps=1e-10, para_eps=1e-10,
                             precision=E.PREC_MIXED if precision == "mixed" else E.PREC_FP64, max_cycles=200)
 
@@ -279,7 +282,7 @@ def study_warmstart(args):
     out = {"study": "warmstart", "workload": f"parallel quarter-five-spot {N}x{N} (IMPES steps as in the bench)",
            "steps": args.steps}
     for warm in (0, 1):
-        P = workload_params(E, N, args.precision)
+        P = workload_params(E, N, args.precision, args.nu)
         P.warm_start = warm
         ctx = E.Context(P)
         c0, q = initial_state(N)
@@ -589,7 +592,7 @@ def main():
         dist.init_process_group("nccl")
     B.build()
     N = args.n or N_DEFAULT
-    P = workload_params(E, N, args.precision)
+    P = workload_params(E, N, args.precision, args.nu)
     ctx = E.Context(P)
     c0, q = initial_state(N)
     g = 2
@@ -654,7 +657,7 @@ def main():
     hc = np.zeros((N + 2 * g, N + 2 * g))
     ctx.download(hc, None, None, ghost=g)
     for prec in ("fp64", "mixed"):
-        Pp = workload_params(E, N, prec)
+        Pp = workload_params(E, N, prec, args.nu)
         cp = E.Context(Pp)
         cp.upload(hc, q, ghost=g)
         cyc, rr = cp.pressure_solve_resident()  # capture + warm-up
@@ -677,7 +680,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"parallel quarter-five-spot {N}x{N}, MUSCL + CN Peaceman (alpha_l 1e-3, alpha_t 1e-4,"
-                                   f" Dm 1e-6), MG V(2,2) to 1e-10",
+                                   f" Dm 1e-6), MG V(2,2) to 1e-10"
+                                   + (f", nu = {args.nu:.4g} (weighted nine-point)" if args.nu != 1.0 else ""),
                        "precision": args.precision, "l2": "flushed (256 MB write) between timed steps",
                        "parallelism": f"replicas x{world}"},
             "solver": {"mg_cycles": info.its, "relres": info.relres, "cn_sweeps": info.para_its, "dt": info.dt,

@@ -154,8 +154,11 @@ def time_kernel(ctx, which: int, reps: int = 20):
 
 
 # FP64 operations (FMA, MUL or ADD, one per lane) per cell of one launch of each probed kernel,
-# as the ncu instruction counts show them: the fine sweep is 4 DFMA + 1 DMUL per cell and colour.
+# as the ncu instruction counts show them: the five-point sweep is 4 DFMA + 1 DMUL per cell and
+# colour; the nine-point sweep (nu < 1) 8 DFMA + 1 DMUL + 1 DADD.
 _FP64_OPS_PER_CELL = {0: 5.0, 2: 6.0}
+_NINE_POINT = {0: ("k_gs4_exp9<double> (fine four-colour GS sweep, nine-point, FP64)", 10.0),
+               1: ("k_gs4_exp9<float> (fine four-colour GS sweep, nine-point, FP32)", None)}
 
 
 def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None, traffic_path: str | None = None):
@@ -174,20 +177,23 @@ def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None, traffi
         except Exception:  # noqa: BLE001
             pass
     ach = b / (ms * 1e-3) / 1e9
-    out = {"bound": "hbm", "kernel": KERNELS[which], "achieved": ach, "peak": peak, "unit": "GB/s",
+    nine = P.nu != 1.0 and which in _NINE_POINT
+    name = _NINE_POINT[which][0] if nine else KERNELS[which]
+    out = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
            "frac": ach / peak, "peak_source": src, "bytes_per_launch": b, "ms_per_launch": ms, "traffic": None}
     tpath = traffic_path or os.path.join(os.path.dirname(HERE), "profiles", "traffic.json")
     if os.path.exists(tpath):
         try:
-            t = json.load(open(tpath)).get(KERNELS[which].split(" ")[0])
+            t = json.load(open(tpath)).get(name.split(" ")[0])
             if t:
                 out["traffic"] = float(t["dram_bytes_per_launch"])
                 out["traffic_source"] = t["source"]
         except Exception:  # noqa: BLE001
             pass
-    if which in _FP64_OPS_PER_CELL:
+    per_cell = (_NINE_POINT[which][1] if nine else _FP64_OPS_PER_CELL.get(which))
+    if per_cell:
         n = float(P.N1) * float(P.N2)
-        ops = _FP64_OPS_PER_CELL[which] * n
+        ops = per_cell * n
         fma = measure_fp64()
         out["fp64"] = {"achieved_ops_per_s": ops / (ms * 1e-3), "peak_ops_per_s": fma,
                        "frac": ops / (ms * 1e-3) / fma, "ops_per_launch": ops,

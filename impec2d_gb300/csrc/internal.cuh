@@ -121,7 +121,7 @@ namespace impec {
 struct LearnedHook;  // learned_net.cu
 
 struct Tuning {
-    long pre = 2, post = 2;        // smoother sweeps before / after the coarse correction
+    long pre = 2, post = 2;        // smoother sweeps before / after the coarse correction (1, 1 for nine-point operators)
     long cluster = 1;              // coarse levels in one thread-block-cluster launch
     long cl_cells = 16384;         // largest level of the cluster V-cycle
     long cl_cta0 = 256;            // cluster levels up to this many cells run on CTA 0

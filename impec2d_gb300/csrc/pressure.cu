@@ -710,6 +710,12 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         IMPEC_CUDA_TRY(cudaMemset(ctx->cg_q, 0, nf * 8));
         ctx->krylov = (int)env_long("IMPEC_MG_KRYLOV", 1) != 0;
         Tuning& T = ctx->tune;
+        if (ctx->L[0].kind != FACE5) {
+            // weighted nine-point operators (nu < 1): V(1,1) preconditions CG best (1024^2 step:
+            // 6.97 ms against 8.55 ms with V(2,2); 16 instead of 14 iterations)
+            T.pre = 1;
+            T.post = 1;
+        }
         T.pre = env_long("IMPEC_MG_PRE", T.pre);
         T.post = env_long("IMPEC_MG_POST", T.post);
         T.cluster = env_long("IMPEC_MG_CLUSTER", T.cluster);
