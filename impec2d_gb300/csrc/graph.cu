@@ -32,12 +32,13 @@ __global__ void k_clip_dt(DevScalars* S) {
 }
 
 // Advances the clock and counts the kernels this replay executed: the fixed nodes plus the
-// loop bodies times their trip counts.
-__global__ void k_advance(DevScalars* S, long long outer, long long mg_body, long long cn_body) {
+// loop bodies times their trip counts.  Each of the cn_solves CN solves runs its first sweep
+// outside the loop (it is among the fixed nodes) but counts it in cn_cycles_total.
+__global__ void k_advance(DevScalars* S, long long outer, long long mg_body, long long cn_body, int cn_solves) {
     pdl_enter();
     S->t += S->dt;
     S->steps++;
-    S->graph_launches += outer + mg_body * S->mg_cycles + cn_body * S->cn_cycles_total;
+    S->graph_launches += outer + mg_body * S->mg_cycles + cn_body * (S->cn_cycles_total - cn_solves);
 }
 
 // Adds a WHILE node at the current position of the capture on ctx->cap_stream.  init(h)
@@ -87,10 +88,14 @@ static impec_status capture_while(impec_ctx* ctx, Init init, Body body, long lon
 
 static impec_status capture_cn_solve(impec_ctx* ctx, double* c) {
     const double tol = ctx->P.para_eps;
-    IMPEC_TRY(cn_prepare(ctx, c, 0.5, &ctx->dscal->dt));
+    IMPEC_TRY(cn_prepare(ctx, c, 0.5, &ctx->dscal->dt, false));
     long long nb = 0;
     IMPEC_TRY(capture_while(
-        ctx, [&](cudaGraphConditionalHandle h) { return cn_check(ctx, tol, 0, h, 1); },
+        ctx,
+        [&](cudaGraphConditionalHandle h) {  // the first sweep runs before the first check (as dispersion_cn_dev)
+            IMPEC_TRY(cn_iteration(ctx, c));
+            return cn_check(ctx, tol, 1, h, 1);
+        },
         [&](cudaGraphConditionalHandle h) {
             IMPEC_TRY(cn_iteration(ctx, c));
             return cn_check(ctx, tol, 1, h, 1);
@@ -138,7 +143,7 @@ static impec_status capture_step_into(impec_ctx* ctx, int pfs_in) {
         ++ctx->nlaunch;
         const long long loops = mg_body + (P.diffusion ? 2 * ctx->step_cn_body_launches : 0);
         launch_k(ctx->stream, k_advance, 1, 1, 0, S, ctx->nlaunch - n0 - loops, mg_body,
-                                            P.diffusion ? ctx->step_cn_body_launches : 0);
+                 P.diffusion ? ctx->step_cn_body_launches : 0LL, P.diffusion ? 2 : 0);
         IMPEC_LAUNCH_CHECK();
         return IMPEC_OK;
     };
@@ -249,7 +254,7 @@ static impec_status step_stream(impec_ctx* ctx, double t_clip) {
     launch_k(ctx->stream, k_clip_dt, 1, 1, 0, S);
     IMPEC_TRY(hyperbolic_solve_dev(ctx, ctx->c, ctx->u, ctx->v, &S->dt, &ctx->prev_first_sweep));
     ++ctx->nlaunch;
-    launch_k(ctx->stream, k_advance, 1, 1, 0, S, 0, 0, 0);
+    launch_k(ctx->stream, k_advance, 1, 1, 0, S, 0LL, 0LL, 0LL, 0);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }

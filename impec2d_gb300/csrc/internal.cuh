@@ -226,7 +226,7 @@ impec_status advect_split_dev(impec_ctx* ctx, double* c, const double* u, const 
 impec_status average_dev(impec_ctx* ctx, double* c, const double* a, const double* b);
 // dispersion.cu
 impec_status cn_setup(impec_ctx* ctx, const double* u, const double* v, double dt_scale, const double* dt_dev);
-impec_status cn_prepare(impec_ctx* ctx, double* c, double dt_scale, const double* dt_dev);
+impec_status cn_prepare(impec_ctx* ctx, double* c, double dt_scale, const double* dt_dev, bool residual = true);
 impec_status cn_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h);
 impec_status cn_iteration(impec_ctx* ctx, double* c);
 impec_status dispersion_cn_dev(impec_ctx* ctx, double* c, const double* u, const double* v, double dt_scale,

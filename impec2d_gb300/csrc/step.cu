@@ -19,8 +19,9 @@ static impec_status set_dt(impec_ctx* ctx, double dt) {
 }
 
 static impec_status cn_solve_host(impec_ctx* ctx, double* c, double tol) {
-    IMPEC_TRY(cn_prepare(ctx, c, 0.5, &ctx->dscal->dt));
-    IMPEC_TRY(cn_check(ctx, tol, 0, 0, 0));
+    IMPEC_TRY(cn_prepare(ctx, c, 0.5, &ctx->dscal->dt, false));
+    IMPEC_TRY(cn_iteration(ctx, c));  // the first sweep before the first check, as in the step graph
+    IMPEC_TRY(cn_check(ctx, tol, 1, 0, 0));
     for (;;) {
         IMPEC_TRY(sync_scalars(ctx));
         if (!ctx->hscal->go) break;

@@ -553,3 +553,33 @@ def test_quarter_five_spot_integrated_quantities(engine, oracle_lib, cfg):
     assert abs(bt_e[1] - bt_o[1]) <= 1e-9 * bt_o[1]
     assert rel_out <= 1e-9  # measured: 3e-12
     ctx.close()
+
+
+def test_graph_replay_counts_the_launches_of_the_stream_path(engine, monkeypatch):
+    """The step graph's launch accounting (fixed nodes plus loop bodies times their trip
+    counts, the basis of the bench's gpu_launches) equals the kernels the stream path launches
+    one by one for the same steps, and both give the same state."""
+    E = engine
+    N = 64
+    counts, states = [], []
+    for graph in (True, False):
+        if graph:
+            monkeypatch.delenv("IMPEC_NO_GRAPH", raising=False)
+        else:
+            monkeypatch.setenv("IMPEC_NO_GRAPH", "1")
+        P, ctx = _ctx(E, N, N, stype=0, hmtype=4, nu=1.0, diffusion=1, alpha_l=1e-3, alpha_t=1e-4, eps=1e-10,
+                      para_eps=1e-10)
+        OP = oparams(P)
+        ctx.upload(cell_ghost(OP, np.zeros((N, N))), source(OP), ghost=2)
+        ctx.set_time(0.0)
+        ctx.step()  # graph mode: capture and first replay
+        n0 = E.launch_count(ctx)
+        for _ in range(3):
+            ctx.step()
+        counts.append(E.launch_count(ctx) - n0)
+        ch, ph = np.zeros((N + 4, N + 4)), np.zeros((N + 4, N + 4))
+        ctx.download(ch, ph, None, ghost=2)
+        states.append((ch, ph))
+        ctx.close()
+    assert counts[0] == counts[1] and counts[0] > 0, counts
+    assert np.array_equal(states[0][0], states[1][0]) and np.array_equal(states[0][1], states[1][1])
