@@ -504,7 +504,7 @@ def test_horizontal_source_rate_update_in_place(engine):
     assert np.array_equal(ca, cb)
 
 
-@pytest.mark.parametrize("cfg", ["diag_upwind", "par_muscl_disp"])
+@pytest.mark.parametrize("cfg", ["diag_upwind", "par_muscl_disp", "diag_muscl_disp_nu", "diag_upwind_mixed"])
 def test_quarter_five_spot_integrated_quantities(engine, oracle_lib, cfg):
     """A whole displacement at 32 x 32, M = 41, porosity 1, to 1 pore volume injected, engine
     and oracle in lockstep: the reference's CPU case (diagonal grid, first-order upwind) and
@@ -515,9 +515,13 @@ def test_quarter_five_spot_integrated_quantities(engine, oracle_lib, cfg):
     and mass balance."""
     E = engine
     N = 32
-    kw = dict(diag_upwind=dict(stype=1, hmtype=0),
-              par_muscl_disp=dict(stype=0, hmtype=4, diffusion=1, alpha_l=1e-3, alpha_t=1e-4))[cfg]
-    P, ctx = _ctx(E, N, N, nu=1.0, cfl=0.5, mu_res=41.0, mu_inj=1.0, eps=1e-10, para_eps=1e-10, **kw)
+    kw = dict(diag_upwind=dict(stype=1, hmtype=0, nu=1.0),
+              par_muscl_disp=dict(stype=0, hmtype=4, nu=1.0, diffusion=1, alpha_l=1e-3, alpha_t=1e-4),
+              # the reference examples' weighted nine-point operator
+              diag_muscl_disp_nu=dict(stype=1, hmtype=4, nu=2.0 / 3.0, diffusion=1, alpha_l=1.0, alpha_t=0.1),
+              # mixed-precision pressure against the FP64 oracle
+              diag_upwind_mixed=dict(stype=1, hmtype=0, nu=1.0, precision=1))[cfg]
+    P, ctx = _ctx(E, N, N, cfl=0.5, mu_res=41.0, mu_inj=1.0, eps=1e-10, para_eps=1e-10, **kw)
     OP = oparams(P)
     q = source(OP)
     ctx.upload(cell_ghost(OP, np.zeros((N, N))), q, ghost=2)
@@ -546,12 +550,13 @@ def test_quarter_five_spot_integrated_quantities(engine, oracle_lib, cfg):
     print(f"{n} steps to t = {S.t:.4f}: worst dt deviation {worst_dt:.2e}; breakthrough engine {bt_e}, "
           f"oracle {bt_o}; produced {info.total_outflux:.6f} vs {S.total_outflux:.6f} (rel {rel_out:.2e}); "
           f"max mass error engine {mass_e:.1e}, oracle {mass_o:.1e}")
-    # mass balance: the CN solves stop at a 1e-10 relative residual, which is not exactly conservative
-    assert mass_e <= 1e-9 and mass_o <= 1e-9
+    # mass balance: the engine's CN solves stop at the 1e-10 relative residual asked for, which is
+    # not exactly conservative (measured up to 1.8e-9 with strong nine-point dispersion)
+    assert mass_e <= 1e-8 and mass_o <= 1e-8
     assert worst_dt <= 1e-8
     assert bt_e is not None and bt_o is not None and abs(bt_e[0] - bt_o[0]) <= 1
     assert abs(bt_e[1] - bt_o[1]) <= 1e-9 * bt_o[1]
-    assert rel_out <= 1e-9  # measured: 3e-12
+    assert rel_out <= 1e-8  # measured: 3e-12 (upwind, FP64 or mixed) to 3.6e-9 (nine-point dispersion)
     ctx.close()
 
 
