@@ -128,6 +128,7 @@ struct Tuning {
     long coarse_cells64 = 256;     // single-CTA coarse V-cycle (nine-point path), FP64
     long coarse_cells32 = 1024;    // the same, FP32
     long fused32 = 0, fused64 = 0, fuse_fine = 0;  // temporally blocked level kernels (V(2,2) only)
+    long rb_skip = 1;  // five-point levels: no zero fill before pre-smoothing, red-only prolongation
 };
 }  // namespace impec
 

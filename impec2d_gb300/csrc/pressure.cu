@@ -385,6 +385,21 @@ __global__ void k_rb_face5(int n1, int n2, const T* __restrict__ tx, const T* __
     }
 }
 
+// The first colour of a sweep that starts from x = 0: every neighbour term of k_rb_face5 is
+// zero, so s = b and x = b * idiag.  The second colour reads only this colour's cells, so the
+// iterate needs no zero fill beforehand.
+template <class T>
+__global__ void k_rb_zero(int n1, int n2, const T* __restrict__ idiag, const T* __restrict__ b,
+                          T* __restrict__ x, int color) {
+    pdl_enter();
+    const int jj = blockIdx.x * BX + threadIdx.x, i0 = blockIdx.y * (RB_ROWS * BY) + threadIdx.y;
+#pragma unroll
+    for (int r = 0; r < RB_ROWS; ++r) {
+        const int i = i0 + r * BY, j = 2 * jj + ((i + color) & 1);
+        if (i < n1 && j < n2) x[IX(i, j, n2)] = b[IX(i, j, n2)] * idiag[IX(i, j, n2)];
+    }
+}
+
 template <class T>
 __global__ void k_gs4_exp9(int n1, int n2, const T* __restrict__ a9, const T* __restrict__ idiag,
                            const T* __restrict__ b, T* __restrict__ x, int ci, int cj) {
@@ -437,18 +452,14 @@ __global__ void k_restrict(Level F, const T* __restrict__ tx, const T* __restric
             if (i < F.n1 && j < F.n2) s += resid<T>(F, i, j, tx, ty, a9, dg, b, x);
         }
     bc[IX(I, J, n2c)] = s;
-    xc[IX(I, J, n2c)] = 0;
+    if (xc) xc[IX(I, J, n2c)] = 0;  // nullptr: the coarse cycle starts from x = 0 by itself
 }
 
 // Bilinear cell-centred prolongation (weights 9/16, 3/16, 3/16, 1/16; the outside
 // neighbour is replaced by the cell itself), added to the fine iterate.
 template <class T>
-__global__ void k_prolong(int n1, int n2, T* __restrict__ x, int n1c, int n2c, const T* __restrict__ xc,
-                          const unsigned char* __restrict__ mask) {
-    pdl_enter();
-    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
-    if (i >= n1 || j >= n2) return;
-    if (mask && mask[IX(i, j, n2)]) return;  // known cells take no correction
+__device__ __forceinline__ T prolong_cell(int i, int j, int n2, const T* __restrict__ x, int n1c, int n2c,
+                                          const T* __restrict__ xc) {
     int I = i >> 1, J = j >> 1;
     int I2 = (i & 1) ? I + 1 : I - 1, J2 = (j & 1) ? J + 1 : J - 1;
     if (I2 < 0 || I2 >= n1c) I2 = I;
@@ -458,7 +469,34 @@ __global__ void k_prolong(int n1, int n2, T* __restrict__ x, int n1c, int n2c, c
     v += T(0.1875) * xc[IX(I2, J, n2c)];
     v += T(0.1875) * xc[IX(I, J2, n2c)];
     v += T(0.0625) * xc[IX(I2, J2, n2c)];
-    x[IX(i, j, n2)] = v;
+    return v;
+}
+
+template <class T>
+__global__ void k_prolong(int n1, int n2, T* __restrict__ x, int n1c, int n2c, const T* __restrict__ xc,
+                          const unsigned char* __restrict__ mask) {
+    pdl_enter();
+    int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    if (i >= n1 || j >= n2) return;
+    if (mask && mask[IX(i, j, n2)]) return;  // known cells take no correction
+    x[IX(i, j, n2)] = prolong_cell(i, j, n2, x, n1c, n2c, xc);
+}
+
+// The same correction on the cells of one colour only (threads mapped as k_rb_face5).  When a
+// red-black sweep that starts with the other colour follows, that sweep overwrites the other
+// colour's cells without reading them, so their correction would be dead work.
+template <class T>
+__global__ void k_prolong_rb(int n1, int n2, T* __restrict__ x, int n1c, int n2c, const T* __restrict__ xc,
+                             const unsigned char* __restrict__ mask, int color) {
+    pdl_enter();
+    const int jj = blockIdx.x * BX + threadIdx.x, i0 = blockIdx.y * (RB_ROWS * BY) + threadIdx.y;
+#pragma unroll
+    for (int r = 0; r < RB_ROWS; ++r) {
+        const int i = i0 + r * BY, j = 2 * jj + ((i + color) & 1);
+        if (i >= n1 || j >= n2) continue;
+        if (mask && mask[IX(i, j, n2)]) continue;
+        x[IX(i, j, n2)] = prolong_cell(i, j, n2, x, n1c, n2c, xc);
+    }
 }
 
 // ---------------------------------------------------------------- coarsest level (dense)
@@ -726,6 +764,7 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         T.fused32 = env_long("IMPEC_MG_FUSED32", T.fused32);
         T.fused64 = env_long("IMPEC_MG_FUSED64", T.fused64);
         T.fuse_fine = env_long("IMPEC_MG_FUSE_FINE", T.fuse_fine);
+        T.rb_skip = env_long("IMPEC_MG_RB_SKIP", T.rb_skip);
         ctx->cn_predict = env_long("IMPEC_CN_PREDICT", 1) != 0;
         if (ctx->dir_row >= 0) {
             IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dmask, nf));
@@ -886,16 +925,30 @@ const double* level_diag<double>(const Level& Lv) { return Lv.diag; }
 template <>
 const float* level_diag<float>(const Level& Lv) { return Lv.diag32; }
 
+// Grid of the red-black kernels (k_rb_face5, k_rb_zero, k_prolong_rb): RB_ROWS rows and two
+// columns per thread.
+static dim3 rb_grid(const Level& Lv) {
+    return dim3((Lv.n2 / 2 + 1 + BX - 1) / BX, (Lv.n1 + RB_ROWS * BY - 1) / (RB_ROWS * BY));
+}
+
+// zero: x holds no values yet and stands for x = 0 (five-point levels only, where the first
+// colour's update then needs no neighbour).
 template <class T>
-static void smooth(impec_ctx* ctx, Level& Lv, int sweeps, bool reverse) {
+static void smooth(impec_ctx* ctx, Level& Lv, int sweeps, bool reverse, bool zero = false) {
     const T *tx, *ty, *a9, *id;
     T *x, *b;
     level_ptrs<T>(Lv, tx, ty, a9, id, x, b);
     for (int s = 0; s < sweeps; ++s) {
         if (Lv.kind == FACE5) {
-            dim3 g((Lv.n2 / 2 + 1 + BX - 1) / BX, (Lv.n1 + RB_ROWS * BY - 1) / (RB_ROWS * BY));
-            for (int cc = 0; cc < 2; ++cc)
-                ++ctx->nlaunch, launch_k(ctx->stream, k_rb_face5<T>, g, dim3(BX, BY), 0, Lv.n1, Lv.n2, tx, ty, id, b, x, reverse ? 1 - cc : cc);
+            const dim3 g = rb_grid(Lv);
+            for (int cc = 0; cc < 2; ++cc) {
+                const int col = reverse ? 1 - cc : cc;
+                ++ctx->nlaunch;
+                if (zero && s == 0 && cc == 0)
+                    launch_k(ctx->stream, k_rb_zero<T>, g, dim3(BX, BY), 0, Lv.n1, Lv.n2, id, b, x, col);
+                else
+                    launch_k(ctx->stream, k_rb_face5<T>, g, dim3(BX, BY), 0, Lv.n1, Lv.n2, tx, ty, id, b, x, col);
+            }
         } else {
             dim3 g(((Lv.n2 + 1) / 2 + BX - 1) / BX, ((Lv.n1 + 1) / 2 + BY - 1) / BY);
             for (int cc = 0; cc < 4; ++cc) {
@@ -1059,8 +1112,19 @@ static bool use_fused_level(const impec_ctx* ctx, size_t l) {
     return level_ok && (sizeof(T) == 4 ? t.fused32 : t.fused64) != 0;
 }
 
+// Whether the V-cycle at level l runs per-level red-black kernels, so that a cycle started
+// from x = 0 needs no zero fill of the level's iterate (the first colour is k_rb_zero).
 template <class T>
-static void vcycle(impec_ctx* ctx, size_t l) {
+static bool zero_start_free(impec_ctx* ctx, size_t l) {
+    const Level& F = ctx->L[l];
+    return ctx->tune.rb_skip != 0 && F.kind == FACE5 && ctx->tune.pre >= 1 && l != cluster_start<T>(ctx) &&
+           l != coarse_start<T>(ctx) && !use_fused_level<T>(ctx, l);
+}
+
+// One V-cycle from level l down.  zero: the level's iterate stands for x = 0; unless
+// zero_start_free<T>(ctx, l), the caller has filled it with zeros.
+template <class T>
+static void vcycle(impec_ctx* ctx, size_t l, bool zero) {
     Level& F = ctx->L[l];
     const T *tx, *ty, *a9, *id;
     T *x, *b;
@@ -1083,19 +1147,22 @@ static void vcycle(impec_ctx* ctx, size_t l) {
         dim3 g((F.n2 + TB - 1) / TB, (F.n1 + TB - 1) / TB);
         ++ctx->nlaunch;
         launch_k(ctx->stream, k_level_pre<T>, g, TBT, tb_smem<T, TBH_PRE>(), F.n1, F.n2, tx, ty, id, b, x, C.n2, cb, cx, C.n1);
-        vcycle<T>(ctx, l + 1);
+        vcycle<T>(ctx, l + 1, true);
         ++ctx->nlaunch;
         launch_k(ctx->stream, k_level_post<T>, g, TBT, tb_smem<T, TBH_POST>(), F.n1, F.n2, tx, ty, id, b, x, C.n1, C.n2, cx);
         return;
     }
-    smooth<T>(ctx, F, (int)ctx->tune.pre, false);
+    smooth<T>(ctx, F, (int)ctx->tune.pre, false, zero && zero_start_free<T>(ctx, l));
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_restrict<T>, grid2(C.n1, C.n2), dim3(BX, BY), 0, F, tx, ty, a9, level_diag<T>(F), b, x,
-             C.n1, C.n2, cb, cx);
-    vcycle<T>(ctx, l + 1);
+             C.n1, C.n2, cb, zero_start_free<T>(ctx, l + 1) ? nullptr : cx);
+    vcycle<T>(ctx, l + 1, true);
+    const unsigned char* mask = l == 0 && ctx->dir_row >= 0 ? ctx->dmask : nullptr;
     ++ctx->nlaunch;
-    launch_k(ctx->stream, k_prolong<T>, grid2(F.n1, F.n2), dim3(BX, BY), 0, F.n1, F.n2, x, C.n1, C.n2, cx,
-             l == 0 && ctx->dir_row >= 0 ? ctx->dmask : nullptr);
+    if (ctx->tune.rb_skip != 0 && F.kind == FACE5 && ctx->tune.post >= 1)  // the black cells are overwritten next
+        launch_k(ctx->stream, k_prolong_rb<T>, rb_grid(F), dim3(BX, BY), 0, F.n1, F.n2, x, C.n1, C.n2, cx, mask, 0);
+    else
+        launch_k(ctx->stream, k_prolong<T>, grid2(F.n1, F.n2), dim3(BX, BY), 0, F.n1, F.n2, x, C.n1, C.n2, cx, mask);
     smooth<T>(ctx, F, (int)ctx->tune.post, true);
 }
 
@@ -1360,14 +1427,14 @@ impec_status pressure_iteration(impec_ctx* ctx, double tol, cudaGraphConditional
     const bool mixed = ctx->P.precision == IMPEC_PREC_MIXED;
     if (!ctx->krylov) {
         if (mixed) {
-            IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
-            vcycle<float>(ctx, 0);
+            if (!zero_start_free<float>(ctx, 0)) IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
+            vcycle<float>(ctx, 0, true);
             ++ctx->nlaunch;
             launch_k(ctx->stream, k_add_f32, ctx->num_sms * 4, 256, 0, n, F.x, F.x32);
             IMPEC_LAUNCH_CHECK();
             return pressure_residual(ctx);
         }
-        vcycle<double>(ctx, 0);
+        vcycle<double>(ctx, 0, false);  // corrects the iterate itself
         IMPEC_LAUNCH_CHECK();
         return pressure_residual(ctx);
     }
@@ -1376,11 +1443,11 @@ impec_status pressure_iteration(impec_ctx* ctx, double tol, cudaGraphConditional
     const double* z = mixed ? nullptr : F.x;
     const float* z32 = mixed ? F.x32 : nullptr;
     if (mixed) {
-        IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
-        vcycle<float>(ctx, 0);
+        if (!zero_start_free<float>(ctx, 0)) IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
+        vcycle<float>(ctx, 0, true);
     } else {
-        IMPEC_CUDA_TRY(cudaMemsetAsync(F.x, 0, n * 8, ctx->stream));
-        vcycle<double>(ctx, 0);
+        if (!zero_start_free<double>(ctx, 0)) IMPEC_CUDA_TRY(cudaMemsetAsync(F.x, 0, n * 8, ctx->stream));
+        vcycle<double>(ctx, 0, true);
     }
     const int cap = red_cap(ctx->num_sms, ctx->max_blocks), blocks = seg_blocks(F.n1, F.n2, cap);
     ++ctx->nlaunch;

@@ -131,6 +131,32 @@ def test_cluster_vcycle_matches_per_level_kernels(engine, monkeypatch, N1, N2, p
     assert out[1][3] < out[0][3]  # the cluster kernel replaced per-level launches
 
 
+@pytest.mark.parametrize("N1,N2,stype", [(37, 29, 1), (300, 130, 1), (1024, 1024, 1), (97, 70, 2)])
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("krylov", ["1", "0"])
+def test_red_black_shortcuts_match_full_kernels(engine, monkeypatch, N1, N2, stype, prec, krylov):
+    """Pre-smoothing that starts from an implicit zero (no zero fill; the first colour is
+    x = b / diag) and a red-only prolongation ahead of a sweep that overwrites the black cells
+    change nothing. The cycles, residual and pressure are the same bit for bit as with the full
+    kernels, for the CG and the stationary iteration, and with a Dirichlet row (stype 2)."""
+    E = engine
+    import torch
+    monkeypatch.setenv("IMPEC_MG_KRYLOV", krylov)
+    out = []
+    for skip in ("0", "1"):
+        monkeypatch.setenv("IMPEC_MG_RB_SKIP", skip)
+        P, ctx = _ctx(E, N1, N2, nu=1.0, stype=stype, precision=prec, max_cycles=200)
+        OP = oparams(P)
+        ctx.set_source(dev(source(OP)))
+        p = torch.zeros((N1, N2), dtype=torch.float64, device="cuda")
+        cyc, rr, _ = ctx.pressure_solve(dev(_rand_c(N1, N2, 9)), p, 1e-11)
+        out.append((cyc, rr, host(p)))
+        ctx.close()
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    assert np.array_equal(out[0][2], out[1][2])
+    assert out[1][1] <= 1e-11
+
+
 @pytest.mark.parametrize("N1,N2", GRIDS)
 @pytest.mark.parametrize("nu", [1.0, 2.0 / 3.0])
 def test_velocity(engine, oracle_lib, N1, N2, nu):
