@@ -1203,10 +1203,11 @@ __global__ void k_mg_check(DevScalars* S, double tol, int max_cycles, int inc, c
 
 // ---------------------------------------------------------------- V-cycle preconditioned CG
 // The reference solves the pressure system with CG preconditioned by HYPRE's SMG
-// (src/MGSolver.cpp:594-629); here the preconditioner is one V(2,2) cycle of the engine's own
-// multigrid, z = M^-1 r, in FP64 or (mixed precision) in FP32 on the FP32 copy of r.  CG runs
-// in FP64 on the consistent singular system.  Because the FP32 cycle is not an exactly
-// symmetric operator, the direction uses the flexible (Polak-Ribiere) coefficient
+// (src/MGSolver.cpp:594-629); here the preconditioner is one V-cycle of the engine's own
+// multigrid (V(1,2) for five-point, V(1,1) for nine-point operators by default), z = M^-1 r, in
+// FP64 or (mixed precision) in FP32 on the FP32 copy of r.  CG runs in FP64 on the consistent
+// singular system.  Because neither a cycle with unequal pre- and post-smoothing nor the FP32
+// cycle is a symmetric operator, the direction uses the flexible (Polak-Ribiere) coefficient
 //   beta = (z_k, r_k - r_{k-1}) / (z_{k-1}, r_{k-1}) = -alpha_{k-1} (z_k, A p_{k-1}) / (z_{k-1}, r_{k-1}),
 // which needs only (z, r) and (z, q) with q = A p still holding the previous direction.
 
@@ -1294,14 +1295,52 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_update(int n1, int n2, doubl
     }
 }
 
-// Relative residual of the returned iterate (true residual, recomputed after the loop).
-__global__ void k_true_relres(DevScalars* S, double tol) {
-    pdl_enter();
+// Convergence decision on the true residual (one thread; S->rnorm2 = ||f - A x||^2 of the
+// iterate).  It becomes the reported relres and alone sets or clears FLAG_MG_NOT_CONVERGED.
+__device__ __forceinline__ void true_check(DevScalars* S, double tol, int max_cycles, cudaGraphConditionalHandle h,
+                                           int use_h) {
     const double fn = S->fnorm2, rn = S->rnorm2;
     const double rr = fn > 0 ? sqrt(rn / fn) : sqrt(rn);
     S->relres = rr;
-    if (!(rr == rr) || isinf(rr)) S->flags |= FLAG_MG_NAN;
-    else if (rr > 2.0 * tol && !(S->flags & FLAG_MG_NOT_CONVERGED)) S->flags |= FLAG_MG_NOT_CONVERGED;
+    const bool bad = !(rr == rr) || isinf(rr);
+    const bool go = !bad && rr > tol && S->mg_cycles < max_cycles;
+    if (bad) S->flags |= FLAG_MG_NAN;
+    if (!bad && !go && rr > tol) S->flags |= FLAG_MG_NOT_CONVERGED;
+    else S->flags &= ~FLAG_MG_NOT_CONVERGED;
+    S->go = go ? 1 : 0;
+    if (use_h) cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// End of a CG pass, after k_cg_update, whose check set S->go from the recurrence residual.
+// That residual drifts from the true one by rounding, so a stop (converged, max_cycles or a
+// breakdown) is verified here: the true residual f - A x of the final iterate replaces r (and
+// its FP32 copy), its norm gives the reported relres, and CG continues from it while it is
+// above tol and cycles remain.  On the other passes the kernel only hands S->go to the WHILE
+// condition.  Every thread reads S->go before the last block (the only writer) can change it.
+__global__ void __launch_bounds__(RED_THREADS) k_cg_verify(Level F, const double* __restrict__ f,
+                                                           const double* __restrict__ x, int pin,
+                                                           float* __restrict__ r32, double* __restrict__ r64,
+                                                           DevScalars* S, double* partials, int mb, unsigned* counter,
+                                                           double tol, int max_cycles, cudaGraphConditionalHandle h,
+                                                           int use_h) {
+    pdl_enter();
+    const int go = S->go, nan = S->flags & FLAG_MG_NAN;
+    if (go || nan) {
+        if (use_h && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(h, go ? 1u : 0u);
+        return;
+    }
+    double acc[1] = {0.0};
+    for_cells(F.n1, F.n2, [&](int i, int j, size_t k) {
+        double r = resid<double>(F, i, j, F.tx, F.ty, F.a9, F.diag, f, x);
+        r64[k] = r;
+        if (r32) r32[k] = (float)r;
+        if ((int)k == pin) r = 0.0;  // as k_fine_resid
+        acc[0] += r * r;
+    });
+    if (grid_reduce<1>(acc, 0u, partials, mb, counter, &S->rnorm2) && threadIdx.x == 0) {
+        __threadfence();
+        true_check(S, tol, max_cycles, h, use_h);
+    }
 }
 
 // The pinned cell of the singular system (-1 with a Dirichlet row: nothing is pinned).
@@ -1461,22 +1500,21 @@ impec_status pressure_iteration(impec_ctx* ctx, double tol, cudaGraphConditional
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_cg_update, blocks, RED_THREADS, 0, F.n1, F.n2, ctx->cg_x, r, mixed ? F.b32 : nullptr,
              (const double*)ctx->cg_p, (const double*)ctx->cg_q, pin_index(ctx), S, ctx->partials, ctx->max_blocks,
-             ctx->counter, &S->rnorm2, tol, ctx->P.max_cycles, h, use_h);
+             ctx->counter, &S->rnorm2, tol, ctx->P.max_cycles, h, 0);
+    ++ctx->nlaunch;
+    launch_k(ctx->stream, k_cg_verify, blocks, RED_THREADS, 0, F, (const double*)ctx->f, (const double*)ctx->cg_x,
+             pin_index(ctx), mixed ? F.b32 : nullptr, r, S, ctx->partials, ctx->max_blocks, ctx->counter, tol,
+             ctx->P.max_cycles, h, use_h);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
 
-// Constant shift to the pinned value and copy to p (launch only).  After CG the residual of
-// the returned iterate is recomputed, so the reported relres is the true one.
+// Constant shift to the pinned value and copy to p (launch only).  With CG the reported relres
+// is the true one, from the k_cg_verify that ended the loop.
 impec_status pressure_finish(impec_ctx* ctx, double* p) {
     Level& F = ctx->L[0];
     const size_t n = F.n();
     double* x = solve_iterate(ctx);
-    if (ctx->krylov) {
-        IMPEC_TRY(fine_residual(ctx, x, nullptr, nullptr));
-        ++ctx->nlaunch;
-        launch_k(ctx->stream, k_true_relres, 1, 1, 0, ctx->dscal, ctx->solve_tol);
-    }
     if (ctx->singular) {  // the constant that puts the pinned cell at its value
         ++ctx->nlaunch;
         launch_k(ctx->stream, k_shift, ctx->num_sms * 4, 256, 0, n, x, pin_index(ctx), ctx->dscal);

@@ -63,7 +63,7 @@ def test_tuning_and_autotune(engine):
     N = 200
     ctx = _member(E, N, N, dict(stype=1, nu=1.0, eps=1e-10))
     c = torch.from_numpy(smooth_field(N, N, 3)).cuda()
-    assert ctx.get_tuning("mg_pre") == 2 and ctx.get_tuning("mg_post") == 2
+    assert ctx.get_tuning("mg_pre") == 1 and ctx.get_tuning("mg_post") == 2  # five-point default V(1,2)
     ctx.set_tuning("mg_pre", 1)
     assert ctx.get_tuning("mg_pre") == 1
     with pytest.raises(E.ImpecError):

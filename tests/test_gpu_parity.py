@@ -447,6 +447,46 @@ def test_horizontal_pressure_solve(engine, oracle_lib, N1, N2, nu, prec):
     assert rel_err(host(p), p_or) <= 1e-8
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_true_residual_loop_host_and_graph(engine, oracle_lib, prec):
+    """CG's recurrence residual drifts from the true one by rounding, so each stop is verified
+    on the true residual and CG continues from it until ||b - A p|| / ||b|| itself meets tol.
+    This Dirichlet-row system at 1e-12 needs that: the recurrence stop alone left a true
+    residual of 1.1e-12.  The host-driven solve and the resident graph (WHILE node) give the
+    same cycles, residual and pressure bits, and the oracle's matrix confirms the residual."""
+    E = engine
+    import torch
+    N1, N2, tol = 97, 70, 1e-12
+    out = []
+    for resident in (False, True):
+        P, ctx = _ctx(E, N1, N2, nu=1.0, stype=2, precision=prec, max_cycles=200, eps=tol)
+        OP = oparams(P)
+        c = _rand_c(N1, N2, 4)
+        q = source(OP)
+        if resident:
+            ctx.upload(cell_ghost(OP, c), q, ghost=2)
+            cyc, rr = ctx.pressure_solve_resident()
+            pg = np.zeros((N1 + 4, N2 + 4))
+            ctx.download(None, pg, None, ghost=2)
+            p = pg[2:-2, 2:-2].copy()
+        else:
+            ctx.set_source(dev(q))
+            pd = torch.zeros((N1, N2), dtype=torch.float64, device="cuda")
+            cyc, rr, _ = ctx.pressure_solve(dev(c), pd, tol)
+            p = host(pd)
+        out.append((cyc, rr, p))
+        ctx.close()
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1], (out[0][:2], out[1][:2])
+    assert np.array_equal(out[0][2], out[1][2])
+    assert out[0][1] <= tol
+    A = np.zeros(N1 * N2 * 9)
+    b = np.zeros(N1 * N2)
+    oracle_lib.or_pressure_matrix(C.byref(OP), O.ptr(cell_ghost(OP, c)), O.ptr(A))
+    oracle_lib.or_pressure_rhs(C.byref(OP), O.ptr(q), O.ptr(b))
+    ph = out[0][2].ravel().copy()
+    assert oracle_lib.or_relres9(C.byref(OP), O.ptr(A), O.ptr(ph), O.ptr(b)) <= 2 * tol
+
+
 def test_horizontal_dispersion_cn(engine, oracle_lib):
     """CN with the Dirichlet row c = 0 at i = N1-2."""
     E = engine
@@ -586,29 +626,30 @@ def test_quarter_five_spot_integrated_quantities(engine, oracle_lib, cfg):
     ctx.close()
 
 
-def test_graph_replay_counts_the_launches_of_the_stream_path(engine, monkeypatch):
+@pytest.mark.parametrize("N1,N2,stype,eps", [(64, 64, 0, 1e-10), (97, 70, 2, 1e-12)])
+def test_graph_replay_counts_the_launches_of_the_stream_path(engine, monkeypatch, N1, N2, stype, eps):
     """The step graph's launch accounting (fixed nodes plus loop bodies times their trip
     counts, the basis of the bench's gpu_launches) equals the kernels the stream path launches
-    one by one for the same steps, and both give the same state."""
+    one by one for the same steps, and both give the same state.  The second case is a
+    Dirichlet-row system at a tolerance where the true-residual verification can continue CG."""
     E = engine
-    N = 64
     counts, states = [], []
     for graph in (True, False):
         if graph:
             monkeypatch.delenv("IMPEC_NO_GRAPH", raising=False)
         else:
             monkeypatch.setenv("IMPEC_NO_GRAPH", "1")
-        P, ctx = _ctx(E, N, N, stype=0, hmtype=4, nu=1.0, diffusion=1, alpha_l=1e-3, alpha_t=1e-4, eps=1e-10,
+        P, ctx = _ctx(E, N1, N2, stype=stype, hmtype=4, nu=1.0, diffusion=1, alpha_l=1e-3, alpha_t=1e-4, eps=eps,
                       para_eps=1e-10)
         OP = oparams(P)
-        ctx.upload(cell_ghost(OP, np.zeros((N, N))), source(OP), ghost=2)
+        ctx.upload(cell_ghost(OP, np.zeros((N1, N2))), source(OP), ghost=2)
         ctx.set_time(0.0)
         ctx.step()  # graph mode: capture and first replay
         n0 = E.launch_count(ctx)
         for _ in range(3):
             ctx.step()
         counts.append(E.launch_count(ctx) - n0)
-        ch, ph = np.zeros((N + 4, N + 4)), np.zeros((N + 4, N + 4))
+        ch, ph = np.zeros((N1 + 4, N2 + 4)), np.zeros((N1 + 4, N2 + 4))
         ctx.download(ch, ph, None, ghost=2)
         states.append((ch, ph))
         ctx.close()
