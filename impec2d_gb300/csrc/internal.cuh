@@ -132,6 +132,7 @@ struct Tuning {
     long coarse_cells32 = 1024;    // the same, FP32
     long fused32 = 0, fused64 = 0, fuse_fine = 0;  // temporally blocked level kernels (V(2,2) only)
     long rb_skip = 1;  // five-point levels: no zero fill before pre-smoothing, red-only prolongation
+    long rb_resid = 1;  // five-point levels: restriction sums the red residuals only (black ones are ~0)
 };
 }  // namespace impec
 

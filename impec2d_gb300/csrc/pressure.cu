@@ -441,7 +441,7 @@ __device__ __forceinline__ T resid(const Level& Lv, int i, int j, const T* __res
 template <class T>
 __global__ void k_restrict(Level F, const T* __restrict__ tx, const T* __restrict__ ty, const T* __restrict__ a9,
                            const T* __restrict__ dg, const T* __restrict__ b, const T* __restrict__ x, int n1c,
-                           int n2c, T* __restrict__ bc, T* __restrict__ xc) {
+                           int n2c, T* __restrict__ bc, T* __restrict__ xc, int zero_color) {
     pdl_enter();
     int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
     if (I >= n1c || J >= n2c) return;
@@ -449,6 +449,9 @@ __global__ void k_restrict(Level F, const T* __restrict__ tx, const T* __restric
     for (int a = 0; a < 2; ++a)
         for (int bb = 0; bb < 2; ++bb) {
             int i = 2 * I + a, j = 2 * J + bb;
+            // zero_color >= 0: the red-black sweep just updated that colour, whose residual
+            // s - diag (s / diag) is zero up to one rounding (resid() recomputes the same s)
+            if (((i + j) & 1) == zero_color) continue;
             if (i < F.n1 && j < F.n2) s += resid<T>(F, i, j, tx, ty, a9, dg, b, x);
         }
     bc[IX(I, J, n2c)] = s;
@@ -765,6 +768,7 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         T.fused64 = env_long("IMPEC_MG_FUSED64", T.fused64);
         T.fuse_fine = env_long("IMPEC_MG_FUSE_FINE", T.fuse_fine);
         T.rb_skip = env_long("IMPEC_MG_RB_SKIP", T.rb_skip);
+        T.rb_resid = env_long("IMPEC_MG_RB_RESID", T.rb_resid);
         ctx->cn_predict = env_long("IMPEC_CN_PREDICT", 1) != 0;
         if (ctx->dir_row >= 0) {
             IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dmask, nf));
@@ -1154,8 +1158,10 @@ static void vcycle(impec_ctx* ctx, size_t l, bool zero) {
     }
     smooth<T>(ctx, F, (int)ctx->tune.pre, false, zero && zero_start_free<T>(ctx, l));
     ++ctx->nlaunch;
+    // after a five-point pre-smoothing the colour updated last (black) has a zero residual
+    const int zero_color = ctx->tune.rb_resid != 0 && F.kind == FACE5 && ctx->tune.pre >= 1 ? 1 : -1;
     launch_k(ctx->stream, k_restrict<T>, grid2(C.n1, C.n2), dim3(BX, BY), 0, F, tx, ty, a9, level_diag<T>(F), b, x,
-             C.n1, C.n2, cb, zero_start_free<T>(ctx, l + 1) ? nullptr : cx);
+             C.n1, C.n2, cb, zero_start_free<T>(ctx, l + 1) ? nullptr : cx, zero_color);
     vcycle<T>(ctx, l + 1, true);
     const unsigned char* mask = l == 0 && ctx->dir_row >= 0 ? ctx->dmask : nullptr;
     ++ctx->nlaunch;

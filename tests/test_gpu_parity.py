@@ -157,6 +157,32 @@ def test_red_black_shortcuts_match_full_kernels(engine, monkeypatch, N1, N2, sty
     assert out[1][1] <= 1e-11
 
 
+@pytest.mark.parametrize("N1,N2,stype", [(37, 29, 1), (300, 130, 1), (1024, 1024, 1), (97, 70, 2)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_red_only_restriction(engine, monkeypatch, N1, N2, stype, prec):
+    """Restriction that sums only the red residuals: after the pre-smoothing's black pass the
+    black residuals are zero up to one rounding, so dropping them moves the coarse right-hand
+    side by about machine epsilon.  The solve needs the same CG iterations, meets the
+    tolerance, and lands within it of the full restriction's solution."""
+    E = engine
+    import torch
+    tol = 1e-11
+    out = []
+    for red_only in ("0", "1"):
+        monkeypatch.setenv("IMPEC_MG_RB_RESID", red_only)
+        P, ctx = _ctx(E, N1, N2, nu=1.0, stype=stype, precision=prec, max_cycles=200)
+        OP = oparams(P)
+        ctx.set_source(dev(source(OP)))
+        p = torch.zeros((N1, N2), dtype=torch.float64, device="cuda")
+        cyc, rr, _ = ctx.pressure_solve(dev(_rand_c(N1, N2, 9)), p, tol)
+        out.append((cyc, rr, host(p)))
+        ctx.close()
+    assert out[0][0] == out[1][0], (out[0][:2], out[1][:2])
+    assert out[0][1] <= tol and out[1][1] <= tol
+    # both solve to 1e-11 in relative residual; kappa ~ 1e5 at these sizes
+    assert rel_err(out[1][2], out[0][2]) <= 1e-6
+
+
 @pytest.mark.parametrize("N1,N2", GRIDS)
 @pytest.mark.parametrize("nu", [1.0, 2.0 / 3.0])
 def test_velocity(engine, oracle_lib, N1, N2, nu):
