@@ -130,7 +130,6 @@ struct Tuning {
     long cl_cta0 = 256;            // cluster levels up to this many cells run on CTA 0
     long coarse_cells64 = 256;     // single-CTA coarse V-cycle (nine-point path), FP64
     long coarse_cells32 = 1024;    // the same, FP32
-    long fused32 = 0, fused64 = 0, fuse_fine = 0;  // temporally blocked level kernels (V(2,2) only)
     long rb_skip = 1;  // five-point levels: no zero fill before pre-smoothing, red-only prolongation
     long rb_resid = 1;  // five-point levels: restriction sums the red residuals only (black ones are ~0)
 };

@@ -31,6 +31,7 @@ struct ClusterArgs {
     int nd;  // levels 0 .. nd-1 are spread over the cluster; nd .. nl-1 live on CTA 0
     int singular, dn;
     int pre, post;  // smoother sweeps before / after the coarse correction
+    int zero_color;  // restriction skips cells of this colour (their residual is ~0), or -1
     int n1[CL_MAXL], n2[CL_MAXL], rows[CL_MAXL];
     unsigned off[CL_MAXL][6];  // shared-memory offsets (elements of T) of tx, ty, id, dg, x, b
     const T* tx[CL_MAXL];
@@ -111,7 +112,7 @@ __device__ void cl_restrict(const cooperative_groups::cluster_group& cl, T* sm, 
         for (int a = 0; a < 2; ++a)
             for (int bb = 0; bb < 2; ++bb) {
                 const int i = 2 * I + a, j = 2 * J + bb;
-                if (i >= n1 || j >= n2) continue;
+                if (i >= n1 || j >= n2 || ((i + j) & 1) == A.zero_color) continue;  // as k_restrict
                 const int li = i - lo, c = li * n2 + j;
                 T r = b[c];
                 if (i > 0) r += tx[c] * (li > 0 ? x[c - n2] : xup[j]);

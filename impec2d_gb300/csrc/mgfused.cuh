@@ -1,13 +1,8 @@
-// Fused multigrid kernels (included by pressure.cu).
+// Single-CTA coarse V-cycle (included by pressure.cu).
 //
-// 1. k_coarse_vcycle: the whole V-cycle of the coarse levels (<= 32^2 cells in FP64, <= 64^2 in
-//    FP32) in one CTA, operators and iterates in shared memory, coarsest level by the dense
-//    FP64 inverse.  Replaces ~10 launches per coarse level.
-// 2. k_level_pre / k_level_post: on an intermediate five-point level, two red-black
-//    Gauss-Seidel sweeps fused with the residual and the 2x2 restriction (pre), and the
-//    bilinear prolongation fused with two sweeps (post).  Each CTA updates its tile plus a
-//    shrinking halo (temporal blocking): red/black colours follow the global indices and
-//    faces outside the grid are zero, so the result equals the unfused kernels bit for bit.
+// k_coarse_vcycle: the whole V-cycle of the coarse levels (<= 32^2 cells in FP64, <= 64^2 in
+// FP32) in one CTA, operators and iterates in shared memory, coarsest level by the dense FP64
+// inverse.  Replaces ~10 launches per coarse level.
 #pragma once
 // Included inside namespace impec of pressure.cu (uses its IX, c_off and Level definitions).
 
@@ -17,6 +12,7 @@ template <class T>
 struct CoarseArgs {
     int nl, singular, dn;
     int pre, post;  // smoother sweeps before / after the coarse correction
+    int zero_color;  // restriction skips cells of this colour (their residual is ~0), or -1
     int n1[MGC_MAXL], n2[MGC_MAXL];
     const T* tx[MGC_MAXL];
     const T* ty[MGC_MAXL];
@@ -132,6 +128,7 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
             for (int a = 0; a < 2; ++a)
                 for (int bb = 0; bb < 2; ++bb) {
                     int i = 2 * I + a, j = 2 * J + bb;
+                    if (((i + j) & 1) == A.zero_color) continue;  // as k_restrict
                     if (i < n1 && j < n2) s += cv_resid<T, KIND>(i, j, n1, n2, tx[l], ty[l], a9[l], dg[l], b[l], x[l]);
                 }
             b[l + 1][K] = s;
@@ -190,140 +187,3 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
     const int n0 = A.n1[0] * A.n2[0];
     for (int k = threadIdx.x; k < n0; k += blockDim.x) A.x0[k] = x[0][k];
 }
-
-// ---------------------------------------------------------------- temporally blocked levels
-constexpr int TB = 32;           // output tile edge
-constexpr int TBH_PRE = 5;       // 4 half sweeps + residual
-constexpr int TBH_POST = 4;      // 4 half sweeps
-constexpr int TBT = 256;         // threads
-
-// Loads x, b, idiag over the region [i0-H, i0+TB+H) x [j0-H, j0+TB+H) and the faces around it;
-// cells and faces outside the grid become zero.
-template <class T, int H>
-__device__ __forceinline__ void tb_load(int n1, int n2, int i0, int j0, const T* __restrict__ gtx,
-                                        const T* __restrict__ gty, const T* __restrict__ gid,
-                                        const T* __restrict__ gb, const T* __restrict__ gx, T* x, T* b, T* id, T* tx,
-                                        T* ty) {
-    constexpr int R = TB + 2 * H;
-    for (int k = threadIdx.x; k < R * R; k += TBT) {
-        const int a = k / R, c = k % R, gi = i0 - H + a, gj = j0 - H + c;
-        const bool in = gi >= 0 && gi < n1 && gj >= 0 && gj < n2;
-        x[k] = in ? gx[IX(gi, gj, n2)] : T(0);
-        b[k] = in ? gb[IX(gi, gj, n2)] : T(0);
-        id[k] = in ? gid[IX(gi, gj, n2)] : T(0);
-    }
-    for (int k = threadIdx.x; k < (R + 1) * R; k += TBT) {  // tx: faces fi in [i0-H, i0+TB+H], cols
-        const int a = k / R, c = k % R, fi = i0 - H + a, gj = j0 - H + c;
-        tx[k] = (fi >= 0 && fi <= n1 && gj >= 0 && gj < n2) ? gtx[IX(fi, gj, n2)] : T(0);
-    }
-    for (int k = threadIdx.x; k < R * (R + 1); k += TBT) {  // ty: rows, faces fj in [j0-H, j0+TB+H]
-        const int a = k / (R + 1), c = k % (R + 1), gi = i0 - H + a, fj = j0 - H + c;
-        ty[k] = (gi >= 0 && gi < n1 && fj >= 0 && fj <= n2) ? gty[IX(gi, fj, n2 + 1)] : T(0);
-    }
-}
-
-// Half sweep of colour col on local cells [lo, hi)^2 of a region of edge R.
-template <class T, int R>
-__device__ __forceinline__ void tb_half(int n1, int n2, int i0, int j0, int H, int lo, int hi, int col, const T* b,
-                                        const T* id, const T* tx, const T* ty, T* x) {
-    const int w = hi - lo;
-    for (int k = threadIdx.x; k < w * w; k += TBT) {
-        const int a = lo + k / w, c = lo + k % w, gi = i0 - H + a, gj = j0 - H + c;
-        if (((gi + gj) & 1) != col) continue;
-        if (gi < 0 || gi >= n1 || gj < 0 || gj >= n2) continue;
-        const int q = a * R + c;
-        T s = b[q];
-        if (gi > 0) s += tx[a * R + c] * x[q - R];
-        if (gi < n1 - 1) s += tx[(a + 1) * R + c] * x[q + R];
-        if (gj > 0) s += ty[a * (R + 1) + c] * x[q - 1];
-        if (gj < n2 - 1) s += ty[a * (R + 1) + c + 1] * x[q + 1];
-        x[q] = s * id[q];
-    }
-    __syncthreads();
-}
-
-template <class T>
-__global__ void __launch_bounds__(TBT) k_level_pre(int n1, int n2, const T* __restrict__ gtx, const T* __restrict__ gty,
-                                                   const T* __restrict__ gid, const T* __restrict__ gb,
-                                                   T* __restrict__ gx, int c2, T* __restrict__ bc,
-                                                   T* __restrict__ xc, int nc1) {
-    pdl_enter();
-    constexpr int H = TBH_PRE, R = TB + 2 * H;
-    extern __shared__ __align__(16) unsigned char tb_raw[];
-    T* x = reinterpret_cast<T*>(tb_raw);
-    T* b = x + R * R;
-    T* id = b + R * R;
-    T* tx = id + R * R;
-    T* ty = tx + (R + 1) * R;
-    const int i0 = blockIdx.y * TB, j0 = blockIdx.x * TB;
-    tb_load<T, H>(n1, n2, i0, j0, gtx, gty, gid, gb, gx, x, b, id, tx, ty);
-    __syncthreads();
-    for (int s = 0; s < 4; ++s) tb_half<T, R>(n1, n2, i0, j0, H, s + 1, R - s - 1, s & 1, b, id, tx, ty, x);
-    // residual on the tile (local [H, H+TB)), summed over 2x2 aggregates
-    for (int K = threadIdx.x; K < (TB / 2) * (TB / 2); K += TBT) {
-        const int I = (i0 >> 1) + K / (TB / 2), J = (j0 >> 1) + K % (TB / 2);
-        if (I >= nc1 || J >= c2) continue;
-        T s = 0;
-        for (int a = 0; a < 2; ++a)
-            for (int bb = 0; bb < 2; ++bb) {
-                const int gi = 2 * I + a, gj = 2 * J + bb;
-                if (gi >= n1 || gj >= n2) continue;
-                const int la = gi - i0 + H, lc = gj - j0 + H, q = la * R + lc;
-                T tw = tx[la * R + lc], te = tx[(la + 1) * R + lc], ts = ty[la * (R + 1) + lc], tn = ty[la * (R + 1) + lc + 1];
-                T o = 0;
-                if (gi > 0) o += tw * x[q - R];
-                if (gi < n1 - 1) o += te * x[q + R];
-                if (gj > 0) o += ts * x[q - 1];
-                if (gj < n2 - 1) o += tn * x[q + 1];
-                T diag = tw + te + ts + tn;
-                s += b[q] - (diag * x[q] - o);
-            }
-        bc[IX(I, J, c2)] = s;
-        xc[IX(I, J, c2)] = 0;
-    }
-    for (int k = threadIdx.x; k < TB * TB; k += TBT) {
-        const int gi = i0 + k / TB, gj = j0 + k % TB;
-        if (gi < n1 && gj < n2) gx[IX(gi, gj, n2)] = x[(k / TB + H) * R + (k % TB + H)];
-    }
-}
-
-template <class T>
-__global__ void __launch_bounds__(TBT) k_level_post(int n1, int n2, const T* __restrict__ gtx,
-                                                    const T* __restrict__ gty, const T* __restrict__ gid,
-                                                    const T* __restrict__ gb, T* __restrict__ gx, int c1, int c2,
-                                                    const T* __restrict__ xc) {
-    pdl_enter();
-    constexpr int H = TBH_POST, R = TB + 2 * H;
-    extern __shared__ __align__(16) unsigned char tb_raw[];
-    T* x = reinterpret_cast<T*>(tb_raw);
-    T* b = x + R * R;
-    T* id = b + R * R;
-    T* tx = id + R * R;
-    T* ty = tx + (R + 1) * R;
-    const int i0 = blockIdx.y * TB, j0 = blockIdx.x * TB;
-    tb_load<T, H>(n1, n2, i0, j0, gtx, gty, gid, gb, gx, x, b, id, tx, ty);
-    __syncthreads();
-    for (int k = threadIdx.x; k < R * R; k += TBT) {  // bilinear prolongation on the region
-        const int gi = i0 - H + k / R, gj = j0 - H + k % R;
-        if (gi < 0 || gi >= n1 || gj < 0 || gj >= n2) continue;
-        int I = gi >> 1, J = gj >> 1;
-        int I2 = (gi & 1) ? I + 1 : I - 1, J2 = (gj & 1) ? J + 1 : J - 1;
-        if (I2 < 0 || I2 >= c1) I2 = I;
-        if (J2 < 0 || J2 >= c2) J2 = J;
-        T e = T(0.5625) * xc[IX(I, J, c2)] + T(0.1875) * xc[IX(I2, J, c2)] + T(0.1875) * xc[IX(I, J2, c2)] +
-              T(0.0625) * xc[IX(I2, J2, c2)];
-        x[k] += e;
-    }
-    __syncthreads();
-    for (int s = 0; s < 4; ++s) tb_half<T, R>(n1, n2, i0, j0, H, s + 1, R - s - 1, 1 - (s & 1), b, id, tx, ty, x);
-    for (int k = threadIdx.x; k < TB * TB; k += TBT) {
-        const int gi = i0 + k / TB, gj = j0 + k % TB;
-        if (gi < n1 && gj < n2) gx[IX(gi, gj, n2)] = x[(k / TB + H) * R + (k % TB + H)];
-    }
-}
-
-template <class T, int H>
-constexpr size_t tb_smem() {
-    return sizeof(T) * (size_t)(3 * (TB + 2 * H) * (TB + 2 * H) + 2 * (TB + 2 * H + 1) * (TB + 2 * H));
-}
-

@@ -764,9 +764,6 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         T.cl_cta0 = env_long("IMPEC_MG_CL_CTA0", T.cl_cta0);
         T.coarse_cells64 = env_long("IMPEC_MG_COARSE_CELLS64", T.coarse_cells64);
         T.coarse_cells32 = env_long("IMPEC_MG_COARSE_CELLS32", T.coarse_cells32);
-        T.fused32 = env_long("IMPEC_MG_FUSED32", T.fused32);
-        T.fused64 = env_long("IMPEC_MG_FUSED64", T.fused64);
-        T.fuse_fine = env_long("IMPEC_MG_FUSE_FINE", T.fuse_fine);
         T.rb_skip = env_long("IMPEC_MG_RB_SKIP", T.rb_skip);
         T.rb_resid = env_long("IMPEC_MG_RB_RESID", T.rb_resid);
         ctx->cn_predict = env_long("IMPEC_CN_PREDICT", 1) != 0;
@@ -793,10 +790,6 @@ impec_status pressure_alloc(impec_ctx* ctx) {
             if (cluster_size_for<double>(cs) && cluster_size_for<float>(cs)) ctx->cl_size = cs;
     }
     cudaGetLastError();
-    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_pre<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<double, TBH_PRE>()));
-    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_post<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<double, TBH_POST>()));
-    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_pre<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<float, TBH_PRE>()));
-    IMPEC_CUDA_TRY(cudaFuncSetAttribute(k_level_post<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<float, TBH_POST>()));
     return IMPEC_OK;
 }
 
@@ -987,6 +980,13 @@ static size_t coarse_start(const impec_ctx* ctx) {
     return ctx->L.size() - 1;
 }
 
+// The colour whose residual the restriction skips: after a five-point pre-smoothing the colour
+// updated last (black, 1) has a residual of zero up to one rounding.  -1: none.  Every V-cycle
+// implementation (per-level, cluster, single-CTA) uses it, so they stay bit-identical.
+static int restrict_zero_color(const impec_ctx* ctx, const Level& Lv) {
+    return ctx->tune.rb_resid != 0 && Lv.kind == FACE5 && ctx->tune.pre >= 1 ? 1 : -1;
+}
+
 template <class T>
 static void launch_coarse(impec_ctx* ctx, size_t lc) {
     CoarseArgs<T> A{};
@@ -994,6 +994,7 @@ static void launch_coarse(impec_ctx* ctx, size_t lc) {
     A.singular = ctx->singular;
     A.pre = (int)ctx->tune.pre;
     A.post = (int)ctx->tune.post;
+    A.zero_color = restrict_zero_color(ctx, ctx->L[lc]);
     A.dn = ctx->dense_n;
     A.dinv = ctx->dense_inv;
     for (int k = 0; k < A.nl; ++k) {
@@ -1029,6 +1030,7 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
     A.singular = ctx->singular;
     A.pre = (int)ctx->tune.pre;
     A.post = (int)ctx->tune.post;
+    A.zero_color = restrict_zero_color(ctx, ctx->L[ls]);
     A.dn = ctx->dense_n;
     A.dinv = ctx->dense_inv;
     size_t off = 0;
@@ -1105,24 +1107,13 @@ static void launch_cluster(impec_ctx* ctx, size_t ls) {
     cudaLaunchKernelEx(&cfg, k_cluster_vcycle<T>, A);
 }
 
-// Temporally blocked level kernels (two launches per level and cycle), only on request: on
-// GB300 they are slower than full-sweep launches in both precisions, because the halo cells
-// they recompute cost FP64 issue slots and their per-CTA phases serialise.
-template <class T>
-static bool use_fused_level(const impec_ctx* ctx, size_t l) {
-    const Tuning& t = ctx->tune;
-    if (t.pre != 2 || t.post != 2) return false;  // the fused kernels do V(2,2)
-    const bool level_ok = l > 0 || (t.fuse_fine != 0 && ctx->dir_row < 0);
-    return level_ok && (sizeof(T) == 4 ? t.fused32 : t.fused64) != 0;
-}
-
 // Whether the V-cycle at level l runs per-level red-black kernels, so that a cycle started
 // from x = 0 needs no zero fill of the level's iterate (the first colour is k_rb_zero).
 template <class T>
 static bool zero_start_free(impec_ctx* ctx, size_t l) {
     const Level& F = ctx->L[l];
     return ctx->tune.rb_skip != 0 && F.kind == FACE5 && ctx->tune.pre >= 1 && l != cluster_start<T>(ctx) &&
-           l != coarse_start<T>(ctx) && !use_fused_level<T>(ctx, l);
+           l != coarse_start<T>(ctx);
 }
 
 // One V-cycle from level l down.  zero: the level's iterate stands for x = 0; unless
@@ -1146,20 +1137,9 @@ static void vcycle(impec_ctx* ctx, size_t l, bool zero) {
     const T *ctx_, *cty, *ca9, *cid;
     T *cx, *cb;
     level_ptrs<T>(C, ctx_, cty, ca9, cid, cx, cb);
-    const bool fused = F.kind == FACE5 && use_fused_level<T>(ctx, l);
-    if (fused) {  // two launches for this level: smooth+residual+restrict, prolong+smooth
-        dim3 g((F.n2 + TB - 1) / TB, (F.n1 + TB - 1) / TB);
-        ++ctx->nlaunch;
-        launch_k(ctx->stream, k_level_pre<T>, g, TBT, tb_smem<T, TBH_PRE>(), F.n1, F.n2, tx, ty, id, b, x, C.n2, cb, cx, C.n1);
-        vcycle<T>(ctx, l + 1, true);
-        ++ctx->nlaunch;
-        launch_k(ctx->stream, k_level_post<T>, g, TBT, tb_smem<T, TBH_POST>(), F.n1, F.n2, tx, ty, id, b, x, C.n1, C.n2, cx);
-        return;
-    }
     smooth<T>(ctx, F, (int)ctx->tune.pre, false, zero && zero_start_free<T>(ctx, l));
     ++ctx->nlaunch;
-    // after a five-point pre-smoothing the colour updated last (black) has a zero residual
-    const int zero_color = ctx->tune.rb_resid != 0 && F.kind == FACE5 && ctx->tune.pre >= 1 ? 1 : -1;
+    const int zero_color = restrict_zero_color(ctx, F);
     launch_k(ctx->stream, k_restrict<T>, grid2(C.n1, C.n2), dim3(BX, BY), 0, F, tx, ty, a9, level_diag<T>(F), b, x,
              C.n1, C.n2, cb, zero_start_free<T>(ctx, l + 1) ? nullptr : cx, zero_color);
     vcycle<T>(ctx, l + 1, true);
