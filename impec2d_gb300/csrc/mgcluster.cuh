@@ -32,6 +32,7 @@ struct ClusterArgs {
     int singular, dn;
     int pre, post;  // smoother sweeps before / after the coarse correction
     int zero_color;  // restriction skips cells of this colour (their residual is ~0), or -1
+    int rb_skip;     // first pre-smoothing colour from x = 0 (no neighbours); red-only prolongation
     int n1[CL_MAXL], n2[CL_MAXL], rows[CL_MAXL];
     unsigned off[CL_MAXL][6];  // shared-memory offsets (elements of T) of tx, ty, id, dg, x, b
     const T* tx[CL_MAXL];
@@ -61,10 +62,11 @@ __device__ __forceinline__ void cl_band(const ClusterArgs<T>& A, int l, int rank
     cnt = hi > lo ? hi - lo : 0;
 }
 
-// One colour of a red-black sweep on the band (the arithmetic of k_rb_face5).
+// One colour of a red-black sweep on the band (the arithmetic of k_rb_face5; with zero, the
+// first colour of a sweep from x = 0, that of k_rb_zero: x = b * idiag, no neighbour read).
 template <class T>
 __device__ void cl_sweep(const cooperative_groups::cluster_group& cl, T* sm, int rank, const ClusterArgs<T>& A,
-                         int l, int col) {
+                         int l, int col, bool zero = false) {
     int lo, cnt;
     cl_band(A, l, rank, lo, cnt);
     if (cnt == 0) return;
@@ -74,6 +76,13 @@ __device__ void cl_sweep(const cooperative_groups::cluster_group& cl, T* sm, int
     const T* tx = sm + A.off[l][CL_TX];
     const T* ty = sm + A.off[l][CL_TY];
     const T* id = sm + A.off[l][CL_ID];
+    if (zero) {
+        for (int k = threadIdx.x; k < cnt * half; k += blockDim.x) {
+            const int li = k / half, i = lo + li, j = 2 * (k - li * half) + ((i + col) & 1);
+            if (j < n2) x[li * n2 + j] = b[li * n2 + j] * id[li * n2 + j];
+        }
+        return;
+    }
     const T* xup = lo > 0 ? cl_row(cl, sm, rank, A, l, CL_X, lo - 1, n2) : nullptr;
     const T* xdn = lo + cnt < n1 ? cl_row(cl, sm, rank, A, l, CL_X, lo + cnt, n2) : nullptr;
     for (int k = threadIdx.x; k < cnt * half; k += blockDim.x) {
@@ -126,7 +135,9 @@ __device__ void cl_restrict(const cooperative_groups::cluster_group& cl, T* sm, 
     }
 }
 
-// Bilinear prolongation of the coarse iterate added to the band (the arithmetic of k_prolong).
+// Bilinear prolongation of the coarse iterate added to the band (the arithmetic of k_prolong;
+// with A.rb_skip on the red cells only, as k_prolong_rb: the post-smoothing that follows
+// starts with the black colour and overwrites every black cell unread).
 template <class T>
 __device__ void cl_prolong(const cooperative_groups::cluster_group& cl, T* sm, int rank, const ClusterArgs<T>& A,
                            int l) {
@@ -137,6 +148,7 @@ __device__ void cl_prolong(const cooperative_groups::cluster_group& cl, T* sm, i
     T* x = sm + A.off[l][CL_X];
     for (int k = threadIdx.x; k < cnt * n2; k += blockDim.x) {
         const int li = k / n2, j = k - li * n2, i = lo + li;
+        if (A.rb_skip && ((i + j) & 1)) continue;
         const int I = i >> 1, J = j >> 1;
         int I2 = (i & 1) ? I + 1 : I - 1, J2 = (j & 1) ? J + 1 : J - 1;
         if (I2 < 0 || I2 >= c1) I2 = I;
@@ -224,7 +236,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
     // down: levels spread over the cluster
     for (int l = 0; l < A.nd; ++l) {
         for (int s = 0; s < 2 * A.pre; ++s) {
-            cl_sweep(cl, sm, rank, A, l, s & 1);
+            cl_sweep(cl, sm, rank, A, l, s & 1, A.rb_skip && s == 0 && l > 0);
             cl.sync();
         }
         cl_restrict(cl, sm, rank, A, l);
@@ -234,7 +246,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
     if (rank == 0) {
         for (int l = A.nd; l < A.nl - 1; ++l) {
             for (int s = 0; s < 2 * A.pre; ++s) {
-                cl_sweep(cl, sm, 0, A, l, s & 1);
+                cl_sweep(cl, sm, 0, A, l, s & 1, A.rb_skip && s == 0 && l > 0);
                 __syncthreads();
             }
             cl_restrict(cl, sm, 0, A, l);

@@ -1031,6 +1031,7 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
     A.pre = (int)ctx->tune.pre;
     A.post = (int)ctx->tune.post;
     A.zero_color = restrict_zero_color(ctx, ctx->L[ls]);
+    A.rb_skip = ctx->tune.rb_skip != 0 && ctx->tune.pre >= 1 && ctx->tune.post >= 1 ? 1 : 0;
     A.dn = ctx->dense_n;
     A.dinv = ctx->dense_inv;
     size_t off = 0;
