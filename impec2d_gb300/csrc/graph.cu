@@ -149,9 +149,6 @@ static impec_status capture_step_into(impec_ctx* ctx, int pfs_in) {
     };
     impec_status s = body();
     ctx->stream = saved;
-    const long long loops = mg_body + (P.diffusion ? 2 * ctx->step_cn_body_launches : 0);
-    ctx->step_outer_launches = ctx->nlaunch - n0 - loops;
-    ctx->step_mg_body_launches = mg_body;
     ctx->nlaunch = n0;  // captured launches run (and are counted) on the device at each replay
     return s;
 }
@@ -200,8 +197,6 @@ static impec_status capture_pressure(impec_ctx* ctx, cudaGraph_t* out) {
     cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
     IMPEC_TRY(s);
     IMPEC_CUDA_TRY(e);
-    ctx->pressure_outer_launches = ctx->nlaunch - n0 - mg_body;
-    ctx->step_mg_body_launches = mg_body;
     ctx->nlaunch = n0;
     *out = g;
     return IMPEC_OK;

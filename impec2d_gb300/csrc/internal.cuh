@@ -156,7 +156,6 @@ struct impec_ctx {
     int krylov = 1;  // 1: CG with one V-cycle as preconditioner; 0: stationary V-cycles
     impec::Tuning tune;
     int cn_predict = 1;  // CN starts from the explicit-Euler predictor (IMPEC_CN_PREDICT=0: from c)
-    double solve_tol = 1e-10;  // tolerance of the pressure solve being launched or captured
     int dense_n = 0;
     int pin_i = 1, pin_j = 1;
     double pin_kappa = 1.0;
@@ -193,8 +192,7 @@ struct impec_ctx {
     cudaStream_t cap_stream = nullptr, body_stream = nullptr;
     cudaGraphExec_t step_exec[2] = {nullptr, nullptr};
     cudaGraphExec_t pressure_exec = nullptr;
-    long long pressure_outer_launches = 0;
-    long long step_outer_launches = 0, step_mg_body_launches = 0, step_cn_body_launches = 0;
+    long long step_cn_body_launches = 0;  // kernels of one CN loop body (the step graph's launch count)
     // learned initial guess (learned_net.cu): the attached network's state, and the residual of
     // the previous pressure, the predicted direction, its image under A and the step length
     impec::LearnedHook* learned = nullptr;

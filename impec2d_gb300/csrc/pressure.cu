@@ -1428,7 +1428,6 @@ impec_status pressure_residual(impec_ctx* ctx) {
 }
 
 impec_status pressure_check(impec_ctx* ctx, double tol, int inc, cudaGraphConditionalHandle h, int use_h) {
-    ctx->solve_tol = tol;
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_mg_check, 1, 1, 0, ctx->dscal, tol, ctx->P.max_cycles, inc, h, use_h, ctx->krylov);
     IMPEC_LAUNCH_CHECK();
@@ -1439,7 +1438,6 @@ impec_status pressure_check(impec_ctx* ctx, double tol, int inc, cudaGraphCondit
 // only): a stationary V-cycle, or a CG step preconditioned by one V-cycle (whose residual
 // kernel also runs the check).  h / use_h: the graph's WHILE condition, as pressure_check.
 impec_status pressure_step(impec_ctx* ctx, double tol, cudaGraphConditionalHandle h, int use_h) {
-    ctx->solve_tol = tol;
     if (!ctx->krylov) {
         IMPEC_TRY(pressure_iteration(ctx, tol, h, use_h));
         return pressure_check(ctx, tol, 1, h, use_h);
