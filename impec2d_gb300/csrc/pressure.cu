@@ -441,7 +441,7 @@ __device__ __forceinline__ T resid(const Level& Lv, int i, int j, const T* __res
 template <class T>
 __global__ void k_restrict(Level F, const T* __restrict__ tx, const T* __restrict__ ty, const T* __restrict__ a9,
                            const T* __restrict__ dg, const T* __restrict__ b, const T* __restrict__ x, int n1c,
-                           int n2c, T* __restrict__ bc, T* __restrict__ xc, int zero_color) {
+                           int n2c, T* __restrict__ bc, T* __restrict__ xc, int zero_color, const T* __restrict__ idc) {
     pdl_enter();
     int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
     if (I >= n1c || J >= n2c) return;
@@ -455,7 +455,11 @@ __global__ void k_restrict(Level F, const T* __restrict__ tx, const T* __restric
             if (i < F.n1 && j < F.n2) s += resid<T>(F, i, j, tx, ty, a9, dg, b, x);
         }
     bc[IX(I, J, n2c)] = s;
-    if (xc) xc[IX(I, J, n2c)] = 0;  // nullptr: the coarse cycle starts from x = 0 by itself
+    // The coarse cycle starts from x = 0.  Without idc that zero is written.  With idc (the
+    // coarse 1/diag), the coarse pre-smoothing's first colour (red, as k_rb_zero:
+    // x = b * idiag) is done here, and the black cells are left for its black pass to overwrite.
+    if (!idc) xc[IX(I, J, n2c)] = 0;
+    else if (((I + J) & 1) == 0) xc[IX(I, J, n2c)] = s * idc[IX(I, J, n2c)];
 }
 
 // Bilinear cell-centred prolongation (weights 9/16, 3/16, 3/16, 1/16; the outside
@@ -929,9 +933,10 @@ static dim3 rb_grid(const Level& Lv) {
 }
 
 // zero: x holds no values yet and stands for x = 0 (five-point levels only, where the first
-// colour's update then needs no neighbour).
+// colour's update then needs no neighbour).  first_done: that first colour was already done
+// by the restriction that produced b (k_restrict with the coarse 1/diag).
 template <class T>
-static void smooth(impec_ctx* ctx, Level& Lv, int sweeps, bool reverse, bool zero = false) {
+static void smooth(impec_ctx* ctx, Level& Lv, int sweeps, bool reverse, bool zero = false, bool first_done = false) {
     const T *tx, *ty, *a9, *id;
     T *x, *b;
     level_ptrs<T>(Lv, tx, ty, a9, id, x, b);
@@ -940,11 +945,14 @@ static void smooth(impec_ctx* ctx, Level& Lv, int sweeps, bool reverse, bool zer
             const dim3 g = rb_grid(Lv);
             for (int cc = 0; cc < 2; ++cc) {
                 const int col = reverse ? 1 - cc : cc;
-                ++ctx->nlaunch;
-                if (zero && s == 0 && cc == 0)
+                if (zero && s == 0 && cc == 0) {
+                    if (first_done) continue;
+                    ++ctx->nlaunch;
                     launch_k(ctx->stream, k_rb_zero<T>, g, dim3(BX, BY), 0, Lv.n1, Lv.n2, id, b, x, col);
-                else
+                } else {
+                    ++ctx->nlaunch;
                     launch_k(ctx->stream, k_rb_face5<T>, g, dim3(BX, BY), 0, Lv.n1, Lv.n2, tx, ty, id, b, x, col);
+                }
             }
         } else {
             dim3 g(((Lv.n2 + 1) / 2 + BX - 1) / BX, ((Lv.n1 + 1) / 2 + BY - 1) / BY);
@@ -1118,9 +1126,10 @@ static bool zero_start_free(impec_ctx* ctx, size_t l) {
 }
 
 // One V-cycle from level l down.  zero: the level's iterate stands for x = 0; unless
-// zero_start_free<T>(ctx, l), the caller has filled it with zeros.
+// zero_start_free<T>(ctx, l), the caller has filled it with zeros.  first_done: the caller
+// (the restriction from level l - 1) also did the pre-smoothing's first colour.
 template <class T>
-static void vcycle(impec_ctx* ctx, size_t l, bool zero) {
+static void vcycle(impec_ctx* ctx, size_t l, bool zero, bool first_done = false) {
     Level& F = ctx->L[l];
     const T *tx, *ty, *a9, *id;
     T *x, *b;
@@ -1138,12 +1147,14 @@ static void vcycle(impec_ctx* ctx, size_t l, bool zero) {
     const T *ctx_, *cty, *ca9, *cid;
     T *cx, *cb;
     level_ptrs<T>(C, ctx_, cty, ca9, cid, cx, cb);
-    smooth<T>(ctx, F, (int)ctx->tune.pre, false, zero && zero_start_free<T>(ctx, l));
+    const bool zs = zero && zero_start_free<T>(ctx, l);
+    smooth<T>(ctx, F, (int)ctx->tune.pre, false, zs, zs && first_done);
     ++ctx->nlaunch;
     const int zero_color = restrict_zero_color(ctx, F);
+    const bool cz = zero_start_free<T>(ctx, l + 1);  // the coarse cycle's first colour is done here
     launch_k(ctx->stream, k_restrict<T>, grid2(C.n1, C.n2), dim3(BX, BY), 0, F, tx, ty, a9, level_diag<T>(F), b, x,
-             C.n1, C.n2, cb, zero_start_free<T>(ctx, l + 1) ? nullptr : cx, zero_color);
-    vcycle<T>(ctx, l + 1, true);
+             C.n1, C.n2, cb, cx, zero_color, cz ? (const T*)cid : nullptr);
+    vcycle<T>(ctx, l + 1, true, cz);
     const unsigned char* mask = l == 0 && ctx->dir_row >= 0 ? ctx->dmask : nullptr;
     ++ctx->nlaunch;
     if (ctx->tune.rb_skip != 0 && F.kind == FACE5 && ctx->tune.post >= 1)  // the black cells are overwritten next
