@@ -96,12 +96,22 @@ __global__ void k_corner(int n1, int n2, const double* __restrict__ w1, const do
 
 // ---------------------------------------------------------------- fine operators
 // nu = 1: face transmissibilities dA/dx^2 * lambda with zero flux through the boundary.
+// tx32 / ty32 (or nullptr): their FP32 copies for the mixed-precision cycle.
 __global__ void k_face5_fine(int n1, int n2, const double* __restrict__ lamx, const double* __restrict__ lamy,
-                             double sx, double sy, double* __restrict__ tx, double* __restrict__ ty) {
+                             double sx, double sy, double* __restrict__ tx, double* __restrict__ ty,
+                             float* __restrict__ tx32, float* __restrict__ ty32) {
     pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
-    if (i <= n1 && j < n2) tx[IX(i, j, n2)] = (i == 0 || i == n1) ? 0.0 : lamx[IX(i, j, n2)] * sx;
-    if (i < n1 && j <= n2) ty[IX(i, j, n2 + 1)] = (j == 0 || j == n2) ? 0.0 : lamy[IX(i, j, n2 + 1)] * sy;
+    if (i <= n1 && j < n2) {
+        const double t = (i == 0 || i == n1) ? 0.0 : lamx[IX(i, j, n2)] * sx;
+        tx[IX(i, j, n2)] = t;
+        if (tx32) tx32[IX(i, j, n2)] = (float)t;
+    }
+    if (i < n1 && j <= n2) {
+        const double t = (j == 0 || j == n2) ? 0.0 : lamy[IX(i, j, n2 + 1)] * sy;
+        ty[IX(i, j, n2 + 1)] = t;
+        if (ty32) ty32[IX(i, j, n2 + 1)] = (float)t;
+    }
 }
 
 // Reference row (C,W,SW,S,SE,E,NE,N,NW) of GetWeightedMatrixCoefficientsForCell
@@ -166,7 +176,8 @@ __constant__ int c_off[9][2] = {{0, 0}, {-1, 0}, {-1, -1}, {0, -1}, {1, -1}, {1,
 
 // ---------------------------------------------------------------- coarse operators
 __global__ void k_face5_coarsen(int n1f, int n2f, const double* __restrict__ txf, const double* __restrict__ tyf,
-                                int n1c, int n2c, double* __restrict__ txc, double* __restrict__ tyc) {
+                                int n1c, int n2c, double* __restrict__ txc, double* __restrict__ tyc,
+                                float* __restrict__ txc32, float* __restrict__ tyc32) {
     pdl_enter();
     int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
     if (I <= n1c && J < n2c) {
@@ -177,6 +188,7 @@ __global__ void k_face5_coarsen(int n1f, int n2f, const double* __restrict__ txf
             if (2 * J + 1 < n2f) s += txf[IX(fi, 2 * J + 1, n2f)];
         }
         txc[IX(I, J, n2c)] = 0.5 * s;
+        if (txc32) txc32[IX(I, J, n2c)] = (float)(0.5 * s);
     }
     if (I < n1c && J <= n2c) {
         int fj = 2 * J;
@@ -186,6 +198,7 @@ __global__ void k_face5_coarsen(int n1f, int n2f, const double* __restrict__ txf
             if (2 * I + 1 < n1f) s += tyf[IX(2 * I + 1, fj, n2f + 1)];
         }
         tyc[IX(I, J, n2c + 1)] = 0.5 * s;
+        if (tyc32) tyc32[IX(I, J, n2c + 1)] = (float)(0.5 * s);
     }
 }
 
@@ -304,7 +317,8 @@ __global__ void k_dirichlet_rhs(size_t n, double* __restrict__ f, double* __rest
 
 __global__ void k_idiag(int n1, int n2, int kind, const double* __restrict__ tx, const double* __restrict__ ty,
                         const double* __restrict__ a9, const double* __restrict__ ed,
-                        const unsigned char* __restrict__ mask, double* __restrict__ diag, double* __restrict__ idiag) {
+                        const unsigned char* __restrict__ mask, double* __restrict__ diag, double* __restrict__ idiag,
+                        float* __restrict__ diag32, float* __restrict__ idiag32) {
     pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     if (i >= n1 || j >= n2) return;
@@ -316,8 +330,11 @@ __global__ void k_idiag(int n1, int n2, int kind, const double* __restrict__ tx,
         d = a9[IX(i, j, n2)];
     }
     if (mask && mask[IX(i, j, n2)]) d = 1.0;  // known cell: x = rhs
+    const double id = d != 0.0 ? 1.0 / d : 0.0;
     diag[IX(i, j, n2)] = d;
-    idiag[IX(i, j, n2)] = d != 0.0 ? 1.0 / d : 0.0;
+    idiag[IX(i, j, n2)] = id;
+    if (diag32) diag32[IX(i, j, n2)] = (float)d;  // FP32 copies for the mixed-precision cycle
+    if (idiag32) idiag32[IX(i, j, n2)] = (float)id;
 }
 
 __global__ void k_to_float(size_t n, const double* __restrict__ a, float* __restrict__ b) {
@@ -835,17 +852,21 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
     IMPEC_TRY(face_mobility(ctx, c));
     Level& F = ctx->L[0];
     const Geo& G = ctx->G;
+    const bool mixed = P.precision == IMPEC_PREC_MIXED;
+    // Dirichlet row (horizontal source): known cells out of the operator, their values into fd
+    const bool dir = ctx->dir_row >= 0 && ctx->eliminate;
+    // FP32 copies of the five-point faces written with the FP64 ones, except the finest
+    // level's faces when the Dirichlet elimination changes them afterwards
+    const bool f32 = mixed && F.kind == FACE5;
     if (F.kind == FACE5) {
         double sx = G.dA * (1. / (G.dx * G.dx)), sy = G.dA * (1. / (G.dy * G.dy));
         ++ctx->nlaunch, launch_k(ctx->stream, k_face5_fine, grid2(F.n1 + 1, F.n2 + 1), dim3(BX, BY), 0, F.n1, F.n2, ctx->lamx, ctx->lamy,
-                                                                                  sx, sy, F.tx, F.ty);
+                                 sx, sy, F.tx, F.ty, f32 && !dir ? F.tx32 : nullptr, f32 && !dir ? F.ty32 : nullptr);
     } else {
         ++ctx->nlaunch, launch_k(ctx->stream, k_exp9_fine, grid2(F.n1, F.n2), dim3(BX, BY), 0, F.n1, F.n2, ctx->lamx, ctx->lamy, ctx->cm11,
                                                                          ctx->cm22, ctx->cm12, P.nu, G, F.a9);
     }
     IMPEC_LAUNCH_CHECK();
-    // Dirichlet row (horizontal source): known cells out of the operator, their values into fd
-    const bool dir = ctx->dir_row >= 0 && ctx->eliminate;
     const unsigned char* mask0 = dir ? ctx->dmask : nullptr;
     if (dir) {
         const size_t n = F.n();
@@ -865,7 +886,7 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
         Level &A = ctx->L[l], &B = ctx->L[l + 1];
         if (A.kind == FACE5) {
             ++ctx->nlaunch, launch_k(ctx->stream, k_face5_coarsen, grid2(B.n1 + 1, B.n2 + 1), dim3(BX, BY), 0, A.n1, A.n2, A.tx, A.ty, B.n1,
-                                                                                        B.n2, B.tx, B.ty);
+                                     B.n2, B.tx, B.ty, f32 ? B.tx32 : nullptr, f32 ? B.ty32 : nullptr);
             if (dir)
                 ++ctx->nlaunch, launch_k(ctx->stream, k_ed_coarsen, grid2(B.n1, B.n2), dim3(BX, BY), 0, A.n1, A.n2, A.ed,
                                          B.n1, B.n2, B.ed);
@@ -875,21 +896,20 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
         }
         IMPEC_LAUNCH_CHECK();
     }
-    const bool mixed = P.precision == IMPEC_PREC_MIXED;
     for (size_t l = 0; l < ctx->L.size(); ++l) {
         Level& Lv = ctx->L[l];
         ++ctx->nlaunch, launch_k(ctx->stream, k_idiag, grid2(Lv.n1, Lv.n2), dim3(BX, BY), 0, Lv.n1, Lv.n2, Lv.kind, Lv.tx,
                                  Lv.ty, Lv.a9, dir && Lv.kind == FACE5 ? Lv.ed : nullptr, l == 0 ? mask0 : nullptr,
-                                 Lv.diag, Lv.idiag);
+                                 Lv.diag, Lv.idiag, mixed ? Lv.diag32 : nullptr, mixed ? Lv.idiag32 : nullptr);
         IMPEC_LAUNCH_CHECK();
         if (mixed) {
             const size_t n = Lv.n();
             int nb = ctx->num_sms * 4;
-            ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, n, Lv.idiag, Lv.idiag32);
-            ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, n, Lv.diag, Lv.diag32);
             if (Lv.kind == FACE5) {
-                ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)(Lv.n1 + 1) * Lv.n2, Lv.tx, Lv.tx32);
-                ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)Lv.n1 * (Lv.n2 + 1), Lv.ty, Lv.ty32);
+                if (l == 0 && dir) {  // the elimination changed the finest faces after k_face5_fine
+                    ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)(Lv.n1 + 1) * Lv.n2, Lv.tx, Lv.tx32);
+                    ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)Lv.n1 * (Lv.n2 + 1), Lv.ty, Lv.ty32);
+                }
             } else {
                 ++ctx->nlaunch, launch_k(ctx->stream, k_to_float, nb, 256, 0, n * 9, Lv.a9, Lv.a932);
             }
