@@ -119,28 +119,63 @@ __global__ void k_cn_matrix(CNArgs A, const double* __restrict__ dfx, const doub
     idiag[kk] = 1.0 / o[0];
 }
 
-// SetRHS_Parabolic (src/MGSolver.cpp:1324-1371) with mirrored ghost values of c.
-__global__ void k_cn_rhs(CNArgs A, const double* __restrict__ dfx, const double* __restrict__ dfy,
-                         const double* __restrict__ c, const double* __restrict__ dt_dev, double scale,
-                         double* __restrict__ rhs) {
+// SetRHS_Parabolic (src/MGSolver.cpp:1324-1371) with mirrored ghost values of c, in flux form.
+// The reference's per-cell terms are differences of face terms:
+//   t1 = k4xx (P(i+1/2) - P(i-1/2)),  P = d11 (c_hi - c_lo)                    on x-faces,
+//   t2 = kxy  (Q(i+1/2) - Q(i-1/2)),  Q = d12 (c(a,j+1) + c(a+1,j+1) - c(a,j-1) - c(a+1,j-1)),
+//   t3 = kxy  (S(j+1/2) - S(j-1/2)),  S = d21 (c(i+1,b) + c(i+1,b+1) - c(i-1,b+1) - c(i-1,b)),
+//   t4 = k4yy (R(j+1/2) - R(j-1/2)),  R = d22 (c_hi - c_lo)                    on y-faces,
+// and each face term, summed in the reference's order, has the same value from either side.
+// A block computes the face terms of its 32 x 8 tile once, in shared memory, instead of twice
+// (about 26 FP64 operations per cell instead of 32).  The last rounding of t1..t4 may differ
+// from a per-cell evaluation.  Halo cells beyond an edge take the mirrored value
+// (refl_cell: index -1 -> 0, n -> n-1); cells further out feed only faces outside the grid.
+__global__ void __launch_bounds__(DBX * DBY) k_cn_rhs(CNArgs A, const double* __restrict__ dfx,
+                                                      const double* __restrict__ dfy, const double* __restrict__ c,
+                                                      const double* __restrict__ dt_dev, double scale,
+                                                      double* __restrict__ rhs) {
     pdl_enter();
-    int j = blockIdx.x * DBX + threadIdx.x, i = blockIdx.y * DBY + threadIdx.y;
-    const int n1 = A.n1, n2 = A.n2;
+    __shared__ double cs[DBY + 2][DBX + 2];
+    __shared__ double fp[DBY + 1][DBX], fq[DBY + 1][DBX];  // x-faces i0 .. i0 + DBY of the tile's columns
+    __shared__ double fr[DBY][DBX + 1], fs[DBY][DBX + 1];  // y-faces j0 .. j0 + DBX of the tile's rows
+    const int n1 = A.n1, n2 = A.n2, t = threadIdx.y * DBX + threadIdx.x;
+    const int i0 = blockIdx.y * DBY, j0 = blockIdx.x * DBX;
+    for (int k = t; k < (DBY + 2) * (DBX + 2); k += DBX * DBY) {
+        const int i = min(max(i0 - 1 + k / (DBX + 2), 0), n1 - 1), j = min(max(j0 - 1 + k % (DBX + 2), 0), n2 - 1);
+        cs[k / (DBX + 2)][k % (DBX + 2)] = c[IX(i, j, n2)];
+    }
+    __syncthreads();
+    for (int k = t; k < (DBY + 1) * DBX; k += DBX * DBY) {  // x-face (i0 + r, j): cs rows r, r + 1
+        const int r = k / DBX, q = k % DBX, fi = i0 + r, j = j0 + q;
+        double P = 0.0, Q = 0.0;
+        if (fi <= n1 && j < n2) {
+            const size_t f = IX(fi, j, n2);
+            P = dfx[2 * f] * (cs[r + 1][q + 1] - cs[r][q + 1]);
+            Q = dfx[2 * f + 1] * (cs[r][q + 2] + cs[r + 1][q + 2] - cs[r][q] - cs[r + 1][q]);
+        }
+        fp[r][q] = P;
+        fq[r][q] = Q;
+    }
+    for (int k = t; k < DBY * (DBX + 1); k += DBX * DBY) {  // y-face (i, j0 + q): cs columns q, q + 1
+        const int r = k / (DBX + 1), q = k % (DBX + 1), i = i0 + r, fj = j0 + q;
+        double R = 0.0, S = 0.0;
+        if (i < n1 && fj <= n2) {
+            const size_t f = IX(i, fj, n2 + 1);
+            R = dfy[2 * f] * (cs[r + 1][q + 1] - cs[r + 1][q]);
+            S = dfy[2 * f + 1] * (cs[r + 2][q] + cs[r + 2][q + 1] - cs[r][q + 1] - cs[r][q]);
+        }
+        fr[r][q] = R;
+        fs[r][q] = S;
+    }
+    __syncthreads();
+    const int ty = threadIdx.y, tx = threadIdx.x, i = i0 + ty, j = j0 + tx;
     if (i >= n1 || j >= n2) return;
     const double dt = scale * dt_dev[0];
-    size_t kx0 = IX(i, j, n2), kx1 = IX(i + 1, j, n2), ky0 = IX(i, j, n2 + 1), ky1 = IX(i, j + 1, n2 + 1);
-    double d11_im = dfx[2 * kx0], d12_im = dfx[2 * kx0 + 1], d11_ip = dfx[2 * kx1], d12_ip = dfx[2 * kx1 + 1];
-    double d22_jm = dfy[2 * ky0], d21_jm = dfy[2 * ky0 + 1], d22_jp = dfy[2 * ky1], d21_jp = dfy[2 * ky1 + 1];
-    const int im = refl_cell(i - 1, n1), ip = refl_cell(i + 1, n1), jm = refl_cell(j - 1, n2), jp = refl_cell(j + 1, n2);
-    auto cc = [&](int a, int b) { return c[IX(a, b, n2)]; };
-    const double c0 = cc(i, j);
-    double t1 = A.k4xx * (d11_ip * (cc(ip, j) - c0) - d11_im * (c0 - cc(im, j)));
-    double t2 = A.kxy * (d12_ip * (cc(i, jp) + cc(ip, jp) - cc(i, jm) - cc(ip, jm)) -
-                         d12_im * (cc(i, jp) + cc(im, jp) - cc(im, jm) - cc(i, jm)));
-    double t3 = A.kxy * (d21_jp * (cc(ip, j) + cc(ip, jp) - cc(im, jp) - cc(im, j)) -
-                         d21_jm * (cc(ip, j) + cc(ip, jm) - cc(im, j) - cc(im, jm)));
-    double t4 = A.k4yy * (d22_jp * (cc(i, jp) - c0) - d22_jm * (c0 - cc(i, jm)));
-    rhs[IX(i, j, n2)] = i == A.dir_row ? 0.0 : c0 + dt * 0.125 * (t1 + t2 + t3 + t4);
+    const double t1 = A.k4xx * (fp[ty + 1][tx] - fp[ty][tx]);
+    const double t2 = A.kxy * (fq[ty + 1][tx] - fq[ty][tx]);
+    const double t3 = A.kxy * (fs[ty][tx + 1] - fs[ty][tx]);
+    const double t4 = A.k4yy * (fr[ty][tx + 1] - fr[ty][tx]);
+    rhs[IX(i, j, n2)] = i == A.dir_row ? 0.0 : cs[ty + 1][tx + 1] + dt * 0.125 * (t1 + t2 + t3 + t4);
 }
 
 // First CN iterate: the explicit-Euler predictor x0 = 2 b - c = c + dt L c (b = c + dt/2 L c).
