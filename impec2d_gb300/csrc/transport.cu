@@ -409,8 +409,15 @@ constexpr size_t NOALLOC_MAX_CELLS = size_t(1) << 20;  // 1,048,576 cells: 8 MiB
 constexpr size_t NOALLOC_FIELD_OFFSET = 32;            // doubles before the field (dt at [0]); 256-byte aligned
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_FIELD_OFFSET + NOALLOC_MAX_CELLS];
 
+// Stores dt in the scratch.  dt travels as a kernel argument, so the value itself is what a
+// launch (or a captured launch node) carries; a host-to-device copy would instead carry the
+// address of the caller's stack variable.
+__global__ void k_noalloc_store_dt(double* __restrict__ dst, double dt) { dst[0] = dt; }
+
 // Device address of g_noalloc_scratch on the current device, looked up once per device (the
-// host-side name of the array is only a stand-in, not a device address).
+// host-side name of the array is only a stand-in, not a device address).  The address is kept
+// for the life of the process: after cudaDeviceReset on that device this entry point must not
+// be called again.
 static impec_status noalloc_scratch(double** out) {
     static std::mutex mu;
     static double* addr[64] = {nullptr};
@@ -440,6 +447,12 @@ extern "C" impec_status impec_advect_symmetric_noalloc(const impec_params* P, do
         return IMPEC_ERR_ARG;
     }
     if (P->hmtype != IMPEC_MUSCL && P->hmtype != IMPEC_UPWINDSPLIT) { set_error("unknown hmtype"); return IMPEC_ERR_ARG; }
+    if (P->bc != IMPEC_BC_NEUMANN && P->bc != IMPEC_BC_PERIODIC) { set_error("unknown bc"); return IMPEC_ERR_ARG; }
+    if (P->dim_splitting != IMPEC_SYMMETRIC_PARALLEL) {
+        set_error("impec_advect_symmetric_noalloc performs only the symmetric-parallel splitting; "
+                  "set dim_splitting to IMPEC_SYMMETRIC_PARALLEL");
+        return IMPEC_ERR_ARG;
+    }
     if (!(P->porosity > 0) || !(P->x_ub > P->x_lb) || !(P->y_ub > P->y_lb) || !(dt >= 0) || isinf(dt)) {
         set_error("invalid porosity, domain or dt");
         return IMPEC_ERR_ARG;
@@ -451,7 +464,7 @@ extern "C" impec_status impec_advect_symmetric_noalloc(const impec_params* P, do
     const double dx = (P->x_ub - P->x_lb) / N1, dy = (P->y_ub - P->y_lb) / N2;
     const double fx = 1.0 / (dx * P->porosity), fy = 1.0 / (dy * P->porosity);
     double* cnew = scratch + NOALLOC_FIELD_OFFSET;
-    IMPEC_CUDA_TRY(cudaMemcpyAsync(scratch, &dt, sizeof(double), cudaMemcpyHostToDevice, s));
+    launch_k(s, k_noalloc_store_dt, 1, 1, 0, scratch, dt);
     dim3 g((N2 + TJ - 1) / TJ, (N1 + TI - 1) / TI);
     const bool per = P->bc == IMPEC_BC_PERIODIC;
     if (P->hmtype == IMPEC_MUSCL) {

@@ -263,14 +263,18 @@ impec_status impec_measure_fp64(double* fma_per_second);
  * under a host framework that owns every device allocation (a fixed pool or budget), or that
  * must avoid cudaMalloc's implicit device-wide synchronisation -- and so cannot create an
  * impec_ctx.  It performs AdvectSplit's symmetric-parallel update (MUSCL or upwind by
- * P->hmtype, Neumann or periodic by P->bc) of c_dev in place, given u_dev, v_dev and dt,
+ * P->hmtype, Neumann or periodic by P->bc; P->dim_splitting must be IMPEC_SYMMETRIC_PARALLEL,
+ * other values are rejected with IMPEC_ERR_ARG) of c_dev in place, given u_dev, v_dev and dt,
  * enqueued on `stream` (may be NULL), without allocating: its scratch (a copy of dt and the
  * updated field) is a static device array of 1,048,576 cells (8 MiB) that every GPU which
  * loads the library holds until process exit.  Nothing in it has to start at zero: each call
  * writes dt and every cell of the updated field before reading them.  Larger grids
- * (N1*N2 > 1,048,576) are rejected with IMPEC_ERR_ARG.  The first call on a device looks up the array's device address, so make
- * that first call before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU (different streams, or different host threads) race on it. */
+ * (N1*N2 > 1,048,576) are rejected with IMPEC_ERR_ARG.  dt is handed to the GPU as a kernel
+ * argument (by value), never copied from the caller's memory.  The first call on a device
+ * looks up the array's device address, so make that first call before any stream capture;
+ * the address is kept for the life of the process, so after cudaDeviceReset on a device do
+ * not call this entry point again in that process.  All calls share the array: calls whose
+ * work overlaps on the GPU (different streams, or different host threads) race on it. */
 impec_status impec_advect_symmetric_noalloc(const impec_params* P, double* c_dev, const double* u_dev,
                                             const double* v_dev, double dt, void* stream);
 

@@ -9,7 +9,8 @@ import pytest
 import impec2d_gb300 as E
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_EXAMPLES = "/root/reference/examples"
+# The reference checkout, when one is at hand: IMPEC2D_REFERENCE names its root directory.
+REF_EXAMPLES = os.path.join(os.environ.get("IMPEC2D_REFERENCE", ""), "examples") if os.environ.get("IMPEC2D_REFERENCE") else ""
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -62,7 +63,8 @@ def test_run_horizontal_pulsing_cfg():
     assert 0.05 < first < 0.0854 and rest < 1e-3
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not mounted")
+@pytest.mark.skipif(not REF_EXAMPLES or not os.path.isdir(REF_EXAMPLES),
+                    reason="IMPEC2D_REFERENCE does not name a reference checkout")
 def test_reference_examples_parse_unchanged():
     files = sorted(glob.glob(os.path.join(REF_EXAMPLES, "*.cfg")))
     assert len(files) == 5
