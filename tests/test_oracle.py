@@ -17,7 +17,7 @@ def _advection_error(L, N, vel, profile=0, cfl=0.95):
     v = np.zeros(O.vel_shape(P))
     for i in range(N):
         for j in range(N):
-            c[i + 2, j + 2] = L.or_profile(C.byref(P), profile, (i + .5) / N, (j + .5) / N)
+            c[i + 2, j + 2] = L.or_profile(C.byref(P), profile, 0.0 + (i + 0.5) * (1.0 / N), 0.0 + (j + 0.5) * (1.0 / N))
     v[..., 0], v[..., 1] = vel
     q = np.zeros(N * N)
     dtmax = L.or_max_stable_advection_dt(C.byref(P), O.ptr(v))
@@ -37,12 +37,15 @@ def _advection_error(L, N, vel, profile=0, cfl=0.95):
 def test_advection_convergence_order_known_answer(oracle_lib):
     """examples/hyperbolic_test.cfg:129-139 documents order 1.87621 for MUSCL (van Leer), sine
     profile, L1 norm, CFL 0.95, 50^2 doubled over 4 levels.  The shipped code advects with the
-    diagonal velocity (-L, L) (src/Impec2DSolver.cpp:1003-1015); the fitted slope (least squares of
-    log err vs log dx, as GnuPlotter::PlotConvergence does) must match within 0.05."""
+    diagonal velocity (-L, L) (src/Impec2DSolver.cpp:1003-1015).  Run through the reference's own
+    compiled code (oracle/_ref, tests/test_ref_pin.py) that case gives the fitted slope (least
+    squares of log err vs log dx, as GnuPlotter::PlotConvergence does) 1.86712, with errors equal
+    to the oracle's; the recorded 1.87621 stays as a loose anchor (within 0.01)."""
     Ns = [50, 100, 200, 400]
     errs = [_advection_error(oracle_lib, N, (-1.0, 1.0)) for N in Ns]
     order = np.polyfit(np.log([1.0 / N for N in Ns]), np.log(errs), 1)[0]
-    assert abs(order - 1.87621) < 0.05, order
+    assert abs(order - 1.86712) < 5e-5, order
+    assert abs(order - 1.87621) < 0.01, order
 
 
 @pytest.mark.parametrize("testno", [1, 4])
