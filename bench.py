@@ -47,6 +47,10 @@ def parse():
                          "weighted nine-point operator")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--later-after", type=int, default=1000,
+                    help="time a second window of --steps steps after this many IMPES steps (0: skip)")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the in-run training of the warm-start network for the pressure-solve line")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch each kernel on the stream instead of replaying the step graph (for ncu)")
     ap.add_argument("--study", default=None, choices=["pressure", "warmstart", "ensemble", "learned", "network"],
@@ -103,6 +107,15 @@ def initial_state(N, seed=1234):
     q[N - 1] = -val
     q[(N - 1) * N] = -val
     return c, q
+
+
+def bench_config(N, precision="fp64", nu=1.0):
+    """The `config` object of both arms' JSON lines: the same workload, named the same way."""
+    return {"workload": f"parallel quarter-five-spot {N}x{N}, MUSCL + CN Peaceman (alpha_l 1e-3, alpha_t 1e-4, "
+                        f"Dm 1e-6), pressure by multigrid to relative residual 1e-10"
+                        + (f", nu = {nu:.4g} (weighted nine-point)" if nu != 1.0 else ""),
+            "precision": precision, "l2": "flushed (256 MB write) between timed steps",
+            "parallelism": "one replica per process"}
 
 
 def workload_params(E, N, precision, nu=1.0):
@@ -162,9 +175,8 @@ def cpu_baseline(N, steps, threads=None, warmup=0, budget_s=None):
 
     import oracle as O
     O.build()
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
     L = O.lib()
+    prev_threads = L.or_set_num_threads(threads) if threads else None
     P = O.make_params(N1=N, N2=N, x_ub=math.sqrt(2.0), y_ub=math.sqrt(2.0), stype=O.PARALLEL, hmtype=O.MUSCL, nu=1.0,
                       diffusion=1, alpha_l=1e-3, alpha_t=1e-4, Dm=1e-6, cfl=0.5, eps=1e-10, para_eps=1e-10)
     c0, q = initial_state(N)
@@ -186,7 +198,78 @@ def cpu_baseline(N, steps, threads=None, warmup=0, budget_s=None):
         if budget_s and time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    return N * N * done / dt, L.or_num_threads(), dt, done
+    used = L.or_num_threads()
+    if prev_threads:
+        L.or_set_num_threads(prev_threads)
+    return N * N * done / dt, used, dt, done
+
+
+def pressure_solves(E, ctx, N, q, args, flush):
+    """ms per pressure solve to 1e-10 on the run's current state: the concentration now and the
+    pressure of the step before it.  Modes: plain FP64 multigrid from a zero guess (the
+    reference's method, src/MGSolver.cpp:575-577) and mixed precision from zero; both from the
+    previous step's pressure; and mixed precision with the learned warm start (the previous
+    pressure moved along the network's prediction), the network trained here first on pairs
+    the solver writes from 256^2 heterogeneous realisations (a short in-run training).  Each
+    timed solve starts from the same c and previous p; CUDA events bracket the captured solve."""
+    import torch
+
+    from impec2d_gb300.workloads import device_view
+    cd, pd = [device_view(x, (N, N)) for x in ctx.state_ptrs()[:2]]
+    c_now, p_prev = cd.clone(), pd.clone()
+    out = {}
+    net = None
+    if not args.no_learned:
+        from impec2d_gb300 import learned as LW
+        net = E.Net(seed=args.seed)
+        X, T, t_gen = LW.generate_pairs(E, 20, 100, N=256, every=2, skip=2)
+        hist, t_train = LW.train(net, X, T, epochs=4, batch=64, lr=3e-4, weight_decay=1e-4)
+        out["learned_training"] = {"pairs": int(X.shape[0]), "grid": "256x256 heterogeneous realisations",
+                                   "epochs": 4, "steps": hist[-1][0], "final_batch_loss": hist[-1][1],
+                                   "generation_s": t_gen, "train_s": t_train}
+        del X, T
+        torch.cuda.empty_cache()
+    modes = [("fp64", "zero"), ("mixed", "zero"), ("fp64", "previous"), ("mixed", "previous")]
+    if net:
+        modes.append(("mixed", "learned"))
+    for prec, guess in modes:
+        Pp = workload_params(E, N, prec, args.nu)
+        Pp.warm_start = 0 if guess == "zero" else 1
+        cp = E.Context(Pp)
+        cp.upload(None, q, ghost=2)
+        if guess == "learned":
+            net.attach(cp, factor=max(1, N // 256), mode=1)
+        cc, pc = [device_view(x, (N, N)) for x in cp.state_ptrs()[:2]]
+
+        def reset():
+            cc.copy_(c_now)
+            pc.copy_(p_prev)
+        reset()
+        cp.pressure_solve_resident()  # capture and warm-up
+        ts, cyc = [], []
+        for _ in range(5):
+            reset()
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            cp.pressure_solve_resident(sync=False)
+            e1.record()
+            e1.synchronize()
+            c_, rr, rr0 = cp.last_solve()
+            cyc.append(c_)
+            ts.append(e0.elapsed_time(e1))
+        key = prec if guess == "zero" else f"{prec}_{guess}"
+        out[key] = {"ms_per_solve": statistics.median(ts), "cycles": statistics.median(cyc), "relres": rr,
+                    "initial_relres": rr0, "guess": guess}
+        if guess == "learned":
+            out[key]["alpha"] = E.Net.last_alpha(cp)
+            E.Net.detach(cp)
+        cp.close()
+    if net:
+        net.close()
+    if "mixed_learned" in out:
+        out["mixed_learned_vs_fp64_speedup"] = out["fp64"]["ms_per_solve"] / out["mixed_learned"]["ms_per_solve"]
+    return out
 
 
 def run_reference(args):
@@ -203,9 +286,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": cps, "unit": "cell-steps/s", "n_gpus": args.gpus,
             "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * secs / done,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"parallel quarter-five-spot {n}x{n}, MUSCL + CN Peaceman (alpha_l 1e-3, "
-                                   f"alpha_t 1e-4, Dm 1e-6), MG V(2,2) to 1e-10", "precision": "fp64",
-                       "parallelism": "host cores (OpenMP)"},
+            "config": bench_config(n), "solver": {"schedule": "oracle multigrid V-cycles (stationary)",
+                                                   "threads": cores},
             "cpu_baseline": {"value": cps, "unit": "cell-steps/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": cps, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -653,48 +735,50 @@ def main():
         e2e = {"value": whole_job_rate(N * N * args.steps, te, world), "unit": "cell-steps/s",
                "h2d_bytes_per_step": N * N * 8, "d2h_bytes_per_step": 2 * N * N * 8}
 
-    # ms per pressure solve to 1e-10 on the current state: plain FP64 MG vs mixed precision
-    pressure = {}
-    hc = np.zeros((N + 2 * g, N + 2 * g))
-    ctx.download(hc, None, None, ghost=g)
-    for prec in ("fp64", "mixed"):
-        Pp = workload_params(E, N, prec, args.nu)
-        cp = E.Context(Pp)
-        cp.upload(hc, q, ghost=g)
-        cyc, rr = cp.pressure_solve_resident()  # capture + warm-up
-        ts = []
-        for _ in range(5):
+    # a later window of the same run: the fingers have formed and the solves are harder
+    later = None
+    if args.later_after > 0:
+        done = args.warmup + args.steps + 1
+        if done < args.later_after:
+            ctx.run_steps(args.later_after - done)
+        barrier()
+        lt = []
+        for _ in range(args.steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            cp.pressure_solve_resident(sync=False)
+            ctx.run_steps(1)
             e1.record()
-            ts.append((e0, e1))
-        torch.cuda.synchronize()
-        cyc, rr = cp.pressure_solve_resident()
-        pressure[prec] = {"ms_per_solve": statistics.median(a.elapsed_time(b) for a, b in ts), "cycles": cyc,
-                          "relres": rr}
-        cp.close()
+            lt.append((e0, e1))
+        barrier()
+        lms = max_over_ranks(sum(a.elapsed_time(b) for a, b in lt), device="cuda") / args.steps
+        linfo = ctx.step()
+        later = {"after_step": max(done, args.later_after), "t": linfo.t, "steps": args.steps, "ms_per_step": lms,
+                 "value": whole_job_rate(N * N * args.steps, lms * args.steps * 1e-3, world),
+                 "mg_cycles": linfo.its, "cn_sweeps": linfo.para_its}
+
+    pressure = pressure_solves(E, ctx, N, q, args, flush)
 
     roof = E.roofline_probe(ctx, P, args.precision)
     sched = f"V({ctx.get_tuning('mg_pre')},{ctx.get_tuning('mg_post')})"
     line = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"parallel quarter-five-spot {N}x{N}, MUSCL + CN Peaceman (alpha_l 1e-3, alpha_t 1e-4,"
-                                   f" Dm 1e-6), MG {sched} to 1e-10"
-                                   + (f", nu = {args.nu:.4g} (weighted nine-point)" if args.nu != 1.0 else ""),
-                       "precision": args.precision, "l2": "flushed (256 MB write) between timed steps",
-                       "parallelism": f"replicas x{world}"},
-            "solver": {"mg_cycles": info.its, "relres": info.relres, "cn_sweeps": info.para_its, "dt": info.dt,
-                       "wall_s": t_wall},
+            "config": bench_config(N, args.precision, args.nu),
+            "solver": {"schedule": f"{sched}-preconditioned CG", "mg_cycles": info.its, "relres": info.relres,
+                       "cn_sweeps": info.para_its, "dt": info.dt, "wall_s": t_wall, "replicas": world},
             "pressure_solve_1e-10": pressure, "gpu_launches": int(launches), "clocks": clk, "roofline": roof}
     if e2e:
         line["e2e"] = e2e
+    if later:
+        line["later_window"] = later
     if rank == 0 and not args.no_cpu_baseline:
         cps, cores, secs, _ = cpu_baseline(N, 3)
         line["cpu_baseline"] = {"value": cps, "unit": "cell-steps/s", "cores": cores, "kind": "port",
                                 "sample": f"3 IMPES steps at {N}^2 from t=0, oracle FP64 C++ with OpenMP ({secs:.1f} s)"}
+        cps1, _, secs1, done1 = cpu_baseline(N, 1, threads=1)
+        line["cpu_baseline"]["one_thread"] = {"value": cps1, "unit": "cell-steps/s", "cores": 1,
+                                              "sample": f"{done1} IMPES step at {N}^2 from t=0 ({secs1:.1f} s)"}
     if rank == 0:
         print(json.dumps(line))
     ctx.close()

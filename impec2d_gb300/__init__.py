@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(HERE, "libimpec2d.so")
 MEANCONC, HARMONIC = 0, 1
 EXPLICIT, CRANKNICOLSON = 0, 1
 ALTERNATING, X_FIRST, Y_FIRST, STRANG, SYMMETRIC_PARALLEL = 0, 1, 2, 3, 4
-UPWINDSPLIT, MUSCL = 0, 4
+UPWINDSPLIT, WAFSPLIT, WAF, CTU, MUSCL = 0, 1, 2, 3, 4
 PARALLEL, DIAGONAL, HORIZONTAL = 0, 1, 2
 BC_NEUMANN, BC_PERIODIC = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
@@ -103,6 +103,7 @@ _SIGS = {
     "impec_advect_symmetric_noalloc": (C.c_int, [C.POINTER(Params), _VP, _VP, _VP, C.c_double, _VP]),
     "impec_time_kernel": (C.c_int, [_VP, C.c_int, C.c_int, _PD, _PD]),
     "impec_measure_fp64": (C.c_int, [_PD]),
+    "impec_selftest_bounded_wait": (C.c_int, [C.c_uint, C.c_int, _PI]),
     "impec_set_tuning": (C.c_int, [_VP, C.c_char_p, C.c_long]),
     "impec_get_tuning": (C.c_int, [_VP, C.c_char_p, C.POINTER(C.c_long)]),
     "impec_autotune": (C.c_int, [_VP, C.c_int, C.c_char_p, C.c_int]),

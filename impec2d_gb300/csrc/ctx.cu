@@ -135,8 +135,8 @@ static impec_status validate(const impec_params* P) {
     if (!(P->nu >= 0.0 && P->nu <= 1.0)) { set_error("nu must lie in [0,1] (EllipticSolver::SetNu)"); return IMPEC_ERR_ARG; }
     if (!(P->porosity > 0)) { set_error("porosity must be > 0"); return IMPEC_ERR_ARG; }
     if (!(P->mu_res > 0) || !(P->mu_inj > 0)) { set_error("viscosities must be > 0"); return IMPEC_ERR_ARG; }
-    if (P->hmtype != IMPEC_MUSCL && P->hmtype != IMPEC_UPWINDSPLIT) {
-        set_error("hyper_method: only muscl and upwind_split have implementations (src/SimParams.h:15)");
+    if (P->hmtype < IMPEC_UPWINDSPLIT || P->hmtype > IMPEC_MUSCL) {
+        set_error("unknown hyper_method (src/SimParams.h:15)");
         return IMPEC_ERR_ARG;
     }
     if (P->dim_splitting < 0 || P->dim_splitting > 4) { set_error("unknown dimensional_splitting"); return IMPEC_ERR_ARG; }

@@ -242,6 +242,7 @@ static impec_status step_stream(impec_ctx* ctx, double t_clip) {
     double rr = 0;
     impec_status st = pressure_solve(ctx, ctx->c, ctx->p, ctx->P.eps, &cyc, &rr);
     if (st != IMPEC_OK && st != IMPEC_ERR_NOT_CONVERGED) return st;
+    if (st == IMPEC_ERR_NOT_CONVERGED) ctx->host_flags |= FLAG_MG_NOT_CONVERGED;
     IMPEC_TRY(velocity(ctx, ctx->p, ctx->c, ctx->u, ctx->v));
     IMPEC_TRY(max_stable_dt_dev(ctx, ctx->u, ctx->v));
     IMPEC_CUDA_TRY(cudaMemcpyAsync(&S->t_clip, &t_clip, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));

@@ -394,7 +394,11 @@ impec_params SimParams::engine() const {
     P.ptype = ptype == CRANKNICOLSON ? IMPEC_CRANKNICOLSON : IMPEC_EXPLICIT;
     P.dt_diff_limit = dt_diff_limit;
     P.dim_splitting = (int)dim_splitting;
-    P.hmtype = hmtype == UPWINDSPLIT ? IMPEC_UPWINDSPLIT : IMPEC_MUSCL;
+    P.hmtype = hmtype == UPWINDSPLIT ? IMPEC_UPWINDSPLIT
+               : hmtype == WAFSPLIT  ? IMPEC_WAFSPLIT
+               : hmtype == WAF       ? IMPEC_WAF
+               : hmtype == CTU       ? IMPEC_CTU
+                                     : IMPEC_MUSCL;
     P.stype = stype == PARALLEL ? IMPEC_PARALLEL : (stype == DIAGONAL ? IMPEC_DIAGONAL : IMPEC_HORIZONTAL);
     P.is_test = is_test; P.testno = testno;
     P.bc = is_test ? IMPEC_BC_PERIODIC : IMPEC_BC_NEUMANN;

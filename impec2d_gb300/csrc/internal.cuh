@@ -185,6 +185,9 @@ struct impec_ctx {
     // run state
     double t = 0, t0 = 0, total_outflux = 0;
     int counter_steps = 0, prev_first_sweep = 1, last_its = 0, last_para_its = 0;
+    // FLAG_* bits of the current step that the kernel-by-kernel path learned on the host (its
+    // later solves reset the device flags), merged into the step's report
+    int host_flags = 0;
     double last_relres = 0;
     bool have_source = false;
     long long nlaunch = 0;                         // kernel launches issued (captured ones included)

@@ -1276,3 +1276,37 @@ extern "C" impec_status impec_gemm_bf16(const void* A, int lda, const void* B, i
     }
     return IMPEC_OK;
 }
+
+// ---------------------------------------------------------------- bounded-wait self-test
+// One thread initialises an mbarrier that expects one arrival.  With arrive != 0 it arrives
+// first, so the wait completes; otherwise nothing ever arrives and the wait gives up after
+// max_tries polls, exactly as the tensor-core kernels' waits do when a copy never lands.  The
+// outcome goes to *timed_out (1: gave up, 0: completed); the kernel always returns.
+__global__ void k_selftest_bounded_wait(uint32_t max_tries, int arrive, int* __restrict__ timed_out) {
+    __shared__ __align__(8) uint64_t mbar;
+    if (threadIdx.x != 0) return;
+    umma::mbar_init(&mbar, 1);
+    if (arrive) umma::mbar_arrive(&mbar);
+    *timed_out = umma::mbar_wait(&mbar, 0u, max_tries) ? 0 : 1;
+}
+
+extern "C" impec_status impec_selftest_bounded_wait(unsigned max_tries, int arrive, int* timed_out) {
+    if (!timed_out || max_tries == 0 || max_tries > (1u << 20)) {
+        set_error("impec_selftest_bounded_wait: max_tries must be in [1, 1048576]");
+        return IMPEC_ERR_ARG;
+    }
+    int* flag = device_error_flag();
+    if (!flag) return IMPEC_ERR_CUDA;
+    IMPEC_CUDA_TRY(cudaMemset(flag, 0xff, sizeof(int)));
+    k_selftest_bounded_wait<<<1, 32>>>((uint32_t)max_tries, arrive, flag);
+    IMPEC_LAUNCH_CHECK();
+    int h = -1;
+    IMPEC_CUDA_TRY(cudaMemcpy(&h, flag, sizeof(int), cudaMemcpyDeviceToHost));
+    IMPEC_CUDA_TRY(cudaMemset(flag, 0, sizeof(int)));
+    if (h != 0 && h != 1) {
+        set_error("impec_selftest_bounded_wait: the kernel did not report");
+        return IMPEC_ERR_CUDA;
+    }
+    *timed_out = h;
+    return IMPEC_OK;
+}

@@ -93,6 +93,7 @@ static double mass_error(const impec_ctx* ctx, double mass, double t) {
 
 // One resident IMPES step through the step graph; with info, waits and reports.
 static impec_status one_step(impec_ctx* ctx, double t_clip, impec_step_info* info) {
+    ctx->host_flags = 0;
     IMPEC_TRY(launch_step_graph(ctx, t_clip));
     ctx->counter_steps++;
     if (!info) return IMPEC_OK;
@@ -112,7 +113,8 @@ static impec_status one_step(impec_ctx* ctx, double t_clip, impec_step_info* inf
     info->para_its = H.cn_cycles_total;
     info->prev_first_sweep = ctx->prev_first_sweep;
     info->clipped = H.clipped;
-    const int flags = H.flags;
+    const int flags = H.flags | ctx->host_flags;
+    ctx->host_flags = 0;
     IMPEC_TRY(diagnostics_dev(ctx, ctx->c, ctx->u, ctx->v));
     IMPEC_TRY(sync_scalars(ctx));
     info->mass_err = mass_error(ctx, ctx->hscal->red[0], ctx->t);

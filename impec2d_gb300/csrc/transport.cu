@@ -79,6 +79,25 @@ __device__ __forceinline__ void hancock(double cm, double c0, double cp, double 
     sr = UR + df;
 }
 
+// WAF intercell flux (times phi) for the split sweeps (hyper_method "waf_split" / "waf"; the
+// reference parses these, src/SimParams.cpp:200-208, but ships no source for them).  Toro's
+// weighted average flux with the van Leer limiter (Riemann Solvers and Numerical Methods for
+// Fluid Dynamics, 3rd ed., ch. 13-14): cr = u dt / (dx phi) = u lam is the Courant number,
+// A = 1 - (1 - |cr|) * 2r / (1 + r) for r > 0 (else 1, the upwind flux), r = upwind jump /
+// local jump, and F = u ((1 + s A) cL + (1 - s A) cR) / 2 with s = sign(cr).
+__device__ __forceinline__ double waf_face(double u, double lam, double cLL, double cL, double cR, double cRR) {
+    const double cr = u * lam;
+    const double dloc = cR - cL;
+    double A = 1.0;
+    if (dloc != 0.0) {
+        const double dupw = cr >= 0.0 ? cL - cLL : cRR - cR;
+        const double r = dupw / dloc;
+        if (r > 0.0) A = 1.0 - (1.0 - fabs(cr)) * (2.0 * r / (1.0 + r));
+    }
+    const double s = cr > 0.0 ? 1.0 : (cr < 0.0 ? -1.0 : 0.0);
+    return 0.5 * (1.0 + s * A) * (u * cL) + 0.5 * (1.0 - s * A) * (u * cR);
+}
+
 // Reflected (or wrapped) cell index, clamped into [0, n): tile loads may reach further than
 // two cells past the boundary on small grids; those values never reach an in-domain output.
 template <int BC>
@@ -120,6 +139,12 @@ __device__ __forceinline__ double sweep_cell(const double* __restrict__ c, const
         double cm = C(k - 1), c0 = C(k), cp = C(k + 1);
         Fw = uw * (pos(uw) ? cm : c0);
         Fe = ue * (pos(ue) ? c0 : cp);
+        return c0 + lam * (Fw - Fe);
+    }
+    if (SCHEME == IMPEC_WAFSPLIT) {
+        double cmm = C(k - 2), cm = C(k - 1), c0 = C(k), cp = C(k + 1), cpp = C(k + 2);
+        Fw = waf_face(uw, lam, cmm, cm, c0, cp);
+        Fe = waf_face(ue, lam, cm, c0, cp, cpp);
         return c0 + lam * (Fw - Fe);
     }
     double cmm = C(k - 2), cm = C(k - 1), c0 = C(k), cp = C(k + 1), cpp = C(k + 2);
@@ -288,6 +313,53 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_advect_symmetric(int n1, int 
     }
 }
 
+// ---------------------------------------------------------------- corner transport upwind
+// hyper_method "ctu" (parsed by the reference, src/SimParams.cpp:200-208, no source shipped):
+// Colella's unsplit second-order CTU (J. Comput. Phys. 87 (1990) 171-200) on face velocities.
+// Each face takes its upwind cell's value extrapolated to the face and the half time level --
+// the central slope (unlimited, the recorded order is "2nd order"), the normal Courant
+// correction, and half the transverse upwind advection of that cell -- and the interior is
+// updated conservatively in one pass.  lx = dt/(dx phi), ly = dt/(dy phi) per unit velocity.
+template <int BC>
+__global__ void k_ctu(int n1, int n2, const double* __restrict__ cin, double* __restrict__ cout,
+                      const double* __restrict__ u, const double* __restrict__ v, const double* __restrict__ dt_dev,
+                      double inv_dx_phi, double inv_dy_phi) {
+    pdl_enter();
+    const int j = blockIdx.x * TBX + threadIdx.x, i = blockIdx.y * TBY + threadIdx.y;
+    if (i >= n1 || j >= n2) return;
+    const double dt = dt_dev[0], lx = dt * inv_dx_phi, ly = dt * inv_dy_phi;
+    auto C = [&](int a, int b) { return cin[IX(cell_at<BC>(a, n1), cell_at<BC>(b, n2), n2)]; };
+    // x-face f of row b (normal: odd reflection across x walls; row b: even reflection)
+    auto U = [&](int f, int b) { return face_at<BC>(u, f, n1, n2, cell_at<BC>(b, n2)); };
+    // y-face f of row a
+    auto V = [&](int a, int f) { return face_at<BC>(v + IX(cell_at<BC>(a, n1), 0, n2 + 1), f, n2, 1, 0); };
+    auto ty = [&](int a, int b) {  // cell-centred v times its upwind y difference, cell (a, b)
+        const double bc = 0.5 * (V(a, b) + V(a, b + 1));
+        return bc * (bc >= 0.0 ? C(a, b) - C(a, b - 1) : C(a, b + 1) - C(a, b));
+    };
+    auto tx = [&](int a, int b) {
+        const double ac = 0.5 * (U(a, b) + U(a + 1, b));
+        return ac * (ac >= 0.0 ? C(a, b) - C(a - 1, b) : C(a + 1, b) - C(a, b));
+    };
+    auto Fx = [&](int f) {  // x-face f of row j
+        const double vel = U(f, j);
+        const int m = vel >= 0.0 ? f - 1 : f;
+        const double sx = 0.5 * (C(m + 1, j) - C(m - 1, j));
+        const double st = vel >= 0.0 ? C(m, j) + 0.5 * (1.0 - vel * lx) * sx - 0.5 * ly * ty(m, j)
+                                     : C(m, j) - 0.5 * (1.0 + vel * lx) * sx - 0.5 * ly * ty(m, j);
+        return vel * st;
+    };
+    auto Fy = [&](int f) {  // y-face f of row i
+        const double vel = V(i, f);
+        const int m = vel >= 0.0 ? f - 1 : f;
+        const double sy = 0.5 * (C(i, m + 1) - C(i, m - 1));
+        const double st = vel >= 0.0 ? C(i, m) + 0.5 * (1.0 - vel * ly) * sy - 0.5 * lx * tx(i, m)
+                                     : C(i, m) - 0.5 * (1.0 + vel * ly) * sy - 0.5 * lx * tx(i, m);
+        return vel * st;
+    };
+    cout[IX(i, j, n2)] = C(i, j) + lx * (Fx(i) - Fx(i + 1)) + ly * (Fy(j) - Fy(j + 1));
+}
+
 static dim3 tgrid(int n1, int n2) { return dim3((n2 + TBX - 1) / TBX, (n1 + TBY - 1) / TBY); }
 
 impec_status advect_x_dev(impec_ctx* ctx, const double* cin, double* cout, const double* u, double dt_scale,
@@ -300,6 +372,9 @@ impec_status advect_x_dev(impec_ctx* ctx, const double* cin, double* cout, const
     if (P.hmtype == IMPEC_MUSCL) {
         if (per) launch_k(ctx->stream, k_sweep_x<IMPEC_MUSCL, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
         else launch_k(ctx->stream, k_sweep_x<IMPEC_MUSCL, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
+    } else if (P.hmtype == IMPEC_WAFSPLIT || P.hmtype == IMPEC_WAF) {
+        if (per) launch_k(ctx->stream, k_sweep_x<IMPEC_WAFSPLIT, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
+        else launch_k(ctx->stream, k_sweep_x<IMPEC_WAFSPLIT, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
     } else {
         if (per) launch_k(ctx->stream, k_sweep_x<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
         else launch_k(ctx->stream, k_sweep_x<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cghost, cout, u, dt_dev, dt_scale, f);
@@ -318,6 +393,9 @@ impec_status advect_y_dev(impec_ctx* ctx, const double* cin, double* cout, const
     if (P.hmtype == IMPEC_MUSCL) {
         if (per) launch_k(ctx->stream, k_sweep_y<IMPEC_MUSCL, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
         else launch_k(ctx->stream, k_sweep_y<IMPEC_MUSCL, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
+    } else if (P.hmtype == IMPEC_WAFSPLIT || P.hmtype == IMPEC_WAF) {
+        if (per) launch_k(ctx->stream, k_sweep_y<IMPEC_WAFSPLIT, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
+        else launch_k(ctx->stream, k_sweep_y<IMPEC_WAFSPLIT, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
     } else {
         if (per) launch_k(ctx->stream, k_sweep_y<IMPEC_UPWINDSPLIT, IMPEC_BC_PERIODIC>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
         else launch_k(ctx->stream, k_sweep_y<IMPEC_UPWINDSPLIT, IMPEC_BC_NEUMANN>, g, b, 0, P.N1, P.N2, cin, cout, v, dt_dev, dt_scale, f);
@@ -339,6 +417,27 @@ impec_status advect_split_dev(impec_ctx* ctx, double* c, const double* u, const 
     const impec_params& P = ctx->P;
     const size_t bytes = (size_t)P.N1 * P.N2 * 8;
     double *t1 = ctx->t1, *t2 = ctx->t2, *t3 = ctx->t3;
+    if (P.hmtype == IMPEC_CTU) {  // unsplit: one CTU update, c -> t1, then back into c
+        const double fx = 1.0 / (ctx->G.dx * P.porosity), fy = 1.0 / (ctx->G.dy * P.porosity);
+        ++ctx->nlaunch;
+        if (P.bc == IMPEC_BC_PERIODIC) launch_k(ctx->stream, k_ctu<IMPEC_BC_PERIODIC>, tgrid(P.N1, P.N2), dim3(TBX, TBY), 0, P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+        else launch_k(ctx->stream, k_ctu<IMPEC_BC_NEUMANN>, tgrid(P.N1, P.N2), dim3(TBX, TBY), 0, P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
+        IMPEC_LAUNCH_CHECK();
+        IMPEC_CUDA_TRY(cudaMemcpyAsync(c, t1, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        *pfs = 0;
+        return IMPEC_OK;
+    }
+    if (P.dim_splitting == IMPEC_SYMMETRIC_PARALLEL && (P.hmtype == IMPEC_WAFSPLIT || P.hmtype == IMPEC_WAF)) {
+        // the average of XY and YX through the per-sweep kernels (the fused tile kernel has
+        // MUSCL and upwind states only): t2 = Y(X(c)), t1 = X(Y(c)), c = (t2 + t1) / 2
+        IMPEC_TRY(advect_x_dev(ctx, c, t1, u, 1.0, dt_dev));
+        IMPEC_TRY(advect_y_dev(ctx, t1, t2, v, 1.0, dt_dev));
+        IMPEC_TRY(advect_y_dev(ctx, c, t3, v, 1.0, dt_dev));
+        IMPEC_TRY(advect_x_dev(ctx, t3, t1, u, 1.0, dt_dev));
+        IMPEC_TRY(average_dev(ctx, c, t2, t1));
+        *pfs = 0;
+        return IMPEC_OK;
+    }
     switch (P.dim_splitting) {
         case IMPEC_ALTERNATING:
             if (*pfs == 1) {

@@ -40,7 +40,9 @@ enum { IMPEC_MEANCONC = 0, IMPEC_HARMONIC = 1 };
 enum { IMPEC_EXPLICIT = 0, IMPEC_CRANKNICOLSON = 1 };
 enum { IMPEC_ALTERNATING = 0, IMPEC_X_FIRST = 1, IMPEC_Y_FIRST = 2, IMPEC_STRANG = 3,
        IMPEC_SYMMETRIC_PARALLEL = 4 };
-enum { IMPEC_UPWINDSPLIT = 0, IMPEC_MUSCL = 4 };
+/* hyper_method: upwind_split, waf_split and waf (the WAF flux in the split sweeps), ctu
+ * (unsplit corner transport upwind), muscl. */
+enum { IMPEC_UPWINDSPLIT = 0, IMPEC_WAFSPLIT = 1, IMPEC_WAF = 2, IMPEC_CTU = 3, IMPEC_MUSCL = 4 };
 enum { IMPEC_PARALLEL = 0, IMPEC_DIAGONAL = 1, IMPEC_HORIZONTAL = 2 };
 enum { IMPEC_BC_NEUMANN = 0, IMPEC_BC_PERIODIC = 1 };
 /* Pressure-solver precision: plain FP64 multigrid, or FP32 V-cycles inside FP64
@@ -62,7 +64,7 @@ typedef struct {
     int ptype;                /* dt rule: IMPEC_CRANKNICOLSON ignores the diffusion limit */
     double dt_diff_limit;
     int dim_splitting;        /* IMPEC_SYMMETRIC_PARALLEL etc. */
-    int hmtype;               /* IMPEC_MUSCL | IMPEC_UPWINDSPLIT */
+    int hmtype;               /* IMPEC_MUSCL | IMPEC_UPWINDSPLIT | IMPEC_WAFSPLIT | IMPEC_WAF | IMPEC_CTU */
     int stype;                /* IMPEC_PARALLEL | IMPEC_DIAGONAL (sets the pinned cell) */
     int is_test, testno;      /* analytic permeability of the elliptic tests */
     int bc;                   /* IMPEC_BC_NEUMANN, or IMPEC_BC_PERIODIC (advection test) */
@@ -257,6 +259,15 @@ impec_status impec_learned_alpha(impec_ctx* ctx, double* alpha);
  * chains per thread on every SM): the denominator of the FP64-pipe fractions reported beside
  * the HBM roofline.  No counterpart in the reference. */
 impec_status impec_measure_fp64(double* fma_per_second);
+
+/* Self-test of the bounded waits that guard every tensor-core and TMA wait of the engine (no
+ * counterpart in the reference).  A one-thread kernel waits on an mbarrier with the same
+ * bounded poll loop: with arrive != 0 it arrives first and the wait completes (*timed_out = 0);
+ * with arrive == 0 nothing ever arrives, the wait gives up after max_tries polls
+ * (<= 1,048,576, a fraction of a millisecond) and *timed_out = 1.  Either way the kernel returns
+ * and the context stays usable: this is how a lost copy surfaces as an error status instead of
+ * a hung GPU. */
+impec_status impec_selftest_bounded_wait(unsigned max_tries, int arrive, int* timed_out);
 
 /* Allocation-free transport step.  No counterpart in the reference: it exists for callers
  * that may not allocate device memory themselves or through this library -- code running

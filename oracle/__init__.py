@@ -3,8 +3,8 @@
 The oracle (``oracle_core.cpp``, ``oracle_solve.cpp``) restates the reference
 Impec2D discretisation in plain FP64 C++.  Only ``tests/``, the smoke check and
 the CPU-baseline leg of ``bench.py`` may import this module; the product path
-never does.  See ``oracle.h`` for the parity status (pinned by the reference's
-known-answer convergence tests; unpinned at the HYPRE boundary).
+never does.  See ``oracle.h`` for the parity status: pinned bit for bit to the reference's
+own code compiled in ``oracle/_ref`` (``oracle/ref.py``), except HYPRE's iterates.
 
 Arrays use the reference's ghost-cell layouts (``src/Impec2DSolver.cpp:151-182``):
 scalar ``(N1+2g, N2+2g)``, velocity ``(N1+1+2g, N2+1+2g, 2)``, source ``N1*N2``.
@@ -23,7 +23,7 @@ _LIB = os.path.join(_HERE, "liboracle.so")
 MEANCONC, HARMONIC = 0, 1
 EXPLICIT, CRANKNICOLSON = 0, 1
 ALTERNATING, X_FIRST, Y_FIRST, STRANG, SYMMETRIC_PARALLEL = 0, 1, 2, 3, 4
-UPWINDSPLIT, MUSCL = 0, 4
+UPWINDSPLIT, WAFSPLIT, WAF, CTU, MUSCL = 0, 1, 2, 3, 4
 PARALLEL, DIAGONAL, HORIZONTAL = 0, 1, 2
 CIRCULAR, GAUSSIAN, ONECELL = 0, 1, 2
 
@@ -107,6 +107,7 @@ def _declare(L):
     d("or_advect_x", None, _PP, _D, _D, C.c_double)
     d("or_advect_y", None, _PP, _D, _D, C.c_double)
     d("or_advect_split", None, _PP, _D, _D, C.c_double, C.POINTER(C.c_int))
+    d("or_ctu_advect", None, _PP, _D, _D, C.c_double)
     d("or_peaceman_F", None, _PP, _D, C.c_int, C.c_int, _D, _D)
     d("or_peaceman_G", None, _PP, _D, C.c_int, C.c_int, _D, _D)
     d("or_cn_matrix", None, _PP, _D, C.c_double, _D)
@@ -127,6 +128,7 @@ def _declare(L):
     d("or_mg_solve", C.c_int, _PP, _D, _D, _D, C.c_double, C.c_int, C.POINTER(C.c_int), _D, C.c_int,
       C.c_int, C.c_double)
     d("or_num_threads", C.c_int)
+    d("or_set_num_threads", C.c_int, C.c_int)
 
 
 def ptr(a: np.ndarray | None):

@@ -6,14 +6,18 @@
  * CUDA implementation: only the tests, the smoke check and the CPU-baseline leg
  * of bench.py may load it.  The product never links or calls it.
  *
- * Parity status: the reference needs Blitz++, libconfig++, HYPRE 2.8.0b and MPI,
- * none of which are available, so it cannot be built or run here.  This oracle is
- * therefore pinned only by the reference's own known-answer tests (the advection
- * convergence order in examples/hyperbolic_test.cfg:129-139 and the manufactured
- * elliptic solutions of src/EllipticSolver.cpp:155-470) and by the runtime
- * invariants the reference prints (src/Impec2DSolver.cpp:530-588).  Parity at the
- * HYPRE boundary is unpinned: only the discrete system A x = b is reference code;
- * the oracle solves that system with its own solvers (banded LU, multigrid).
+ * Parity status: PINNED to the reference itself.  The reference's own sources compile
+ * unchanged against the stand-ins in oracle/refshim (a Blitz++ subset, libconfig++, one-rank
+ * MPI, and HYPRE reduced to a recorded system with a direct solve) into oracle/_ref
+ * (recipe oracle/Makefile.ref, entry points oracle/ref_driver.cpp).  Every operation of this
+ * oracle that is reference code -- assembly with its Neumann folds and Dirichlet rows, face
+ * and corner mobilities, velocities, the CFL step, TR, MUSCL and upwind fluxes, the five
+ * split modes, Peaceman tensors, the Crank-Nicolson matrix and right-hand side, sources,
+ * ghost fills and diagnostics -- equals the reference's output bit for bit
+ * (tests/test_ref_pin.py; fixtures the reference wrote, tests/golden/ref_*, checked in
+ * tests/test_oracle_golden.py).  At the HYPRE boundary only the discrete system A x = b is
+ * reference code; HYPRE's iterates are not (its sources are not part of the reference), so
+ * solves are compared by residual under the reference's own assembled system.
  *
  * Array layouts follow the reference's Blitz arrays (src/Impec2DSolver.cpp:151-182):
  *   scalar fields c, p: (N1+2g) x (N2+2g), row-major, j fastest, ghost width g;
@@ -52,7 +56,7 @@ typedef struct {
     int ptype;                     /* OR_EXPLICIT | OR_CRANKNICOLSON (dt rule only) */
     double dt_diff_limit;
     int dim_splitting;
-    int hmtype;                    /* OR_MUSCL | OR_UPWINDSPLIT */
+    int hmtype;                    /* OR_MUSCL | OR_UPWINDSPLIT | OR_WAFSPLIT | OR_WAF | OR_CTU */
     int stype;                     /* OR_PARALLEL | OR_DIAGONAL | OR_HORIZONTAL */
     int is_test, testno;
     double eps, para_eps;
@@ -96,7 +100,11 @@ void or_flux_F(const or_params* P, double* F, const double* c, const double* v, 
 void or_flux_G(const or_params* P, double* G, const double* c, const double* v, double dt);
 void or_advect_x(const or_params* P, double* c, const double* v, double dt);
 void or_advect_y(const or_params* P, double* c, const double* v, double dt);
-/* prev_first_sweep: 0 = X_SWEEP, 1 = Y_SWEEP (state of the ALTERNATING mode). */
+/* hyper_method "ctu": Colella's unsplit corner transport upwind update of the interior
+ * (ghosts of c and v filled). */
+void or_ctu_advect(const or_params* P, double* c, const double* v, double dt);
+/* prev_first_sweep: 0 = X_SWEEP, 1 = Y_SWEEP (state of the ALTERNATING mode).  hmtype OR_CTU
+ * advects unsplit (or_ctu_advect); OR_WAFSPLIT and OR_WAF use the WAF flux in the sweeps. */
 void or_advect_split(const or_params* P, double* c, const double* v, double dt, int* prev_first_sweep);
 void or_peaceman_F(const or_params* P, const double* v, int i, int j, double* d11, double* d12);
 void or_peaceman_G(const or_params* P, const double* v, int i, int j, double* d22, double* d21);
@@ -142,6 +150,7 @@ int or_mg_solve(const or_params* P, const double* A9_neumann, const double* b, d
                 double tol, int max_cycles, int* cycles, double* relres, int pin_i, int pin_j,
                 double pin_value);
 int or_num_threads(void);
+int or_set_num_threads(int n);
 
 #ifdef __cplusplus
 }

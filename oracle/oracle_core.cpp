@@ -636,6 +636,29 @@ inline double upwind(const or_params* P, double speed, double UL, double UR) {  
     return (speed > 0) ? flux(P, speed, UL) : flux(P, speed, UR);
 }
 
+// WAF intercell flux for the linear flux f = vel c / phi (hyper_method "waf_split" / "waf";
+// parsed by the reference, src/SimParams.cpp:200-208, which ships no source for it).  Toro's
+// weighted average flux, Riemann Solvers and Numerical Methods for Fluid Dynamics (3rd ed.),
+// ch. 13-14: F = (1 + s A)/2 f(cL) + (1 - s A)/2 f(cR), s = sign of the Courant number
+// cr = vel dt / (phi dx), A = 1 - (1 - |cr|) psi(r) with the van Leer limiter
+// psi(r) = 2r / (1 + r) for r > 0, else 0 (the limiter the recorded WAF order names,
+// examples/hyperbolic_test.cfg:136), r = upwind jump / local jump.  psi = 1 gives Lax-Wendroff,
+// psi = 0 the upwind (Godunov) flux.
+inline double waf_flux(const or_params* P, double vel, double dtdx, double cLL, double cL, double cR, double cRR) {
+    const double cr = vel / P->porosity * dtdx;
+    const double dloc = cR - cL;
+    double A = 1.0;
+    if (dloc != 0.0) {
+        const double dupw = cr >= 0 ? cL - cLL : cRR - cR;
+        const double r = dupw / dloc;
+        if (r > 0) A = 1.0 - (1.0 - std::fabs(cr)) * (2.0 * r / (1.0 + r));
+    }
+    const double s = cr > 0 ? 1.0 : (cr < 0 ? -1.0 : 0.0);
+    return 0.5 * (1.0 + s * A) * flux(P, vel, cL) + 0.5 * (1.0 - s * A) * flux(P, vel, cR);
+}
+
+inline bool is_waf(const or_params* P) { return P->hmtype == OR_WAFSPLIT || P->hmtype == OR_WAF; }
+
 }  // namespace
 
 extern "C" {
@@ -650,6 +673,12 @@ void or_flux_F(const or_params* P, double* Fflat, const double* cflat, const dou
     if (P->hmtype == OR_UPWINDSPLIT) {  // src/UpwindSplitSolver.cpp:43-51
         for (int i = 0; i <= N1; i++)
             for (int j = -g; j < N2 + g; j++) F(i, j) = upwind(P, v(i, j, 0), c(i - 1, j), c(i, j));
+        return;
+    }
+    if (is_waf(P)) {
+        for (int i = 0; i <= N1; i++)
+            for (int j = -g; j < N2 + g; j++)
+                F(i, j) = waf_flux(P, v(i, j, 0), dt / G.dx, c(i - 2, j), c(i - 1, j), c(i, j), c(i + 1, j));
         return;
     }
     // src/MUSCLSplitSolver.cpp:102-141; U_Lin base (-1,-g,0), extent (N1+3)
@@ -678,6 +707,12 @@ void or_flux_G(const or_params* P, double* Gflat, const double* cflat, const dou
     if (P->hmtype == OR_UPWINDSPLIT) {  // src/UpwindSplitSolver.cpp:53-61
         for (int i = -g; i < N1 + g; i++)
             for (int j = 0; j <= N2; j++) Gf(i, j) = upwind(P, v(i, j, 1), c(i, j - 1), c(i, j));
+        return;
+    }
+    if (is_waf(P)) {
+        for (int i = -g; i < N1 + g; i++)
+            for (int j = 0; j <= N2; j++)
+                Gf(i, j) = waf_flux(P, v(i, j, 1), dt / Ge.dy, c(i, j - 2), c(i, j - 1), c(i, j), c(i, j + 1));
         return;
     }
     // src/MUSCLSplitSolver.cpp:152-189; U_Lin base (-g,-1,0), extent (N2+3)
@@ -730,9 +765,73 @@ static void fill_boundaries(const or_params* P, double* c) {  // HyperbolicSolve
         or_fill_scalar_neumann(P, c);
 }
 
-// AdvectSplit (src/HyperbolicSplitSolver.cpp:51-106)
+// Corner transport upwind (hyper_method "ctu"; parsed by the reference, src/SimParams.cpp:
+// 200-208, which ships no source for it): Colella's unsplit second-order scheme, J. Comput.
+// Phys. 87 (1990) 171-200, for c_t + div(V c) / phi = 0 with face velocities.  Each face takes
+// the state of its upwind cell m extrapolated to the face and the half time level,
+//   c(m) +- (1 -+ a dt/dx) sx(m) / 2 - dt/(2 dy) b(m) dyc(m),
+// with a the face speed, sx(m) the central slope (c(m+1) - c(m-1)) / 2 (unlimited: the
+// recorded CTU order is labelled "2nd order", examples/hyperbolic_test.cfg:137), b(m) the
+// cell-centred transverse speed and dyc(m) its upwind difference; then the conservative
+// unsplit update of the interior.  Speeds are velocity / phi; CFL <= 1 per direction.
+void or_ctu_advect(const or_params* P, double* cflat, const double* vflat, double dt) {
+    Geo G(P);
+    S2 c = sview(P, cflat);
+    V3 v = vview(P, vflat);
+    const int g = P->g, N1 = P->N1, N2 = P->N2;
+    const double lx = dt / G.dx, ly = dt / G.dy, phi = P->porosity;
+    auto bcen = [&](int i, int j) { return 0.5 * (v(i, j, 1) + v(i, j + 1, 1)) / phi; };
+    auto acen = [&](int i, int j) { return 0.5 * (v(i, j, 0) + v(i + 1, j, 0)) / phi; };
+    auto ty = [&](int i, int j) {  // b dc/dy, upwind difference, at cell (i, j)
+        const double b = bcen(i, j);
+        return b * (b >= 0 ? c(i, j) - c(i, j - 1) : c(i, j + 1) - c(i, j));
+    };
+    auto tx = [&](int i, int j) {
+        const double a = acen(i, j);
+        return a * (a >= 0 ? c(i, j) - c(i - 1, j) : c(i + 1, j) - c(i, j));
+    };
+    auto Fx = [&](int i, int j) {  // x-face i (between cells i-1 and i)
+        const double vel = v(i, j, 0), a = vel / phi;
+        double st;
+        if (a >= 0) {
+            const int m = i - 1;
+            st = c(m, j) + 0.5 * (1.0 - a * lx) * (0.5 * (c(m + 1, j) - c(m - 1, j))) - 0.5 * ly * ty(m, j);
+        } else {
+            const int m = i;
+            st = c(m, j) - 0.5 * (1.0 + a * lx) * (0.5 * (c(m + 1, j) - c(m - 1, j))) - 0.5 * ly * ty(m, j);
+        }
+        return flux(P, vel, st);
+    };
+    auto Fy = [&](int i, int j) {  // y-face j (between cells j-1 and j)
+        const double vel = v(i, j, 1), b = vel / phi;
+        double st;
+        if (b >= 0) {
+            const int m = j - 1;
+            st = c(i, m) + 0.5 * (1.0 - b * ly) * (0.5 * (c(i, m + 1) - c(i, m - 1))) - 0.5 * lx * tx(i, m);
+        } else {
+            const int m = j;
+            st = c(i, m) - 0.5 * (1.0 + b * ly) * (0.5 * (c(i, m + 1) - c(i, m - 1))) - 0.5 * lx * tx(i, m);
+        }
+        return flux(P, vel, st);
+    };
+    std::vector<double> out((size_t)N1 * N2);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < N1; i++)
+        for (int j = 0; j < N2; j++)
+            out[(size_t)i * N2 + j] = c(i, j) + lx * (Fx(i, j) - Fx(i + 1, j)) + ly * (Fy(i, j) - Fy(i, j + 1));
+    for (int i = 0; i < N1; i++)
+        for (int j = 0; j < N2; j++) c(i, j) = out[(size_t)i * N2 + j];
+    (void)g;
+}
+
+// AdvectSplit (src/HyperbolicSplitSolver.cpp:51-106); hyper_method "ctu" advects unsplit.
 void or_advect_split(const or_params* P, double* c, const double* v, double dt, int* prev_first_sweep) {
     fill_boundaries(P, c);
+    if (P->hmtype == OR_CTU) {
+        or_ctu_advect(P, c, v, dt);
+        fill_boundaries(P, c);
+        return;
+    }
     const size_t n = (size_t)(P->N1 + 2 * P->g) * (P->N2 + 2 * P->g);
     switch (P->dim_splitting) {
         case OR_ALTERNATING:

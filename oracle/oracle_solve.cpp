@@ -237,6 +237,19 @@ int or_num_threads(void) {
 #endif
 }
 
+// Threads of the oracle's OpenMP loops from now on (the CPU baseline's 1-thread and all-core
+// runs in one process); returns the previous count.
+int or_set_num_threads(int n) {
+#ifdef _OPENMP
+    const int prev = omp_get_max_threads();
+    if (n > 0) omp_set_num_threads(n);
+    return prev;
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
 int or_solve_banded(const or_params* P, const double* A9, const double* b, double* x) {
     const int N1 = P->N1, N2 = P->N2, n = N1 * N2;
     Banded M;
