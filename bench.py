@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--later-after", type=int, default=1000,
                     help="time a second window of --steps steps after this many IMPES steps (0: skip)")
+    ap.add_argument("--no-large-roofline", action="store_true",
+                    help="skip the 4096^2 roofline probe of the fine-level sweep")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the in-run training of the warm-start network for the pressure-solve line")
     ap.add_argument("--no-graph", action="store_true",
@@ -759,7 +761,21 @@ def main():
 
     pressure = pressure_solves(E, ctx, N, q, args, flush)
 
-    roof = E.roofline_probe(ctx, P, args.precision)
+    roof = E.roofline_probe(ctx, P, args.precision, flush=flush)
+    # the same sweep where the hierarchy cannot stay in L2: 4096^2 (BASELINE's large grid)
+    roof_large = None
+    if not args.no_large_roofline and args.nu == 1.0:
+        NL = 4096
+        PL = workload_params(E, NL, args.precision, args.nu)
+        cl = E.Context(PL)
+        cL, qL = initial_state(NL)
+        cgL = np.zeros((NL + 2 * g, NL + 2 * g))
+        cgL[g:g + NL, g:g + NL] = cL
+        cl.upload(cgL, qL, ghost=g)
+        cl.pressure_solve_resident()  # builds the operator hierarchy of this state
+        roof_large = E.roofline_probe(cl, PL, args.precision, flush=flush)
+        cl.close()
+        del cgL
     sched = f"V({ctx.get_tuning('mg_pre')},{ctx.get_tuning('mg_post')})"
     line = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -768,6 +784,8 @@ def main():
             "solver": {"schedule": f"{sched}-preconditioned CG", "mg_cycles": info.its, "relres": info.relres,
                        "cn_sweeps": info.para_its, "dt": info.dt, "wall_s": t_wall, "replicas": world},
             "pressure_solve_1e-10": pressure, "gpu_launches": int(launches), "clocks": clk, "roofline": roof}
+    if roof_large:
+        line["roofline_4096"] = roof_large
     if e2e:
         line["e2e"] = e2e
     if later:

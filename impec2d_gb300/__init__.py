@@ -102,6 +102,7 @@ _SIGS = {
     "impec_pressure_solve_resident": (C.c_int, [_VP, C.c_int, _PI, _PD]),
     "impec_advect_symmetric_noalloc": (C.c_int, [C.POINTER(Params), _VP, _VP, _VP, C.c_double, _VP]),
     "impec_time_kernel": (C.c_int, [_VP, C.c_int, C.c_int, _PD, _PD]),
+    "impec_time_kernel_cold": (C.c_int, [_VP, C.c_int, C.c_int, _VP, C.c_size_t, _PD, _PD, _PD]),
     "impec_measure_fp64": (C.c_int, [_PD]),
     "impec_selftest_bounded_wait": (C.c_int, [C.c_uint, C.c_int, _PI]),
     "impec_set_tuning": (C.c_int, [_VP, C.c_char_p, C.c_long]),
@@ -154,22 +155,31 @@ def time_kernel(ctx, which: int, reps: int = 20):
     return ms.value, b.value
 
 
-# FP64 operations (FMA, MUL or ADD, one per lane) per cell of one launch of each probed kernel,
-# as the ncu instruction counts show them: the five-point sweep is 4 DFMA + 1 DMUL per cell and
-# colour; the nine-point sweep (nu < 1) 8 DFMA + 1 DMUL + 1 DADD.
-_FP64_OPS_PER_CELL = {0: 5.0, 2: 6.0}
-_NINE_POINT = {0: ("k_gs4_exp9<double> (fine four-colour GS sweep, nine-point, FP64)", 10.0),
-               1: ("k_gs4_exp9<float> (fine four-colour GS sweep, nine-point, FP32)", None)}
-
-
-def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None, traffic_path: str | None = None):
-    """Achieved bandwidth of the dominant kernel (CUDA events on its stream) against the
-    measured HBM copy bandwidth, and its FP64 operation rate against the measured DFMA rate
-    of the device.  ``traffic`` (DRAM bytes per launch) comes from the ncu capture recorded in
-    profiles/traffic.json when that file names the kernel."""
+def roofline_probe(ctx, P, precision: str, flush=None, peaks_path: str | None = None, traffic_path: str | None = None,
+                   reps: int = 20):
+    """Achieved bandwidth of the dominant kernel, the fine-level red-black sweep, against the
+    measured HBM copy bandwidth, and its FP64 operation rate against the measured DFMA rate.
+    Each repetition is timed cold: L2 is overwritten first (``flush``, a CUDA tensor larger
+    than L2), then CUDA events on the engine's stream bracket the sweep.  Algorithmic bytes
+    follow the five-point model: x read and written, b, and the two face planes (40 B per cell in
+    FP64).  ``traffic`` (DRAM bytes per sweep) comes from the ncu capture recorded in
+    profiles/traffic.json when that file names the kernel and grid."""
     import json
     which = 1 if precision == "mixed" else 0
-    ms, b = time_kernel(ctx, which)
+    if P.nu != 1.0:  # nine-point operator: four-colour sweeps, timed back to back
+        ms, b = time_kernel(ctx, which)
+        t = "double" if which == 0 else "float"
+        return {"bound": "hbm", "kernel": f"k_gs4_exp9<{t}> (fine four-colour GS sweep, nine-point)",
+                "grid": f"{P.N1}x{P.N2}", "achieved": b / (ms * 1e-3) / 1e9, "peak": 6800.0, "unit": "GB/s",
+                "frac": b / (ms * 1e-3) / 1e9 / 6800.0, "peak_source": "fallback", "bytes_per_launch": b,
+                "ms_per_launch": ms, "timing": "back-to-back launches", "traffic": None}
+    if flush is None:
+        import torch
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ms, ms_min, b = C.c_double(), C.c_double(), C.c_double()
+    _chk(lib().impec_time_kernel_cold(ctx.h, which, reps, C.c_void_p(flush.data_ptr()), flush.numel() * flush.element_size(),
+                                      C.byref(ms), C.byref(ms_min), C.byref(b)), "time_kernel_cold")
+    ms, ms_min, b = ms.value, ms_min.value, b.value
     peak, src = 6800.0, "fallback"
     path = peaks_path or os.path.join(os.path.dirname(HERE), "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -178,23 +188,26 @@ def roofline_probe(ctx, P, precision: str, peaks_path: str | None = None, traffi
         except Exception:  # noqa: BLE001
             pass
     ach = b / (ms * 1e-3) / 1e9
-    nine = P.nu != 1.0 and which in _NINE_POINT
-    name = _NINE_POINT[which][0] if nine else KERNELS[which]
-    out = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
-           "frac": ach / peak, "peak_source": src, "bytes_per_launch": b, "ms_per_launch": ms, "traffic": None}
+    tile = ctx.get_tuning("tile_cells")
+    one_launch = tile > 0 and P.N1 * P.N2 >= tile
+    t = "double" if which == 0 else "float"
+    name = (f"k_rb_tile<{t}> (fine red-black sweep, both colours in one launch)" if one_launch
+            else f"k_rb_face5<{t}> (fine red-black sweep, one launch per colour)")
+    out = {"bound": "hbm", "kernel": name, "grid": f"{P.N1}x{P.N2}", "achieved": ach, "peak": peak, "unit": "GB/s",
+           "frac": ach / peak, "peak_source": src, "bytes_per_launch": b, "bytes_model": "x r+w, b, tx, ty",
+           "ms_per_launch": ms, "ms_per_launch_min": ms_min, "timing": "cold (L2 overwritten before each sweep)",
+           "traffic": None}
     tpath = traffic_path or os.path.join(os.path.dirname(HERE), "profiles", "traffic.json")
     if os.path.exists(tpath):
         try:
-            t = json.load(open(tpath)).get(name.split(" ")[0])
-            if t:
-                out["traffic"] = float(t["dram_bytes_per_launch"])
-                out["traffic_source"] = t["source"]
+            rec = json.load(open(tpath)).get(f"{name.split(' ')[0]}@{P.N1}x{P.N2}")
+            if rec:
+                out["traffic"] = float(rec["dram_bytes_per_launch"])
+                out["traffic_source"] = rec["source"]
         except Exception:  # noqa: BLE001
             pass
-    per_cell = (_NINE_POINT[which][1] if nine else _FP64_OPS_PER_CELL.get(which))
-    if per_cell:
-        n = float(P.N1) * float(P.N2)
-        ops = per_cell * n
+    if which == 0:
+        ops = 5.0 * float(P.N1) * float(P.N2)  # 4 DFMA + 1 DMUL per cell (ncu instruction counts)
         fma = measure_fp64()
         out["fp64"] = {"achieved_ops_per_s": ops / (ms * 1e-3), "peak_ops_per_s": fma,
                        "frac": ops / (ms * 1e-3) / fma, "ops_per_launch": ops,

@@ -67,6 +67,9 @@ struct Level {
     // FP32 copies for the mixed-precision cycle
     float *tx32 = nullptr, *ty32 = nullptr, *a932 = nullptr, *idiag32 = nullptr, *diag32 = nullptr;
     float *x32 = nullptr, *b32 = nullptr;
+    // second iterate buffers of the one-launch red-black sweep (ping-pong; FACE5 levels)
+    double* xa = nullptr;
+    float* xa32 = nullptr;
 };
 
 enum { FLAG_MG_NOT_CONVERGED = 1, FLAG_MG_NAN = 2, FLAG_CN_NOT_CONVERGED = 4, FLAG_CN_NAN = 8 };
@@ -132,6 +135,10 @@ struct Tuning {
     long coarse_cells32 = 1024;    // the same, FP32
     long rb_skip = 1;  // five-point levels: no zero fill before pre-smoothing, red-only prolongation
     long rb_resid = 1;  // five-point levels: restriction sums the red residuals only (black ones are ~0)
+    // five-point levels of at least this many cells sweep both colours in one launch
+    // (k_rb_tile, ping-pong iterate): every coefficient is read once per sweep instead of once
+    // per colour, which pays where the level streams from HBM; 0 disables
+    long tile_cells = 1L << 22;
 };
 }  // namespace impec
 

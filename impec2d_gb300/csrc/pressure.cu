@@ -417,6 +417,77 @@ __global__ void k_rb_zero(int n1, int n2, const T* __restrict__ idiag, const T* 
     }
 }
 
+// One whole red-black sweep in one launch (levels whose arrays stream from HBM).  A CTA owns a
+// TILE_R x TILE_C tile.  Phase 1 updates the first colour F on the tile and a one-cell ring
+// around it (the ring's values equal what the neighbouring tiles compute: same inputs, same
+// arithmetic), from the other colour's old values in x_in; phase 2 updates the other colour
+// on the tile from the phase-1 values in shared memory.  Both colours of the tile go to x_out.
+// The other colour's old values of a tile's edge are read by its neighbours' phase 1, so the
+// sweep cannot write in place: x_in and x_out are two buffers (ping-pong).  Each coefficient
+// (b, 1/diag, tx, ty) is read once per sweep instead of once per colour, and x once, in whole
+// sectors.  Per-cell arithmetic and its order equal k_rb_face5's, so the result is the same bit
+// for bit.  ZERO: the sweep starts from x = 0 (as k_rb_zero), so phase 1 is x = b * idiag and
+// x_in is not read.
+constexpr int TILE_R = 32, TILE_C = 64, TILE_THREADS = 256;
+constexpr int TILE_W = TILE_C + 4;  // shared row width: columns j0-2 .. j0+TILE_C+1
+
+template <class T, bool ZERO>
+__global__ void __launch_bounds__(TILE_THREADS) k_rb_tile(int n1, int n2, const T* __restrict__ tx,
+                                                          const T* __restrict__ ty, const T* __restrict__ idiag,
+                                                          const T* __restrict__ b, const T* __restrict__ x_in,
+                                                          T* __restrict__ x_out, int first) {
+    pdl_enter();
+    __shared__ T sx[(TILE_R + 4) * TILE_W];  // rows i0-2 .. i0+TILE_R+1
+    const int i0 = blockIdx.y * TILE_R, j0 = blockIdx.x * TILE_C, t = threadIdx.x;
+    auto S = [&](int i, int j) -> T& { return sx[(i - i0 + 2) * TILE_W + (j - j0 + 2)]; };
+    if (!ZERO) {
+        for (int k = t; k < (TILE_R + 4) * TILE_W; k += TILE_THREADS) {
+            const int i = i0 - 2 + k / TILE_W, j = j0 - 2 + k % TILE_W;
+            sx[k] = (i >= 0 && i < n1 && j >= 0 && j < n2) ? x_in[IX(i, j, n2)] : T(0);
+        }
+        __syncthreads();
+    }
+    // phase 1: colour `first` on rows i0-1 .. i0+TILE_R, columns j0-1 .. j0+TILE_C
+    constexpr int H1 = (TILE_C + 2) / 2;
+    for (int k = t; k < (TILE_R + 2) * H1; k += TILE_THREADS) {
+        const int i = i0 - 1 + k / H1;
+        const int j = j0 - 1 + (((i + j0 - 1 + first) & 1)) + 2 * (k % H1);
+        if (i < 0 || i >= n1 || j < 0 || j >= n2) continue;
+        T v;
+        if (ZERO) {
+            v = b[IX(i, j, n2)] * idiag[IX(i, j, n2)];
+        } else {
+            T s = b[IX(i, j, n2)];
+            if (i > 0) s += tx[IX(i, j, n2)] * S(i - 1, j);
+            if (i < n1 - 1) s += tx[IX(i + 1, j, n2)] * S(i + 1, j);
+            if (j > 0) s += ty[IX(i, j, n2 + 1)] * S(i, j - 1);
+            if (j < n2 - 1) s += ty[IX(i, j + 1, n2 + 1)] * S(i, j + 1);
+            v = s * idiag[IX(i, j, n2)];
+        }
+        S(i, j) = v;  // phase 1 reads only the other colour: no conflict
+    }
+    __syncthreads();
+    // phase 2: the other colour on the tile, from the phase-1 values
+    constexpr int H2 = TILE_C / 2;
+    const int second = first ^ 1;
+    for (int k = t; k < TILE_R * H2; k += TILE_THREADS) {
+        const int i = i0 + k / H2;
+        const int j = j0 + ((i + j0 + second) & 1) + 2 * (k % H2);
+        if (i >= n1 || j >= n2) continue;
+        T s = b[IX(i, j, n2)];
+        if (i > 0) s += tx[IX(i, j, n2)] * S(i - 1, j);
+        if (i < n1 - 1) s += tx[IX(i + 1, j, n2)] * S(i + 1, j);
+        if (j > 0) s += ty[IX(i, j, n2 + 1)] * S(i, j - 1);
+        if (j < n2 - 1) s += ty[IX(i, j + 1, n2 + 1)] * S(i, j + 1);
+        S(i, j) = s * idiag[IX(i, j, n2)];  // phase 2 reads only colour `first`: no conflict
+    }
+    __syncthreads();
+    for (int k = t; k < TILE_R * TILE_C; k += TILE_THREADS) {
+        const int i = i0 + k / TILE_C, j = j0 + k % TILE_C;
+        if (i < n1 && j < n2) x_out[IX(i, j, n2)] = S(i, j);
+    }
+}
+
 template <class T>
 __global__ void k_gs4_exp9(int n1, int n2, const T* __restrict__ a9, const T* __restrict__ idiag,
                            const T* __restrict__ b, T* __restrict__ x, int ci, int cj) {
@@ -757,6 +828,10 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.b, n * 8));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.x32, n * 4));
         IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.b32, n * 4));
+        if (Lv.kind == FACE5) {
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.xa, n * 8));
+            IMPEC_CUDA_TRY(cudaMalloc((void**)&Lv.xa32, n * 4));
+        }
         ctx->L.push_back(Lv);
         const int cmax = (int)env_long("IMPEC_MG_COARSEST", 4);  // coarsest level: both sides <= cmax
         if (n1 <= cmax && n2 <= cmax) break;
@@ -787,6 +862,7 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         T.coarse_cells32 = env_long("IMPEC_MG_COARSE_CELLS32", T.coarse_cells32);
         T.rb_skip = env_long("IMPEC_MG_RB_SKIP", T.rb_skip);
         T.rb_resid = env_long("IMPEC_MG_RB_RESID", T.rb_resid);
+        T.tile_cells = env_long("IMPEC_MG_TILE_CELLS", T.tile_cells);
         ctx->cn_predict = env_long("IMPEC_CN_PREDICT", 1) != 0;
         if (ctx->dir_row >= 0) {
             IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dmask, nf));
@@ -817,7 +893,7 @@ impec_status pressure_alloc(impec_ctx* ctx) {
 void pressure_free(impec_ctx* ctx) {
     for (Level& Lv : ctx->L) {
         void* ps[] = {Lv.tx,   Lv.ty,   Lv.a9,   Lv.idiag,   Lv.diag,   Lv.ed,  Lv.x,   Lv.b,
-                      Lv.tx32, Lv.ty32, Lv.a932, Lv.idiag32, Lv.diag32, Lv.x32, Lv.b32};
+                      Lv.tx32, Lv.ty32, Lv.a932, Lv.idiag32, Lv.diag32, Lv.x32, Lv.b32, Lv.xa, Lv.xa32};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
@@ -946,6 +1022,32 @@ const double* level_diag<double>(const Level& Lv) { return Lv.diag; }
 template <>
 const float* level_diag<float>(const Level& Lv) { return Lv.diag32; }
 
+template <class T>
+static T* level_alt(Level& Lv);
+template <>
+double* level_alt<double>(Level& Lv) { return Lv.xa; }
+template <>
+float* level_alt<float>(Level& Lv) { return Lv.xa32; }
+template <class T>
+static void swap_iterate(Level& Lv);
+template <>
+void swap_iterate<double>(Level& Lv) { std::swap(Lv.x, Lv.xa); }
+template <>
+void swap_iterate<float>(Level& Lv) { std::swap(Lv.x32, Lv.xa32); }
+
+// Whether level l sweeps with k_rb_tile.  Each sweep writes the other iterate buffer and the
+// level's pointers are swapped, so every kernel takes the iterate from the Level when it is
+// launched.  A captured loop body replays the pointers of its capture, which is consistent only
+// if each V-cycle starts the level from a write that reads no old iterate: true for the coarse
+// levels and, with CG, for the finest level (its cycles start from x = 0); the stationary
+// iteration's finest level, which corrects the solution in place, keeps the two-launch sweep.
+template <class T>
+static bool use_tile(impec_ctx* ctx, size_t l) {
+    Level& Lv = ctx->L[l];
+    return ctx->tune.tile_cells > 0 && Lv.kind == FACE5 && Lv.n() >= (size_t)ctx->tune.tile_cells &&
+           (ctx->krylov || l > 0) && level_alt<T>(Lv) != nullptr;
+}
+
 // Grid of the red-black kernels (k_rb_face5, k_rb_zero, k_prolong_rb): RB_ROWS rows and two
 // columns per thread.
 static dim3 rb_grid(const Level& Lv) {
@@ -960,6 +1062,23 @@ static void smooth(impec_ctx* ctx, Level& Lv, int sweeps, bool reverse, bool zer
     const T *tx, *ty, *a9, *id;
     T *x, *b;
     level_ptrs<T>(Lv, tx, ty, a9, id, x, b);
+    if (use_tile<T>(ctx, (size_t)(&Lv - ctx->L.data()))) {  // one launch per sweep, ping-pong
+        const dim3 g((Lv.n2 + TILE_C - 1) / TILE_C, (Lv.n1 + TILE_R - 1) / TILE_R);
+        for (int s = 0; s < sweeps; ++s) {
+            level_ptrs<T>(Lv, tx, ty, a9, id, x, b);
+            T* xo = level_alt<T>(Lv);
+            const int first = reverse ? 1 : 0;
+            ++ctx->nlaunch;
+            if (zero && s == 0)  // x = 0: the first colour is b * idiag (first is red here)
+                launch_k(ctx->stream, k_rb_tile<T, true>, g, TILE_THREADS, 0, Lv.n1, Lv.n2, tx, ty, id, b, (const T*)x,
+                         xo, first);
+            else
+                launch_k(ctx->stream, k_rb_tile<T, false>, g, TILE_THREADS, 0, Lv.n1, Lv.n2, tx, ty, id, b,
+                         (const T*)x, xo, first);
+            swap_iterate<T>(Lv);
+        }
+        return;
+    }
     for (int s = 0; s < sweeps; ++s) {
         if (Lv.kind == FACE5) {
             const dim3 g = rb_grid(Lv);
@@ -1169,12 +1288,16 @@ static void vcycle(impec_ctx* ctx, size_t l, bool zero, bool first_done = false)
     level_ptrs<T>(C, ctx_, cty, ca9, cid, cx, cb);
     const bool zs = zero && zero_start_free<T>(ctx, l);
     smooth<T>(ctx, F, (int)ctx->tune.pre, false, zs, zs && first_done);
+    level_ptrs<T>(F, tx, ty, a9, id, x, b);  // the sweep may have moved the iterate (ping-pong)
     ++ctx->nlaunch;
     const int zero_color = restrict_zero_color(ctx, F);
-    const bool cz = zero_start_free<T>(ctx, l + 1);  // the coarse cycle's first colour is done here
+    // the coarse cycle's first colour is done here, unless that level sweeps in one launch
+    // (its zero-start sweep computes the first colour itself)
+    const bool cz = zero_start_free<T>(ctx, l + 1) && !use_tile<T>(ctx, l + 1);
     launch_k(ctx->stream, k_restrict<T>, grid2(C.n1, C.n2), dim3(BX, BY), 0, F, tx, ty, a9, level_diag<T>(F), b, x,
              C.n1, C.n2, cb, cx, zero_color, cz ? (const T*)cid : nullptr);
     vcycle<T>(ctx, l + 1, true, cz);
+    level_ptrs<T>(C, ctx_, cty, ca9, cid, cx, cb);  // the coarse iterate may have moved too
     const unsigned char* mask = l == 0 && ctx->dir_row >= 0 ? ctx->dmask : nullptr;
     ++ctx->nlaunch;
     if (ctx->tune.rb_skip != 0 && F.kind == FACE5 && ctx->tune.post >= 1)  // the black cells are overwritten next
@@ -1495,8 +1618,6 @@ impec_status pressure_iteration(impec_ctx* ctx, double tol, cudaGraphConditional
     }
     DevScalars* S = ctx->dscal;
     double* r = mixed ? ctx->r : F.b;
-    const double* z = mixed ? nullptr : F.x;
-    const float* z32 = mixed ? F.x32 : nullptr;
     if (mixed) {
         if (!zero_start_free<float>(ctx, 0)) IMPEC_CUDA_TRY(cudaMemsetAsync(F.x32, 0, n * 4, ctx->stream));
         vcycle<float>(ctx, 0, true);
@@ -1504,6 +1625,9 @@ impec_status pressure_iteration(impec_ctx* ctx, double tol, cudaGraphConditional
         if (!zero_start_free<double>(ctx, 0)) IMPEC_CUDA_TRY(cudaMemsetAsync(F.x, 0, n * 8, ctx->stream));
         vcycle<double>(ctx, 0, true);
     }
+    // the preconditioned residual z, where the cycle left it (the sweeps may swap buffers)
+    const double* z = mixed ? nullptr : F.x;
+    const float* z32 = mixed ? F.x32 : nullptr;
     const int cap = red_cap(ctx->num_sms, ctx->max_blocks), blocks = seg_blocks(F.n1, F.n2, cap);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_cg_dots, blocks, RED_THREADS, 0, F.n1, F.n2, r, z, z32, ctx->cg_q, ctx->partials,
@@ -1697,6 +1821,49 @@ impec_status max_stable_dt_dev(impec_ctx* ctx, const double* u, const double* v)
 }  // namespace impec
 
 using namespace impec;
+
+// Cold timing of one probed kernel: before each repetition `flush_bytes` of `flush` are
+// overwritten on the context's stream (evicting the kernel's data from L2), then the kernel
+// runs between two events on that stream.  *ms: mean over the repetitions, *ms_min: the fastest.
+extern "C" impec_status impec_time_kernel_cold(impec_ctx* ctx, int which, int reps, void* flush, size_t flush_bytes,
+                                               double* ms, double* ms_min, double* bytes) {
+    if (!ctx || reps <= 0 || which < 0 || which > 1 || !flush || !flush_bytes) return IMPEC_ERR_ARG;
+    Level& F = ctx->L[0];
+    if (F.kind != FACE5) return IMPEC_ERR_ARG;
+    const double n = (double)F.n();
+    if (which == 1 && ctx->P.precision != IMPEC_PREC_MIXED) {  // FP32 copies of the fine level
+        const int nb = ctx->num_sms * 4;
+        launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)(F.n1 + 1) * F.n2, F.tx, F.tx32);
+        launch_k(ctx->stream, k_to_float, nb, 256, 0, (size_t)F.n1 * (F.n2 + 1), F.ty, F.ty32);
+        launch_k(ctx->stream, k_to_float, nb, 256, 0, F.n(), F.idiag, F.idiag32);
+        launch_k(ctx->stream, k_to_float, nb, 256, 0, F.n(), F.b, F.b32);
+        launch_k(ctx->stream, k_to_float, nb, 256, 0, F.n(), F.x, F.x32);
+        IMPEC_LAUNCH_CHECK();
+    }
+    cudaEvent_t e0, e1;
+    IMPEC_CUDA_TRY(cudaEventCreate(&e0));
+    IMPEC_CUDA_TRY(cudaEventCreate(&e1));
+    double tot = 0, best = 1e30;
+    for (int r = 0; r < reps; ++r) {
+        IMPEC_CUDA_TRY(cudaMemsetAsync(flush, r & 0xff, flush_bytes, ctx->stream));
+        IMPEC_CUDA_TRY(cudaEventRecord(e0, ctx->stream));
+        if (which == 0) smooth<double>(ctx, F, 1, false);
+        else smooth<float>(ctx, F, 1, false);
+        IMPEC_CUDA_TRY(cudaEventRecord(e1, ctx->stream));
+        IMPEC_CUDA_TRY(cudaEventSynchronize(e1));
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        tot += t;
+        best = t < best ? t : best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms) *ms = tot / reps;
+    if (ms_min) *ms_min = best;
+    // algorithmic bytes of one five-point sweep: x read and written, b, and the two face planes
+    if (bytes) *bytes = n * (which == 0 ? 8.0 : 4.0) * 5.0;
+    return IMPEC_OK;
+}
 
 extern "C" impec_status impec_time_kernel(impec_ctx* ctx, int which, int reps, double* ms, double* bytes) {
     if (!ctx || reps <= 0 || which < 0 || which > 4) return IMPEC_ERR_ARG;

@@ -381,7 +381,7 @@ static long* tuning_field(impec_ctx* ctx, const char* name) {
     struct { const char* n; long* v; } tab[] = {
         {"mg_pre", &t.pre},          {"mg_post", &t.post},         {"cluster", &t.cluster},
         {"cluster_cells", &t.cl_cells}, {"cluster_cta0", &t.cl_cta0}, {"coarse_cells64", &t.coarse_cells64},
-        {"coarse_cells32", &t.coarse_cells32}};
+        {"coarse_cells32", &t.coarse_cells32}, {"tile_cells", &t.tile_cells}};
     for (auto& e : tab)
         if (!strcmp(e.n, name)) return e.v;
     return nullptr;

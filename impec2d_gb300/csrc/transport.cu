@@ -417,15 +417,14 @@ impec_status advect_split_dev(impec_ctx* ctx, double* c, const double* u, const 
     const impec_params& P = ctx->P;
     const size_t bytes = (size_t)P.N1 * P.N2 * 8;
     double *t1 = ctx->t1, *t2 = ctx->t2, *t3 = ctx->t3;
-    if (P.hmtype == IMPEC_CTU) {  // unsplit: one CTU update, c -> t1, then back into c
+    if (P.hmtype == IMPEC_CTU) {  // unsplit: one CTU update, c -> t1, then back into c; pfs untouched
         const double fx = 1.0 / (ctx->G.dx * P.porosity), fy = 1.0 / (ctx->G.dy * P.porosity);
         ++ctx->nlaunch;
         if (P.bc == IMPEC_BC_PERIODIC) launch_k(ctx->stream, k_ctu<IMPEC_BC_PERIODIC>, tgrid(P.N1, P.N2), dim3(TBX, TBY), 0, P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
         else launch_k(ctx->stream, k_ctu<IMPEC_BC_NEUMANN>, tgrid(P.N1, P.N2), dim3(TBX, TBY), 0, P.N1, P.N2, c, t1, u, v, dt_dev, fx, fy);
         IMPEC_LAUNCH_CHECK();
         IMPEC_CUDA_TRY(cudaMemcpyAsync(c, t1, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-        *pfs = 0;
-        return IMPEC_OK;
+        return IMPEC_OK;  // unsplit: the alternating-sweep state stays as it was
     }
     if (P.dim_splitting == IMPEC_SYMMETRIC_PARALLEL && (P.hmtype == IMPEC_WAFSPLIT || P.hmtype == IMPEC_WAF)) {
         // the average of XY and YX through the per-sweep kernels (the fused tile kernel has

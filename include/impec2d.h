@@ -255,6 +255,15 @@ impec_status impec_learned_target(impec_ctx* ctx, float* T);
 /* Step length of the last solve's learned correction (0: rejected). */
 impec_status impec_learned_alpha(impec_ctx* ctx, double* alpha);
 
+/* Cold timing of one fine-level smoother sweep (which 0: FP64, 1: FP32; five-point levels):
+ * before each of `reps` repetitions `flush_bytes` of the device buffer `flush` are overwritten
+ * on the context's stream, so the sweep's data comes from HBM; each repetition is timed with
+ * events on that stream.  *ms: mean, *ms_min: fastest, *bytes: the sweep's algorithmic bytes (x
+ * read and written, b, the two face planes).  A benchmark probe; no counterpart in the
+ * reference. */
+impec_status impec_time_kernel_cold(impec_ctx* ctx, int which, int reps, void* flush, size_t flush_bytes,
+                                    double* ms, double* ms_min, double* bytes);
+
 /* FP64 fused multiply-adds per second that the current device sustains (eight independent
  * chains per thread on every SM): the denominator of the FP64-pipe fractions reported beside
  * the HBM roofline.  No counterpart in the reference. */

@@ -734,3 +734,39 @@ def test_waf_ctu_convergence_through_the_cfg_surface(engine, oracle_lib, tmp_pat
         assert abs(np.exp(rows[k, 1]) / e_or - 1) <= 1e-9, (N, np.exp(rows[k, 1]), e_or)
     fit = np.polyfit(rows[:, 0], rows[:, 1], 1)[0]
     assert abs(fit - order) < 1e-3, fit
+
+
+@pytest.mark.parametrize("N1,N2,stype", [(300, 130, 1), (1024, 1024, 1), (97, 70, 2), (515, 333, 1)])
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("krylov", ["1", "0"])
+@pytest.mark.parametrize("graph", [True, False])
+def test_one_launch_sweep_matches_two_launch_sweeps(engine, monkeypatch, N1, N2, stype, prec, krylov, graph):
+    """A red-black sweep in one launch (k_rb_tile: both colours per tile, a recomputed ring,
+    ping-pong iterates) gives the two-launch sweeps' result bit for bit: the same cycles,
+    residual and pressure, for CG and the stationary iteration (whose finest level keeps the
+    two-launch sweep), in FP64 and mixed precision, with a Dirichlet row (stype 2), through
+    the captured solve graph (replayed three times) and the host-driven loop."""
+    E = engine
+    import torch
+    monkeypatch.setenv("IMPEC_MG_KRYLOV", krylov)
+    out = []
+    for tile in ("0", "1"):
+        monkeypatch.setenv("IMPEC_MG_TILE_CELLS", tile)
+        P, ctx = _ctx(E, N1, N2, nu=1.0, stype=stype, precision=prec, max_cycles=200)
+        OP = oparams(P)
+        q = source(OP)
+        c = _rand_c(N1, N2, 12)
+        if graph:
+            ctx.upload(cell_ghost(OP, c), q, ghost=2)
+            res = [ctx.pressure_solve_resident() for _ in range(3)]
+            ph = np.zeros(O.scalar_shape(OP))
+            ctx.download(None, ph, None, ghost=2)
+            out.append((res, O.interior(OP, ph).copy()))
+        else:
+            ctx.set_source(dev(q))
+            p = torch.zeros((N1, N2), dtype=torch.float64, device="cuda")
+            cyc, rr, _ = ctx.pressure_solve(dev(c), p, 1e-11)
+            out.append(([(cyc, rr)], host(p)))
+        ctx.close()
+    assert out[0][0] == out[1][0], (out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
