@@ -135,10 +135,12 @@ struct Tuning {
     long coarse_cells32 = 1024;    // the same, FP32
     long rb_skip = 1;  // five-point levels: no zero fill before pre-smoothing, red-only prolongation
     long rb_resid = 1;  // five-point levels: restriction sums the red residuals only (black ones are ~0)
-    // five-point levels of at least this many cells sweep both colours in one launch
+    // FP64 five-point levels of at least this many cells sweep both colours in one launch
     // (k_rb_tile, ping-pong iterate): every coefficient is read once per sweep instead of once
-    // per colour, which pays where the level streams from HBM; 0 disables
-    long tile_cells = 1L << 22;
+    // per colour, which pays where the level streams from HBM (4096^2 sweep 199 against 240 us
+    // cold, solve 16.9 against 17.9 ms) and costs where it sits in L2 (1024^2 and 2048^2 solves
+    // 10% and 3% slower: the recomputed ring and one more dependent phase); 0 disables
+    long tile_cells = 1L << 23;
 };
 }  // namespace impec
 

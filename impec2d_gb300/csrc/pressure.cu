@@ -97,21 +97,43 @@ __global__ void k_corner(int n1, int n2, const double* __restrict__ w1, const do
 // ---------------------------------------------------------------- fine operators
 // nu = 1: face transmissibilities dA/dx^2 * lambda with zero flux through the boundary.
 // tx32 / ty32 (or nullptr): their FP32 copies for the mixed-precision cycle.
+// Diagonal of a five-point cell from its four faces, in k_idiag's order, and its reciprocal
+// (with the FP32 copies of the mixed-precision cycle when asked).
+__device__ __forceinline__ void store_diag5(size_t k, double tw, double te, double ts, double tn,
+                                            double* __restrict__ diag, double* __restrict__ idiag,
+                                            float* __restrict__ diag32, float* __restrict__ idiag32) {
+    const double d = tw + te + ts + tn;
+    const double id = d != 0.0 ? 1.0 / d : 0.0;
+    diag[k] = d;
+    idiag[k] = id;
+    if (diag32) diag32[k] = (float)d;
+    if (idiag32) idiag32[k] = (float)id;
+}
+
+// Finest five-point faces t = lambda * dA / h^2 (boundary faces 0).  With diag != null (no
+// Dirichlet row, which changes the faces afterwards) the kernel also writes the diagonal and its
+// reciprocal, recomputing the east and north faces of its cell: the separate k_idiag launch of
+// this level is then not needed, and the values are the same bit for bit.
 __global__ void k_face5_fine(int n1, int n2, const double* __restrict__ lamx, const double* __restrict__ lamy,
                              double sx, double sy, double* __restrict__ tx, double* __restrict__ ty,
-                             float* __restrict__ tx32, float* __restrict__ ty32) {
+                             float* __restrict__ tx32, float* __restrict__ ty32, double* __restrict__ diag,
+                             double* __restrict__ idiag, float* __restrict__ diag32, float* __restrict__ idiag32) {
     pdl_enter();
     int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    auto fx = [&](int a, int b) { return (a == 0 || a == n1) ? 0.0 : lamx[IX(a, b, n2)] * sx; };
+    auto fy = [&](int a, int b) { return (b == 0 || b == n2) ? 0.0 : lamy[IX(a, b, n2 + 1)] * sy; };
     if (i <= n1 && j < n2) {
-        const double t = (i == 0 || i == n1) ? 0.0 : lamx[IX(i, j, n2)] * sx;
+        const double t = fx(i, j);
         tx[IX(i, j, n2)] = t;
         if (tx32) tx32[IX(i, j, n2)] = (float)t;
     }
     if (i < n1 && j <= n2) {
-        const double t = (j == 0 || j == n2) ? 0.0 : lamy[IX(i, j, n2 + 1)] * sy;
+        const double t = fy(i, j);
         ty[IX(i, j, n2 + 1)] = t;
         if (ty32) ty32[IX(i, j, n2 + 1)] = (float)t;
     }
+    if (diag && i < n1 && j < n2)
+        store_diag5(IX(i, j, n2), fx(i, j), fx(i + 1, j), fy(i, j), fy(i, j + 1), diag, idiag, diag32, idiag32);
 }
 
 // Reference row (C,W,SW,S,SE,E,NE,N,NW) of GetWeightedMatrixCoefficientsForCell
@@ -175,31 +197,45 @@ __global__ void k_exp9_fine(int n1, int n2, const double* __restrict__ lamx, con
 __constant__ int c_off[9][2] = {{0, 0}, {-1, 0}, {-1, -1}, {0, -1}, {1, -1}, {1, 0}, {1, 1}, {0, 1}, {-1, 1}};
 
 // ---------------------------------------------------------------- coarse operators
+// Coarse five-point faces (half the sum of the two fine faces they cover).  With diag != null
+// (no extra diagonal from a Dirichlet row) the kernel also writes the coarse diagonal and its
+// reciprocal from recomputed faces, in place of the level's k_idiag launch (same values).
 __global__ void k_face5_coarsen(int n1f, int n2f, const double* __restrict__ txf, const double* __restrict__ tyf,
                                 int n1c, int n2c, double* __restrict__ txc, double* __restrict__ tyc,
-                                float* __restrict__ txc32, float* __restrict__ tyc32) {
+                                float* __restrict__ txc32, float* __restrict__ tyc32, double* __restrict__ diag,
+                                double* __restrict__ idiag, float* __restrict__ diag32, float* __restrict__ idiag32) {
     pdl_enter();
     int J = blockIdx.x * BX + threadIdx.x, I = blockIdx.y * BY + threadIdx.y;
-    if (I <= n1c && J < n2c) {
-        int fi = 2 * I;
+    auto cx = [&](int a, int b) {  // coarse x-face (a, b)
+        int fi = 2 * a;
         double s = 0.0;
         if (fi <= n1f) {
-            s = txf[IX(fi, 2 * J, n2f)];
-            if (2 * J + 1 < n2f) s += txf[IX(fi, 2 * J + 1, n2f)];
+            s = txf[IX(fi, 2 * b, n2f)];
+            if (2 * b + 1 < n2f) s += txf[IX(fi, 2 * b + 1, n2f)];
         }
-        txc[IX(I, J, n2c)] = 0.5 * s;
-        if (txc32) txc32[IX(I, J, n2c)] = (float)(0.5 * s);
-    }
-    if (I < n1c && J <= n2c) {
-        int fj = 2 * J;
+        return 0.5 * s;
+    };
+    auto cy = [&](int a, int b) {  // coarse y-face (a, b)
+        int fj = 2 * b;
         double s = 0.0;
         if (fj <= n2f) {
-            s = tyf[IX(2 * I, fj, n2f + 1)];
-            if (2 * I + 1 < n1f) s += tyf[IX(2 * I + 1, fj, n2f + 1)];
+            s = tyf[IX(2 * a, fj, n2f + 1)];
+            if (2 * a + 1 < n1f) s += tyf[IX(2 * a + 1, fj, n2f + 1)];
         }
-        tyc[IX(I, J, n2c + 1)] = 0.5 * s;
-        if (tyc32) tyc32[IX(I, J, n2c + 1)] = (float)(0.5 * s);
+        return 0.5 * s;
+    };
+    if (I <= n1c && J < n2c) {
+        const double t = cx(I, J);
+        txc[IX(I, J, n2c)] = t;
+        if (txc32) txc32[IX(I, J, n2c)] = (float)t;
     }
+    if (I < n1c && J <= n2c) {
+        const double t = cy(I, J);
+        tyc[IX(I, J, n2c + 1)] = t;
+        if (tyc32) tyc32[IX(I, J, n2c + 1)] = (float)t;
+    }
+    if (diag && I < n1c && J < n2c)
+        store_diag5(IX(I, J, n2c), cx(I, J), cx(I + 1, J), cy(I, J), cy(I, J + 1), diag, idiag, diag32, idiag32);
 }
 
 __global__ void k_exp9_coarsen(int n1f, int n2f, const double* __restrict__ af, const unsigned char* __restrict__ maskf,
@@ -937,7 +973,9 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
     if (F.kind == FACE5) {
         double sx = G.dA * (1. / (G.dx * G.dx)), sy = G.dA * (1. / (G.dy * G.dy));
         ++ctx->nlaunch, launch_k(ctx->stream, k_face5_fine, grid2(F.n1 + 1, F.n2 + 1), dim3(BX, BY), 0, F.n1, F.n2, ctx->lamx, ctx->lamy,
-                                 sx, sy, F.tx, F.ty, f32 && !dir ? F.tx32 : nullptr, f32 && !dir ? F.ty32 : nullptr);
+                                 sx, sy, F.tx, F.ty, f32 && !dir ? F.tx32 : nullptr, f32 && !dir ? F.ty32 : nullptr,
+                                 dir ? nullptr : F.diag, dir ? nullptr : F.idiag,
+                                 mixed && !dir ? F.diag32 : nullptr, mixed && !dir ? F.idiag32 : nullptr);
     } else {
         ++ctx->nlaunch, launch_k(ctx->stream, k_exp9_fine, grid2(F.n1, F.n2), dim3(BX, BY), 0, F.n1, F.n2, ctx->lamx, ctx->lamy, ctx->cm11,
                                                                          ctx->cm22, ctx->cm12, P.nu, G, F.a9);
@@ -962,7 +1000,9 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
         Level &A = ctx->L[l], &B = ctx->L[l + 1];
         if (A.kind == FACE5) {
             ++ctx->nlaunch, launch_k(ctx->stream, k_face5_coarsen, grid2(B.n1 + 1, B.n2 + 1), dim3(BX, BY), 0, A.n1, A.n2, A.tx, A.ty, B.n1,
-                                     B.n2, B.tx, B.ty, f32 ? B.tx32 : nullptr, f32 ? B.ty32 : nullptr);
+                                     B.n2, B.tx, B.ty, f32 ? B.tx32 : nullptr, f32 ? B.ty32 : nullptr,
+                                     dir ? nullptr : B.diag, dir ? nullptr : B.idiag,
+                                     mixed && !dir ? B.diag32 : nullptr, mixed && !dir ? B.idiag32 : nullptr);
             if (dir)
                 ++ctx->nlaunch, launch_k(ctx->stream, k_ed_coarsen, grid2(B.n1, B.n2), dim3(BX, BY), 0, A.n1, A.n2, A.ed,
                                          B.n1, B.n2, B.ed);
@@ -974,10 +1014,13 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
     }
     for (size_t l = 0; l < ctx->L.size(); ++l) {
         Level& Lv = ctx->L[l];
-        ++ctx->nlaunch, launch_k(ctx->stream, k_idiag, grid2(Lv.n1, Lv.n2), dim3(BX, BY), 0, Lv.n1, Lv.n2, Lv.kind, Lv.tx,
-                                 Lv.ty, Lv.a9, dir && Lv.kind == FACE5 ? Lv.ed : nullptr, l == 0 ? mask0 : nullptr,
-                                 Lv.diag, Lv.idiag, mixed ? Lv.diag32 : nullptr, mixed ? Lv.idiag32 : nullptr);
-        IMPEC_LAUNCH_CHECK();
+        if (Lv.kind != FACE5 || dir) {  // five-point levels without a Dirichlet row got theirs above
+            ++ctx->nlaunch, launch_k(ctx->stream, k_idiag, grid2(Lv.n1, Lv.n2), dim3(BX, BY), 0, Lv.n1, Lv.n2, Lv.kind,
+                                     Lv.tx, Lv.ty, Lv.a9, dir && Lv.kind == FACE5 ? Lv.ed : nullptr,
+                                     l == 0 ? mask0 : nullptr, Lv.diag, Lv.idiag, mixed ? Lv.diag32 : nullptr,
+                                     mixed ? Lv.idiag32 : nullptr);
+            IMPEC_LAUNCH_CHECK();
+        }
         if (mixed) {
             const size_t n = Lv.n();
             int nb = ctx->num_sms * 4;
@@ -1041,10 +1084,12 @@ void swap_iterate<float>(Level& Lv) { std::swap(Lv.x32, Lv.xa32); }
 // if each V-cycle starts the level from a write that reads no old iterate: true for the coarse
 // levels and, with CG, for the finest level (its cycles start from x = 0); the stationary
 // iteration's finest level, which corrects the solution in place, keeps the two-launch sweep.
+// FP64 only: the FP32 sweeps of the mixed-precision cycle measured no faster in one launch
+// (4096^2: 133 against 131 us cold).
 template <class T>
 static bool use_tile(impec_ctx* ctx, size_t l) {
     Level& Lv = ctx->L[l];
-    return ctx->tune.tile_cells > 0 && Lv.kind == FACE5 && Lv.n() >= (size_t)ctx->tune.tile_cells &&
+    return sizeof(T) == 8 && ctx->tune.tile_cells > 0 && Lv.kind == FACE5 && Lv.n() >= (size_t)ctx->tune.tile_cells &&
            (ctx->krylov || l > 0) && level_alt<T>(Lv) != nullptr;
 }
 
