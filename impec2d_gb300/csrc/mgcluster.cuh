@@ -15,6 +15,9 @@
 // restriction aggregate never straddles two CTAs); CTA r owns rows [r*rows[l], (r+1)*rows[l]).
 // Levels nd .. nl-1 have rows[l] = n1[l]: CTA 0 owns all of them.
 //
+// Staging: every CTA copies its bands (and CTA 0 the coarsest inverse) with asynchronous
+// element copies (cp.async), all in flight at once, and waits for them once.
+//
 // Every barrier is reached by all threads of all CTAs the same number of times (the counts
 // depend only on nd), and no CTA reads another's shared memory after the last barrier.
 #pragma once
@@ -42,6 +45,7 @@ struct ClusterArgs {
     T* x0;        // iterate of level 0 (global), read at the start and written at the end
     const T* b0;  // right-hand side of level 0 (global)
     const double* dinv;
+    unsigned dinv_off;  // byte offset in shared memory of CTA 0's copy of dinv
 };
 
 // Pointer to row i of array `arr` of level l, in the shared memory of the CTA that owns it.
@@ -164,40 +168,6 @@ __device__ void cl_prolong(const cooperative_groups::cluster_group& cl, T* sm, i
     }
 }
 
-// Dense coarsest solve on CTA 0 (the arithmetic of k_coarse_vcycle): x = Dinv b with b(0) := 0
-// and the mean removed for the singular system.
-template <class T>
-__device__ void cl_dense(T* sm, const ClusterArgs<T>& A) {
-    __shared__ double red[32];
-    const int L = A.nl - 1, n = A.dn;
-    const T* b = sm + A.off[L][CL_B];
-    T* x = sm + A.off[L][CL_X];
-    double v = 0;
-    if ((int)threadIdx.x < n) {
-        double s = 0;
-        for (int c = 0; c < n; ++c) {
-            double bc = (A.singular && c == 0) ? 0.0 : (double)b[c];
-            s += A.dinv[(size_t)threadIdx.x * n + c] * bc;
-        }
-        v = s;
-    }
-    double m = 0;
-    if (A.singular) {
-        double w = v;
-        for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = w;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0;
-            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
-            red[0] = t / n;
-        }
-        __syncthreads();
-        m = red[0];
-    }
-    if ((int)threadIdx.x < n) x[threadIdx.x] = (T)(v - m);
-}
-
 template <class T>
 __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_constant__ ClusterArgs<T> A) {
     pdl_enter();
@@ -217,21 +187,28 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
         T* ty = sm + A.off[l][CL_TY];
         T* id = sm + A.off[l][CL_ID];
         T* dg = sm + A.off[l][CL_DG];
-        for (int k = threadIdx.x; k < (cnt + 1) * n2; k += blockDim.x) tx[k] = A.tx[l][(size_t)lo * n2 + k];
-        for (int k = threadIdx.x; k < cnt * (n2 + 1); k += blockDim.x) ty[k] = A.ty[l][(size_t)lo * (n2 + 1) + k];
+        for (int k = threadIdx.x; k < (cnt + 1) * n2; k += blockDim.x)
+            stage_async(tx + k, A.tx[l] + (size_t)lo * n2 + k);
+        for (int k = threadIdx.x; k < cnt * (n2 + 1); k += blockDim.x)
+            stage_async(ty + k, A.ty[l] + (size_t)lo * (n2 + 1) + k);
         for (int k = threadIdx.x; k < cnt * n2; k += blockDim.x) {
-            id[k] = A.id[l][(size_t)lo * n2 + k];
-            dg[k] = A.dg[l][(size_t)lo * n2 + k];
+            stage_async(id + k, A.id[l] + (size_t)lo * n2 + k);
+            stage_async(dg + k, A.dg[l] + (size_t)lo * n2 + k);
         }
         if (l == 0) {
             T* x = sm + A.off[0][CL_X];
             T* b = sm + A.off[0][CL_B];
             for (int k = threadIdx.x; k < cnt * n2; k += blockDim.x) {
-                x[k] = A.x0[(size_t)lo * n2 + k];
-                b[k] = A.b0[(size_t)lo * n2 + k];
+                stage_async(x + k, A.x0 + (size_t)lo * n2 + k);
+                stage_async(b + k, A.b0 + (size_t)lo * n2 + k);
             }
         }
     }
+    if (rank == 0) {  // the dense inverse of the coarsest level
+        double* dinv = reinterpret_cast<double*>(cl_raw + A.dinv_off);
+        for (int k = threadIdx.x; k < A.dn * A.dn; k += blockDim.x) stage_async(dinv + k, A.dinv + k);
+    }
+    stage_wait();
     cl.sync();
     // down: levels spread over the cluster
     for (int l = 0; l < A.nd; ++l) {
@@ -252,8 +229,9 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
             cl_restrict(cl, sm, 0, A, l);
             __syncthreads();
         }
-        cl_dense(sm, A);
-        __syncthreads();
+        const double* dinv = reinterpret_cast<const double*>(cl_raw + A.dinv_off);
+        const int L = A.nl - 1;
+        dense_coarse_apply<T>(A.dn, dinv, sm + A.off[L][CL_B], sm + A.off[L][CL_X], A.singular);
         for (int l = A.nl - 2; l >= A.nd; --l) {
             cl_prolong(cl, sm, 0, A, l);
             __syncthreads();

@@ -8,6 +8,46 @@
 
 constexpr int MGC_MAXL = 8;
 
+// Asynchronous copy of one element, global -> this CTA's shared memory (cp.async of 4 or 8
+// bytes: any element-aligned address qualifies).  A staging loop issues all of its copies
+// before one cp.async.wait_all, instead of one global-load round trip per element.
+template <class T>
+__device__ __forceinline__ void stage_async(T* dst, const T* src) {
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "cp.async element");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src),
+                 "n"(sizeof(T))
+                 : "memory");
+}
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Coarsest-level solve x = Dinv b' in FP64 (n <= 64), b' = b with b(0) := 0 for the singular
+// system (whose Dinv, from k_dense_invert, already removes the mean of the result).  Every
+// thread of the block takes part (the count of loop trips and shuffles is the same for all):
+// row r is summed by the 8 lanes of one lane group, lane g over the columns g, g + 8, g + 16,
+// ... in ascending order; an xor butterfly then adds the 8 partials as
+// ((p0+p1)+(p2+p3))+((p4+p5)+(p6+p7)) on every lane.  On this FP64 pipe the latency of the
+// dependent chain sets the time, so it is kept short: 8 multiply-adds and 3 additions.  The
+// coarse V-cycle kernels all solve the coarsest level here, so they give the same bits.
+// dinv: row-major, row stride n, in global or shared memory.
+template <class T>
+__device__ void dense_coarse_apply(int n, const double* dinv, const T* b, T* x, int singular) {
+    const int t = threadIdx.x, g = t & 7, rows = blockDim.x >> 3;
+    for (int base = 0; base < n; base += rows) {
+        const int r = base + (t >> 3);
+        double s = 0.0;
+        if (r < n)
+            for (int c = g; c < n; c += 8) {
+                const double bc = (singular && c == 0) ? 0.0 : (double)b[c];
+                s += dinv[r * n + c] * bc;
+            }
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        s += __shfl_xor_sync(0xffffffffu, s, 4);
+        if (r < n && g == 0) x[r] = (T)s;
+    }
+    __syncthreads();
+}
+
 template <class T>
 struct CoarseArgs {
     int nl, singular, dn;
@@ -105,18 +145,24 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
     for (int l = 0; l < A.nl; ++l) {
         const int n1 = A.n1[l], n2 = A.n2[l], n = n1 * n2;
         if (KIND == FACE5) {
-            for (int k = threadIdx.x; k < (n1 + 1) * n2; k += blockDim.x) tx[l][k] = A.tx[l][k];
-            for (int k = threadIdx.x; k < n1 * (n2 + 1); k += blockDim.x) ty[l][k] = A.ty[l][k];
-            for (int k = threadIdx.x; k < n; k += blockDim.x) dg[l][k] = A.dg[l][k];
+            for (int k = threadIdx.x; k < (n1 + 1) * n2; k += blockDim.x) stage_async(tx[l] + k, A.tx[l] + k);
+            for (int k = threadIdx.x; k < n1 * (n2 + 1); k += blockDim.x) stage_async(ty[l] + k, A.ty[l] + k);
+            for (int k = threadIdx.x; k < n; k += blockDim.x) stage_async(dg[l] + k, A.dg[l] + k);
         } else {
-            for (int k = threadIdx.x; k < 9 * n; k += blockDim.x) a9[l][k] = A.a9[l][k];
+            for (int k = threadIdx.x; k < 9 * n; k += blockDim.x) stage_async(a9[l] + k, A.a9[l] + k);
         }
         for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            id[l][k] = A.id[l][k];
-            x[l][k] = l == 0 ? A.x0[k] : T(0);
-            b[l][k] = l == 0 ? A.b0[k] : T(0);
+            stage_async(id[l] + k, A.id[l] + k);
+            if (l == 0) {
+                stage_async(x[l] + k, A.x0 + k);
+                stage_async(b[l] + k, A.b0 + k);
+            } else {
+                x[l][k] = T(0);
+                b[l][k] = T(0);
+            }
         }
     }
+    stage_wait();
     __syncthreads();
     const int L = A.nl - 1;  // dense level
     for (int l = 0; l < L; ++l) {
@@ -136,35 +182,7 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseArgs<T> A) {
         }
         __syncthreads();
     }
-    {  // coarsest: x = Dinv b (FP64), b(0) := 0 and mean removal for the singular system
-        __shared__ double red[32];
-        const int n = A.dn;
-        double v = 0;
-        if ((int)threadIdx.x < n) {
-            double s = 0;
-            for (int c = 0; c < n; ++c) {
-                double bc = (A.singular && c == 0) ? 0.0 : (double)b[L][c];
-                s += A.dinv[(size_t)threadIdx.x * n + c] * bc;
-            }
-            v = s;
-        }
-        double m = 0;
-        if (A.singular) {
-            double w = v;
-            for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = w;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double t = 0;
-                for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
-                red[0] = t / n;
-            }
-            __syncthreads();
-            m = red[0];
-        }
-        if ((int)threadIdx.x < n) x[L][threadIdx.x] = (T)(v - m);
-        __syncthreads();
-    }
+    dense_coarse_apply<T>(A.dn, A.dinv, b[L], x[L], A.singular);  // coarsest level
     for (int l = L - 1; l >= 0; --l) {
         const int n1 = A.n1[l], n2 = A.n2[l], c1 = A.n1[l + 1], c2 = A.n2[l + 1];
         for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) {

@@ -661,7 +661,10 @@ __global__ void k_dense_build(Level C, const double* __restrict__ tx, const doub
 }
 
 // Gauss-Jordan inversion of an n x n (n <= 64) diagonally dominant matrix in shared memory.
-__global__ void k_dense_invert(int n, const double* __restrict__ D, double* __restrict__ Dinv) {
+// singular: D is the pinned singular system (row 0 = e_0), whose coarse solution has its mean
+// removed; the mean removal is linear, so it is folded into the stored matrix, which becomes
+// (I - 1 1^T / n) D^-1: every column less its mean.
+__global__ void k_dense_invert(int n, const double* __restrict__ D, double* __restrict__ Dinv, int singular) {
     pdl_enter();
     extern __shared__ double sm[];
     double* A = sm;          // n x n
@@ -691,36 +694,16 @@ __global__ void k_dense_invert(int n, const double* __restrict__ D, double* __re
             if (r != piv) A[r * n + piv] = 0.0;
         __syncthreads();
     }
-    for (int k = threadIdx.x; k < n * n; k += blockDim.x) Dinv[k] = B[k];
-}
-
-// x = Dinv * b (FP64 arithmetic), b(0) := 0 and mean removal for the singular system.
-template <class T>
-__global__ void k_dense_solve(int n, const double* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x,
-                              int singular) {
-    pdl_enter();
-    __shared__ double sb[64];
-    __shared__ double sx[64];
-    for (int k = threadIdx.x; k < n; k += blockDim.x) sb[k] = (singular && k == 0) ? 0.0 : (double)b[k];
-    __syncthreads();
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
-        double s = 0;
-        for (int cc = 0; cc < n; ++cc) s += Dinv[(size_t)r * n + cc] * sb[cc];
-        sx[r] = s;
-    }
-    __syncthreads();
     if (singular) {
-        __shared__ double mean;
-        if (threadIdx.x == 0) {
+        for (int cc = threadIdx.x; cc < n; cc += blockDim.x) {
             double m = 0;
-            for (int k = 0; k < n; ++k) m += sx[k];
-            mean = m / n;
+            for (int r = 0; r < n; ++r) m += B[r * n + cc];
+            m /= n;
+            for (int r = 0; r < n; ++r) B[r * n + cc] -= m;
         }
         __syncthreads();
-        for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = (T)(sx[k] - mean);
-    } else {
-        for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = (T)sx[k];
     }
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) Dinv[k] = B[k];
 }
 
 // ---------------------------------------------------------------- fine residual, norms, rhs
@@ -1040,7 +1023,7 @@ impec_status pressure_setup(impec_ctx* ctx, const double* c) {
                              ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n);
     IMPEC_LAUNCH_CHECK();
     ++ctx->nlaunch, launch_k(ctx->stream, k_dense_invert, 1, 256, 2 * ctx->dense_n * ctx->dense_n * 8,
-        ctx->dense_n, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n, ctx->dense_inv);
+        ctx->dense_n, ctx->dense_inv + (size_t)ctx->dense_n * ctx->dense_n, ctx->dense_inv, ctx->singular);
     IMPEC_LAUNCH_CHECK();
     return IMPEC_OK;
 }
@@ -1259,7 +1242,8 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
         }
     }
     A.nd = nd;
-    smem = off * sizeof(T);
+    A.dinv_off = (unsigned)((off * sizeof(T) + 15) / 16 * 16);
+    smem = A.dinv_off + (size_t)A.dn * A.dn * sizeof(double);
     return nd > 0 && smem <= MG_CLUSTER_SMEM;
 }
 
@@ -1352,8 +1336,6 @@ static void vcycle(impec_ctx* ctx, size_t l, bool zero, bool first_done = false)
     smooth<T>(ctx, F, (int)ctx->tune.post, true);
 }
 
-// Convergence check of the multigrid loop (one thread): relres = ||r||/||f||; decides whether
-// another cycle runs and, inside a graph, sets the WHILE node's condition.
 // Convergence check of the solve loop (one thread): relres = ||r||/||f||; decides whether
 // another cycle runs and, inside a graph, sets the WHILE node's condition.  With CG
 // (krylov) and after an iteration, it also keeps the iteration's alpha and (r, z) for the

@@ -102,9 +102,11 @@ def test_developed_state_step_at_1024(engine, oracle_lib):
     assert oracle_lib.or_cn_solve(C.byref(OP), O.ptr(cn), O.ptr(vo), 0.5 * dt, 1, 1e-13, None, None) == 0
     assert rel_err(host(cc), O.interior(OP, cn)) <= 1e-11
     ctx.close()
-    # the whole step from the developed state: engine (graph) against the oracle
+    # the whole step from the developed state: engine (graph) against the oracle.  Both solve the
+    # pressure to 2e-12: about 1e-12 is the smallest relative residual FP64 reaches on this
+    # state (the rounding of A x beside the wells), so a 1e-12 solve can stall at max_cycles.
     P2 = E.default_params(N, N, stype=E.PARALLEL, x_ub=2 ** 0.5, y_ub=2 ** 0.5, hmtype=E.MUSCL, diffusion=1,
-                          alpha_l=1e-3, alpha_t=1e-4, Dm=1e-6, eps=1e-12, para_eps=1e-12, max_cycles=200)
+                          alpha_l=1e-3, alpha_t=1e-4, Dm=1e-6, eps=2e-12, para_eps=1e-12, max_cycles=200)
     ctx = E.Context(P2)
     ctx.upload(cg, q, ghost=2)
     ctx.set_time(0.0)
