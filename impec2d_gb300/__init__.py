@@ -92,6 +92,8 @@ _SIGS = {
     "impec_state_upload": (C.c_int, [_VP, _PD, _PD, C.c_int]),
     "impec_state_download": (C.c_int, [_VP, _PD, _PD, _PD, C.c_int]),
     "impec_set_time": (C.c_int, [_VP, C.c_double]),
+    "impec_checkpoint_save": (C.c_int, [_VP, C.c_char_p]),
+    "impec_checkpoint_load": (C.c_int, [_VP, C.c_char_p]),
     "impec_velocity_upload": (C.c_int, [_VP, _PD, C.c_int]),
     "impec_pressure_upload": (C.c_int, [_VP, _PD, C.c_int]),
     "impec_set_pin_kappa": (C.c_int, [_VP, C.c_double]),
@@ -512,6 +514,12 @@ class Context:
         info = StepInfo()
         _chk(lib().impec_run_steps(self.h, n, C.byref(info)), "run_steps")
         return info
+
+    def checkpoint_save(self, path: str):
+        _chk(lib().impec_checkpoint_save(self.h, os.fsencode(path)), "checkpoint_save")
+
+    def checkpoint_load(self, path: str):
+        _chk(lib().impec_checkpoint_load(self.h, os.fsencode(path)), "checkpoint_load")
 
     def upload(self, c_host=None, q_host=None, ghost=2):
         import numpy as np

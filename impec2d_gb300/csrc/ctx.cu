@@ -149,6 +149,7 @@ static impec_status validate(const impec_params* P) {
 }
 
 impec_status impec_ctx_create(const impec_params* P, void* stream, impec_ctx** out) {
+    IMPEC_RANGE("impec_ctx_create");
     if (!P || !out) { set_error("null argument"); return IMPEC_ERR_ARG; }
     *out = nullptr;
     IMPEC_TRY(validate(P));

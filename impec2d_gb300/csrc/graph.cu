@@ -240,15 +240,25 @@ static impec_status step_stream(impec_ctx* ctx, double t_clip) {
     launch_k(ctx->stream, k_step_begin, 1, 1, 0, S);
     int cyc = 0;
     double rr = 0;
-    impec_status st = pressure_solve(ctx, ctx->c, ctx->p, ctx->P.eps, &cyc, &rr);
+    impec_status st;
+    {
+        IMPEC_RANGE("pressure");
+        st = pressure_solve(ctx, ctx->c, ctx->p, ctx->P.eps, &cyc, &rr);
+    }
     if (st != IMPEC_OK && st != IMPEC_ERR_NOT_CONVERGED) return st;
     if (st == IMPEC_ERR_NOT_CONVERGED) ctx->host_flags |= FLAG_MG_NOT_CONVERGED;
-    IMPEC_TRY(velocity(ctx, ctx->p, ctx->c, ctx->u, ctx->v));
-    IMPEC_TRY(max_stable_dt_dev(ctx, ctx->u, ctx->v));
+    {
+        IMPEC_RANGE("velocity and dt");
+        IMPEC_TRY(velocity(ctx, ctx->p, ctx->c, ctx->u, ctx->v));
+        IMPEC_TRY(max_stable_dt_dev(ctx, ctx->u, ctx->v));
+    }
     IMPEC_CUDA_TRY(cudaMemcpyAsync(&S->t_clip, &t_clip, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_clip_dt, 1, 1, 0, S);
-    IMPEC_TRY(hyperbolic_solve_dev(ctx, ctx->c, ctx->u, ctx->v, &S->dt, &ctx->prev_first_sweep));
+    {
+        IMPEC_RANGE("transport and dispersion");
+        IMPEC_TRY(hyperbolic_solve_dev(ctx, ctx->c, ctx->u, ctx->v, &S->dt, &ctx->prev_first_sweep));
+    }
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_advance, 1, 1, 0, S, 0LL, 0LL, 0LL, 0);
     IMPEC_LAUNCH_CHECK();
@@ -307,6 +317,7 @@ static void ensemble_free(impec_ensemble* e) {
 }
 
 extern "C" impec_status impec_ensemble_create(impec_ctx* const* members, int n, impec_ensemble** out) {
+    IMPEC_RANGE("impec_ensemble_create");
     if (!members || n < 1 || !out) return IMPEC_ERR_ARG;
     for (int i = 0; i < n; ++i) {
         if (!members[i]) return IMPEC_ERR_ARG;
@@ -384,6 +395,7 @@ extern "C" impec_status impec_ensemble_create(impec_ctx* const* members, int n, 
 }
 
 extern "C" impec_status impec_ensemble_step(impec_ensemble* e, int nsteps, int sync) {
+    IMPEC_RANGE("impec_ensemble_step");
     if (!e || nsteps < 0) return IMPEC_ERR_ARG;
     for (impec_ctx* c : e->m) {  // work queued on a member's own stream comes first
         IMPEC_CUDA_TRY(cudaEventRecord(e->done, c->stream));

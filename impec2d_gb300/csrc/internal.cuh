@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <string>
@@ -11,6 +12,19 @@
 #include "../../include/impec2d.h"
 
 namespace impec {
+
+// ---------------------------------------------------------------- NVTX ranges
+// A named range over a host call, seen by profilers that record NVTX (Nsight Systems, ncu
+// --nvtx); without such a tool attached a push or pop is a no-op.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define IMPEC_RANGE_CAT2(a, b) a##b
+#define IMPEC_RANGE_CAT(a, b) IMPEC_RANGE_CAT2(a, b)
+#define IMPEC_RANGE(name) ::impec::NvtxRange IMPEC_RANGE_CAT(impec_range_, __LINE__)(name)
 
 // ---------------------------------------------------------------- error handling
 void set_error(const std::string& msg);

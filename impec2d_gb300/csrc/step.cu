@@ -133,6 +133,7 @@ using namespace impec;
 extern "C" {
 
 impec_status impec_pressure_solve(impec_ctx* ctx, const double* c, double* p, double tol, int* cycles, double* relres) {
+    IMPEC_RANGE("impec_pressure_solve");
     if (!ctx || !c || !p) return IMPEC_ERR_ARG;
     impec_status s = pressure_solve(ctx, c, p, tol, cycles, relres);
     if (s == IMPEC_OK) IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -161,6 +162,7 @@ impec_status impec_pressure_apply(impec_ctx* ctx, const double* c, const double*
 }
 
 impec_status impec_velocity(impec_ctx* ctx, const double* p, const double* c, double* u, double* v) {
+    IMPEC_RANGE("impec_velocity");
     if (!ctx || !p || !c || !u || !v) return IMPEC_ERR_ARG;
     IMPEC_TRY(face_mobility(ctx, c));
     IMPEC_TRY(velocity(ctx, p, c, u, v));
@@ -205,6 +207,7 @@ impec_status impec_advect_y(impec_ctx* ctx, double* c, const double* v, double d
 }
 
 impec_status impec_advect_split(impec_ctx* ctx, double* c, const double* u, const double* v, double dt, int* pfs) {
+    IMPEC_RANGE("impec_advect_split");
     if (!ctx || !c || !u || !v || !pfs) return IMPEC_ERR_ARG;
     IMPEC_TRY(set_dt(ctx, dt));
     IMPEC_TRY(advect_split_dev(ctx, c, u, v, &ctx->dscal->dt, pfs));
@@ -214,6 +217,7 @@ impec_status impec_advect_split(impec_ctx* ctx, double* c, const double* u, cons
 
 impec_status impec_dispersion_cn(impec_ctx* ctx, double* c, const double* u, const double* v, double dt, double tol,
                                  int* its, double* relres) {
+    IMPEC_RANGE("impec_dispersion_cn");
     if (!ctx || !c || !u || !v) return IMPEC_ERR_ARG;
     IMPEC_TRY(set_dt(ctx, dt));
     impec_status s = dispersion_cn_dev(ctx, c, u, v, 1.0, &ctx->dscal->dt, tol, its, relres);
@@ -223,6 +227,7 @@ impec_status impec_dispersion_cn(impec_ctx* ctx, double* c, const double* u, con
 
 impec_status impec_hyperbolic_solve(impec_ctx* ctx, double* c, const double* u, const double* v, double dt, int* pfs,
                                     double* outflux) {
+    IMPEC_RANGE("impec_hyperbolic_solve");
     if (!ctx || !c || !u || !v || !pfs) return IMPEC_ERR_ARG;
     IMPEC_TRY(set_dt(ctx, dt));
     double z = outflux ? *outflux : 0.0;
@@ -247,12 +252,14 @@ impec_status impec_diagnostics(impec_ctx* ctx, const double* c, const double* u,
 }
 
 impec_status impec_step(impec_ctx* ctx, double t_clip, impec_step_info* info) {
+    IMPEC_RANGE("impec_step");
     if (!ctx) return IMPEC_ERR_ARG;
     impec_step_info tmp;
     return one_step(ctx, t_clip, info ? info : &tmp);
 }
 
 impec_status impec_run_steps(impec_ctx* ctx, int n, impec_step_info* info) {
+    IMPEC_RANGE("impec_run_steps");
     if (!ctx || n < 0) return IMPEC_ERR_ARG;
     for (int s = 0; s + 1 < n; ++s) IMPEC_TRY(one_step(ctx, -1.0, nullptr));
     if (n > 0 && info) return one_step(ctx, -1.0, info);
@@ -304,6 +311,7 @@ impec_status impec_pressure_upload(impec_ctx* ctx, const double* p_host, int g) 
 }
 
 impec_status impec_pressure_solve_resident(impec_ctx* ctx, int sync, int* cycles, double* relres) {
+    IMPEC_RANGE("impec_pressure_solve_resident");
     if (!ctx) return IMPEC_ERR_ARG;
     IMPEC_TRY(launch_pressure_graph(ctx));
     if (!sync) return IMPEC_OK;
@@ -335,6 +343,7 @@ impec_status impec_launch_count(impec_ctx* ctx, long long* n) {
 
 // Reference ghost layouts on the host <-> engine device layout.
 impec_status impec_state_upload(impec_ctx* ctx, const double* c_host, const double* q_host, int g) {
+    IMPEC_RANGE("impec_state_upload");
     if (!ctx || g < 0) return IMPEC_ERR_ARG;
     const int N1 = ctx->P.N1, N2 = ctx->P.N2, w = N2 + 2 * g;
     if (c_host) {  // interior rows straight from the ghosted host array (one strided copy)
@@ -350,6 +359,7 @@ impec_status impec_state_upload(impec_ctx* ctx, const double* c_host, const doub
 }
 
 impec_status impec_state_download(impec_ctx* ctx, double* c_host, double* p_host, double* v_host, int g) {
+    IMPEC_RANGE("impec_state_download");
     if (!ctx || g < 0) return IMPEC_ERR_ARG;
     const int N1 = ctx->P.N1, N2 = ctx->P.N2, w = N2 + 2 * g;
     auto get = [&](const double* dev, double* host) -> impec_status {  // interior rows, one strided copy
@@ -426,6 +436,7 @@ impec_status impec_get_tuning(impec_ctx* ctx, const char* name, long* value) {
 // context's current state for each candidate smoother schedule and cluster choice, keeps the
 // fastest, and leaves it set.  Every candidate still solves to the context's tolerance.
 impec_status impec_autotune(impec_ctx* ctx, int reps, char* report, int report_len) {
+    IMPEC_RANGE("impec_autotune");
     if (!ctx || reps < 1) return IMPEC_ERR_ARG;
     struct Cand { long pre, post, cluster; };
     const Cand cands[] = {{2, 2, 1}, {1, 1, 1}, {2, 1, 1}, {1, 2, 1}, {3, 3, 1}, {2, 2, 0}, {1, 1, 0}};
@@ -481,3 +492,108 @@ impec_status impec_autotune(impec_ctx* ctx, int reps, char* report, int report_l
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- checkpoint of the run
+// File layout (native byte order): a fixed header, then c and p (N1*N2 doubles each, row-major,
+// no ghost cells), u ((N1+1)*N2) and v (N1*(N2+1)).  The header's checksum is FNV-1a (64 bit)
+// over the payload bytes.  Everything a later step reads from the run is in it: the fields,
+// the clock and start time, the outflux accumulator of the mass balance, the step counter and
+// the sweep order of alternating splittings.
+struct CheckpointHeader {
+    char magic[8];  // "IMPECCK1"
+    int32_t version, n1, n2, prev_first_sweep;
+    int64_t steps;
+    double t, t0, total_outflux;
+    uint64_t checksum;
+};
+static const char kCkptMagic[8] = {'I', 'M', 'P', 'E', 'C', 'C', 'K', '1'};
+
+static uint64_t fnv1a(const void* data, size_t bytes, uint64_t h) {
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    for (size_t k = 0; k < bytes; ++k) h = (h ^ p[k]) * 1099511628211ull;
+    return h;
+}
+
+extern "C" impec_status impec_checkpoint_save(impec_ctx* ctx, const char* path) {
+    IMPEC_RANGE("impec_checkpoint_save");
+    if (!ctx || !path) return IMPEC_ERR_ARG;
+    const int N1 = ctx->P.N1, N2 = ctx->P.N2;
+    const size_t nc = (size_t)N1 * N2, nu = (size_t)(N1 + 1) * N2, nv = (size_t)N1 * (N2 + 1);
+    std::vector<double> buf(2 * nc + nu + nv);
+    IMPEC_TRY(sync_scalars(ctx));  // the clock and outflux as the last step left them
+    double* h = buf.data();
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(h, ctx->c, nc * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(h + nc, ctx->p, nc * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(h + 2 * nc, ctx->u, nu * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(h + 2 * nc + nu, ctx->v, nv * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    CheckpointHeader H;
+    std::memset(&H, 0, sizeof(H));
+    std::memcpy(H.magic, kCkptMagic, 8);
+    H.version = 1;
+    H.n1 = N1;
+    H.n2 = N2;
+    H.prev_first_sweep = ctx->prev_first_sweep;
+    H.steps = ctx->counter_steps;
+    H.t = ctx->hscal->t;
+    H.t0 = ctx->t0;
+    H.total_outflux = ctx->hscal->total_outflux;
+    H.checksum = fnv1a(h, buf.size() * 8, 1469598103934665603ull);
+    FILE* f = std::fopen(path, "wb");
+    if (!f) {
+        set_error(std::string("impec_checkpoint_save: cannot open ") + path);
+        return IMPEC_ERR_ARG;
+    }
+    const bool ok = std::fwrite(&H, sizeof(H), 1, f) == 1 && std::fwrite(h, 8, buf.size(), f) == buf.size();
+    if (std::fclose(f) != 0 || !ok) {
+        set_error(std::string("impec_checkpoint_save: write failed: ") + path);
+        return IMPEC_ERR_ARG;
+    }
+    return IMPEC_OK;
+}
+
+extern "C" impec_status impec_checkpoint_load(impec_ctx* ctx, const char* path) {
+    IMPEC_RANGE("impec_checkpoint_load");
+    if (!ctx || !path) return IMPEC_ERR_ARG;
+    if (ctx->ensembles > 0) {  // an ensemble's graph reads this context's clock from the device
+        set_error("impec_checkpoint_load: the context is a member of a live ensemble");
+        return IMPEC_ERR_ARG;
+    }
+    const int N1 = ctx->P.N1, N2 = ctx->P.N2;
+    const size_t nc = (size_t)N1 * N2, nu = (size_t)(N1 + 1) * N2, nv = (size_t)N1 * (N2 + 1);
+    FILE* f = std::fopen(path, "rb");
+    if (!f) {
+        set_error(std::string("impec_checkpoint_load: cannot open ") + path);
+        return IMPEC_ERR_ARG;
+    }
+    CheckpointHeader H;
+    std::vector<double> buf(2 * nc + nu + nv);
+    bool ok = std::fread(&H, sizeof(H), 1, f) == 1 && std::memcmp(H.magic, kCkptMagic, 8) == 0 && H.version == 1 &&
+              H.n1 == N1 && H.n2 == N2;
+    ok = ok && std::fread(buf.data(), 8, buf.size(), f) == buf.size();
+    std::fclose(f);
+    if (!ok) {
+        set_error(std::string("impec_checkpoint_load: not a checkpoint of a ") + std::to_string(N1) + "x" +
+                  std::to_string(N2) + " run: " + path);
+        return IMPEC_ERR_ARG;
+    }
+    if (fnv1a(buf.data(), buf.size() * 8, 1469598103934665603ull) != H.checksum) {
+        set_error(std::string("impec_checkpoint_load: checksum mismatch: ") + path);
+        return IMPEC_ERR_ARG;
+    }
+    const double* h = buf.data();
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->c, h, nc * 8, cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->p, h + nc, nc * 8, cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->u, h + 2 * nc, nu * 8, cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(ctx->v, h + 2 * nc + nu, nv * 8, cudaMemcpyHostToDevice, ctx->stream));
+    const double clock[2] = {H.t, H.total_outflux};
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(&ctx->dscal->t, &clock[0], 8, cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaMemcpyAsync(&ctx->dscal->total_outflux, &clock[1], 8, cudaMemcpyHostToDevice, ctx->stream));
+    IMPEC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // the host buffers above go out of scope
+    ctx->t = H.t;
+    ctx->t0 = H.t0;
+    ctx->total_outflux = H.total_outflux;
+    ctx->counter_steps = (int)H.steps;
+    ctx->prev_first_sweep = H.prev_first_sweep;
+    return IMPEC_OK;
+}

@@ -160,6 +160,14 @@ impec_status impec_step(impec_ctx* ctx, double t_clip, impec_step_info* info);
 /* n steps with no host synchronisation between them (dt stays on the device; info of the
  * last step is returned).  Used by throughput runs. */
 impec_status impec_run_steps(impec_ctx* ctx, int n, impec_step_info* info);
+/* Binary checkpoint of the resident run, for restarts that continue bit for bit: c, p, u, v,
+ * the clock, start time, outflux accumulator, step counter and sweep order.  No counterpart in
+ * the reference, which restarts only from an init_file of c (Impec2DSolver::Init,
+ * src/Impec2DSolver.cpp:194-220; supported by the .cfg path).  Load checks the grid size, the
+ * format and a checksum (IMPEC_ERR_ARG with a message otherwise) and is refused while the
+ * context is a member of a live ensemble.  Both wait for the context's stream. */
+impec_status impec_checkpoint_save(impec_ctx* ctx, const char* path);
+impec_status impec_checkpoint_load(impec_ctx* ctx, const char* path);
 
 /* Pressure solve of the resident state (c -> p) as one CUDA graph (no host round trip per
  * cycle).  With sync = 0 the call only enqueues; cycles/relres are then not written. */
