@@ -151,10 +151,11 @@ struct Tuning {
     long rb_resid = 1;  // five-point levels: restriction sums the red residuals only (black ones are ~0)
     // FP64 five-point levels of at least this many cells sweep both colours in one launch
     // (k_rb_tile, ping-pong iterate): every coefficient is read once per sweep instead of once
-    // per colour, which pays where the level streams from HBM (4096^2 sweep 199 against 240 us
-    // cold, solve 16.9 against 17.9 ms) and costs where it sits in L2 (1024^2 and 2048^2 solves
-    // 10% and 3% slower: the recomputed ring and one more dependent phase); 0 disables
-    long tile_cells = 1L << 23;
+    // per colour, which pays where the level streams from HBM (4096^2 sweep 185 against 240 us
+    // cold; 4096^2 solve 17.9 ms with 2048^2 and 4096^2 levels so swept, 18.0 with 4096^2
+    // alone, 19.7 with none) and costs where it sits in L2 (1024^2 solve 2.23 against 2.08 ms
+    // with every level so swept: the recomputed ring and one more dependent phase); 0 disables
+    long tile_cells = 1L << 22;
 };
 }  // namespace impec
 

@@ -8,18 +8,6 @@
 
 constexpr int MGC_MAXL = 8;
 
-// Asynchronous copy of one element, global -> this CTA's shared memory (cp.async of 4 or 8
-// bytes: any element-aligned address qualifies).  A staging loop issues all of its copies
-// before one cp.async.wait_all, instead of one global-load round trip per element.
-template <class T>
-__device__ __forceinline__ void stage_async(T* dst, const T* src) {
-    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "cp.async element");
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src),
-                 "n"(sizeof(T))
-                 : "memory");
-}
-__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
 // Coarsest-level solve x = Dinv b' in FP64 (n <= 64), b' = b with b(0) := 0 for the singular
 // system (whose Dinv, from k_dense_invert, already removes the mean of the result).  Every
 // thread of the block takes part (the count of loop trips and shuffles is the same for all):

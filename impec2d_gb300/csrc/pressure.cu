@@ -464,6 +464,18 @@ __global__ void k_rb_zero(int n1, int n2, const T* __restrict__ idiag, const T* 
 // sectors.  Per-cell arithmetic and its order equal k_rb_face5's, so the result is the same bit
 // for bit.  ZERO: the sweep starts from x = 0 (as k_rb_zero), so phase 1 is x = b * idiag and
 // x_in is not read.
+// Asynchronous copy of one element, global -> this CTA's shared memory (cp.async of 4 or 8
+// bytes: any element-aligned address qualifies).  A staging loop issues all of its copies
+// before one cp.async.wait_all, instead of one global-load round trip per element.
+template <class T>
+__device__ __forceinline__ void stage_async(T* dst, const T* src) {
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "cp.async element");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src),
+                 "n"(sizeof(T))
+                 : "memory");
+}
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 constexpr int TILE_R = 32, TILE_C = 64, TILE_THREADS = 256;
 constexpr int TILE_W = TILE_C + 4;  // shared row width: columns j0-2 .. j0+TILE_C+1
 
@@ -476,11 +488,13 @@ __global__ void __launch_bounds__(TILE_THREADS) k_rb_tile(int n1, int n2, const 
     __shared__ T sx[(TILE_R + 4) * TILE_W];  // rows i0-2 .. i0+TILE_R+1
     const int i0 = blockIdx.y * TILE_R, j0 = blockIdx.x * TILE_C, t = threadIdx.x;
     auto S = [&](int i, int j) -> T& { return sx[(i - i0 + 2) * TILE_W + (j - j0 + 2)]; };
-    if (!ZERO) {
+    if (!ZERO) {  // the iterate tile: every element copy in flight at once
         for (int k = t; k < (TILE_R + 4) * TILE_W; k += TILE_THREADS) {
             const int i = i0 - 2 + k / TILE_W, j = j0 - 2 + k % TILE_W;
-            sx[k] = (i >= 0 && i < n1 && j >= 0 && j < n2) ? x_in[IX(i, j, n2)] : T(0);
+            if (i >= 0 && i < n1 && j >= 0 && j < n2) stage_async(sx + k, x_in + IX(i, j, n2));
+            else sx[k] = T(0);
         }
+        stage_wait();
         __syncthreads();
     }
     // phase 1: colour `first` on rows i0-1 .. i0+TILE_R, columns j0-1 .. j0+TILE_C
