@@ -191,6 +191,8 @@ def roofline_probe(ctx, P, precision: str, flush=None, peaks_path: str | None = 
             pass
     ach = b / (ms * 1e-3) / 1e9
     tile = ctx.get_tuning("tile_cells")
+    if which == 1:
+        tile = ctx.get_tuning("tile_cells32")
     one_launch = tile > 0 and P.N1 * P.N2 >= tile
     t = "double" if which == 0 else "float"
     name = (f"k_rb_tile<{t}> (fine red-black sweep, both colours in one launch)" if one_launch

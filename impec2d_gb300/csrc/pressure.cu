@@ -896,6 +896,7 @@ impec_status pressure_alloc(impec_ctx* ctx) {
         T.rb_skip = env_long("IMPEC_MG_RB_SKIP", T.rb_skip);
         T.rb_resid = env_long("IMPEC_MG_RB_RESID", T.rb_resid);
         T.tile_cells = env_long("IMPEC_MG_TILE_CELLS", T.tile_cells);
+        T.tile_cells32 = env_long("IMPEC_MG_TILE_CELLS32", T.tile_cells32);
         ctx->cn_predict = env_long("IMPEC_CN_PREDICT", 1) != 0;
         if (ctx->dir_row >= 0) {
             IMPEC_CUDA_TRY(cudaMalloc((void**)&ctx->dmask, nf));
@@ -1086,8 +1087,9 @@ void swap_iterate<float>(Level& Lv) { std::swap(Lv.x32, Lv.xa32); }
 template <class T>
 static bool use_tile(impec_ctx* ctx, size_t l) {
     Level& Lv = ctx->L[l];
-    return sizeof(T) == 8 && ctx->tune.tile_cells > 0 && Lv.kind == FACE5 && Lv.n() >= (size_t)ctx->tune.tile_cells &&
-           (ctx->krylov || l > 0) && level_alt<T>(Lv) != nullptr;
+    const long cells = sizeof(T) == 8 ? ctx->tune.tile_cells : ctx->tune.tile_cells32;
+    return cells > 0 && Lv.kind == FACE5 && Lv.n() >= (size_t)cells && (ctx->krylov || l > 0) &&
+           level_alt<T>(Lv) != nullptr;
 }
 
 // Grid of the red-black kernels (k_rb_face5, k_rb_zero, k_prolong_rb): RB_ROWS rows and two

@@ -391,7 +391,8 @@ static long* tuning_field(impec_ctx* ctx, const char* name) {
     struct { const char* n; long* v; } tab[] = {
         {"mg_pre", &t.pre},          {"mg_post", &t.post},         {"cluster", &t.cluster},
         {"cluster_cells", &t.cl_cells}, {"cluster_cta0", &t.cl_cta0}, {"coarse_cells64", &t.coarse_cells64},
-        {"coarse_cells32", &t.coarse_cells32}, {"tile_cells", &t.tile_cells}};
+        {"coarse_cells32", &t.coarse_cells32}, {"tile_cells", &t.tile_cells},
+        {"tile_cells32", &t.tile_cells32}};
     for (auto& e : tab)
         if (!strcmp(e.n, name)) return e.v;
     return nullptr;

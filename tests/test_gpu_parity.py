@@ -752,6 +752,7 @@ def test_one_launch_sweep_matches_two_launch_sweeps(engine, monkeypatch, N1, N2,
     out = []
     for tile in ("0", "1"):
         monkeypatch.setenv("IMPEC_MG_TILE_CELLS", tile)
+        monkeypatch.setenv("IMPEC_MG_TILE_CELLS32", tile)
         P, ctx = _ctx(E, N1, N2, nu=1.0, stype=stype, precision=prec, max_cycles=200)
         OP = oparams(P)
         q = source(OP)
