@@ -1,9 +1,11 @@
 // Cluster V-cycle (included by pressure.cu inside namespace impec).
 //
-// The coarse levels of one V-cycle (<= 128^2 cells by default, five-point operators) in a
-// single launch of one thread-block cluster of up to 16 CTAs.  Each CTA keeps a band of rows
-// of every level -- faces, 1/diagonal, diagonal, iterate, right-hand side -- in its shared
-// memory.  A stencil reads the row above or below its band from the neighbouring CTA's shared
+// The coarse levels of one V-cycle (<= 128^2 cells by default) in a single launch of one
+// thread-block cluster of up to 16 CTAs.  Each CTA keeps a band of rows of every level in its
+// shared memory: for five-point operators the faces, 1/diagonal, diagonal, iterate and
+// right-hand side; for nine-point ones (nu < 1) the nine coefficient planes, 1/diagonal,
+// iterate and right-hand side, smoothed by four-colour Gauss-Seidel (the arithmetic of
+// k_gs4_exp9).  A stencil reads the row above or below its band from the neighbouring CTA's shared
 // memory (distributed shared memory), and the phases of the cycle (one colour of a sweep, the
 // restriction, the prolongation) are separated by cluster barriers.  The smallest levels
 // (<= 256 cells by default) and the dense coarsest solve run on CTA 0 alone, with block
@@ -26,11 +28,14 @@
 constexpr int CL_MAXL = 10;
 constexpr int CL_THREADS = 512;
 constexpr int CL_MAX_CTAS = 16;
+// shared arrays of a level; a nine-point level keeps its nine planes at CL_TX (plane stride
+// rows * n2) and has no CL_TY / CL_DG (the diagonal is plane 0)
 enum { CL_TX = 0, CL_TY, CL_ID, CL_DG, CL_X, CL_B };
 
 template <class T>
 struct ClusterArgs {
-    int nl;  // levels handled: 0 .. nl-1 (nl-1 is the dense coarsest level)
+    int kind;  // FACE5 or EXP9 (every level of the cycle)
+    int nl;    // levels handled: 0 .. nl-1 (nl-1 is the dense coarsest level)
     int nd;  // levels 0 .. nd-1 are spread over the cluster; nd .. nl-1 live on CTA 0
     int singular, dn;
     int pre, post;  // smoother sweeps before / after the coarse correction
@@ -42,6 +47,7 @@ struct ClusterArgs {
     const T* ty[CL_MAXL];
     const T* id[CL_MAXL];
     const T* dg[CL_MAXL];
+    const T* a9[CL_MAXL];  // nine-point planes (EXP9)
     T* x0;        // iterate of level 0 (global), read at the start and written at the end
     const T* b0;  // right-hand side of level 0 (global)
     const double* dinv;
@@ -102,6 +108,49 @@ __device__ void cl_sweep(const cooperative_groups::cluster_group& cl, T* sm, int
     }
 }
 
+// One colour (ci, cj) = (col >> 1, col & 1) of a four-colour Gauss-Seidel sweep of a
+// nine-point level on the band: s = b - sum_e a_e x_e over the neighbours in c_off order,
+// x = s * idiag (the arithmetic of k_gs4_exp9).  Bands start on even rows, so a band row's
+// parity is its global row's.
+template <class T>
+__device__ void cl_sweep9(const cooperative_groups::cluster_group& cl, T* sm, int rank, const ClusterArgs<T>& A,
+                          int l, int col) {
+    int lo, cnt;
+    cl_band(A, l, rank, lo, cnt);
+    if (cnt == 0) return;
+    const int n1 = A.n1[l], n2 = A.n2[l], ci = col >> 1, cj = col & 1;
+    const size_t ps = (size_t)A.rows[l] * n2;  // plane stride of the staged band
+    T* x = sm + A.off[l][CL_X];
+    const T* b = sm + A.off[l][CL_B];
+    const T* id = sm + A.off[l][CL_ID];
+    const T* a9 = sm + A.off[l][CL_TX];
+    const T* xup = lo > 0 ? cl_row(cl, sm, rank, A, l, CL_X, lo - 1, n2) : nullptr;
+    const T* xdn = lo + cnt < n1 ? cl_row(cl, sm, rank, A, l, CL_X, lo + cnt, n2) : nullptr;
+    const int nr = (cnt - ci + 1) / 2, nc = (n2 - cj + 1) / 2;
+    for (int k = threadIdx.x; k < nr * nc; k += blockDim.x) {
+        const int li = ci + 2 * (k / nc), j = cj + 2 * (k % nc), i = lo + li, c = li * n2 + j;
+        T o = 0;
+#pragma unroll
+        for (int e = 1; e < 9; ++e) {
+            const int ii = i + c_off[e][0], jj = j + c_off[e][1];
+            if (ii < 0 || ii >= n1 || jj < 0 || jj >= n2) continue;
+            const T xv = ii < lo ? xup[jj] : (ii >= lo + cnt ? xdn[jj] : x[(ii - lo) * n2 + jj]);
+            o += a9[e * ps + c] * xv;
+        }
+        x[c] = (b[c] - o) * id[c];
+    }
+}
+
+// The s-th colour launch of a smoothing pass (s counts colours over all its sweeps): five-point
+// colours alternate 0, 1 (post: 1, 0); nine-point ones run 0..3 (post: 3..0).  zero: the first
+// colour of a five-point pass from x = 0.
+template <class T>
+__device__ void cl_colour(const cooperative_groups::cluster_group& cl, T* sm, int rank, const ClusterArgs<T>& A,
+                          int l, int s, bool post, bool zero) {
+    if (A.kind == FACE5) cl_sweep(cl, sm, rank, A, l, post ? 1 - (s & 1) : (s & 1), zero);
+    else cl_sweep9(cl, sm, rank, A, l, post ? 3 - (s & 3) : (s & 3));
+}
+
 // Residual of the band summed over 2x2 aggregates into the coarse right-hand side (owned by
 // whichever CTA holds the coarse row); coarse iterate := 0.  The arithmetic of k_restrict.
 template <class T>
@@ -116,6 +165,7 @@ __device__ void cl_restrict(const cooperative_groups::cluster_group& cl, T* sm, 
     const T* tx = sm + A.off[l][CL_TX];
     const T* ty = sm + A.off[l][CL_TY];
     const T* dg = sm + A.off[l][CL_DG];
+    const size_t ps = (size_t)A.rows[l] * n2;  // nine-point plane stride
     const T* xup = lo > 0 ? cl_row(cl, sm, rank, A, l, CL_X, lo - 1, n2) : nullptr;
     const T* xdn = lo + cnt < n1 ? cl_row(cl, sm, rank, A, l, CL_X, lo + cnt, n2) : nullptr;
     const int I0 = lo >> 1, I1 = (lo + cnt + 1) >> 1;
@@ -128,11 +178,21 @@ __device__ void cl_restrict(const cooperative_groups::cluster_group& cl, T* sm, 
                 if (i >= n1 || j >= n2 || ((i + j) & 1) == A.zero_color) continue;  // as k_restrict
                 const int li = i - lo, c = li * n2 + j;
                 T r = b[c];
-                if (i > 0) r += tx[c] * (li > 0 ? x[c - n2] : xup[j]);
-                if (i < n1 - 1) r += tx[c + n2] * (li + 1 < cnt ? x[c + n2] : xdn[j]);
-                if (j > 0) r += ty[li * (n2 + 1) + j] * x[c - 1];
-                if (j < n2 - 1) r += ty[li * (n2 + 1) + j + 1] * x[c + 1];
-                s += r - dg[c] * x[c];
+                if (A.kind == FACE5) {
+                    if (i > 0) r += tx[c] * (li > 0 ? x[c - n2] : xup[j]);
+                    if (i < n1 - 1) r += tx[c + n2] * (li + 1 < cnt ? x[c + n2] : xdn[j]);
+                    if (j > 0) r += ty[li * (n2 + 1) + j] * x[c - 1];
+                    if (j < n2 - 1) r += ty[li * (n2 + 1) + j + 1] * x[c + 1];
+                    s += r - dg[c] * x[c];
+                } else {  // as resid() for nine-point operators: r = b - sum a_e x_e - a_0 x
+                    for (int e = 1; e < 9; ++e) {
+                        const int ii = i + c_off[e][0], jj = j + c_off[e][1];
+                        if (ii < 0 || ii >= n1 || jj < 0 || jj >= n2) continue;
+                        const T xv = ii < lo ? xup[jj] : (ii >= lo + cnt ? xdn[jj] : x[(ii - lo) * n2 + jj]);
+                        r -= tx[e * ps + c] * xv;
+                    }
+                    s += r - tx[c] * x[c];
+                }
             }
         cl_row(cl, sm, rank, A, l + 1, CL_B, I, c2)[J] = s;
         cl_row(cl, sm, rank, A, l + 1, CL_X, I, c2)[J] = T(0);
@@ -187,13 +247,21 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
         T* ty = sm + A.off[l][CL_TY];
         T* id = sm + A.off[l][CL_ID];
         T* dg = sm + A.off[l][CL_DG];
-        for (int k = threadIdx.x; k < (cnt + 1) * n2; k += blockDim.x)
-            stage_async(tx + k, A.tx[l] + (size_t)lo * n2 + k);
-        for (int k = threadIdx.x; k < cnt * (n2 + 1); k += blockDim.x)
-            stage_async(ty + k, A.ty[l] + (size_t)lo * (n2 + 1) + k);
-        for (int k = threadIdx.x; k < cnt * n2; k += blockDim.x) {
-            stage_async(id + k, A.id[l] + (size_t)lo * n2 + k);
-            stage_async(dg + k, A.dg[l] + (size_t)lo * n2 + k);
+        if (A.kind == FACE5) {
+            for (int k = threadIdx.x; k < (cnt + 1) * n2; k += blockDim.x)
+                stage_async(tx + k, A.tx[l] + (size_t)lo * n2 + k);
+            for (int k = threadIdx.x; k < cnt * (n2 + 1); k += blockDim.x)
+                stage_async(ty + k, A.ty[l] + (size_t)lo * (n2 + 1) + k);
+            for (int k = threadIdx.x; k < cnt * n2; k += blockDim.x) {
+                stage_async(id + k, A.id[l] + (size_t)lo * n2 + k);
+                stage_async(dg + k, A.dg[l] + (size_t)lo * n2 + k);
+            }
+        } else if (l + 1 < A.nl) {  // nine planes and 1/diagonal (the dense level needs neither)
+            const size_t ps = (size_t)A.rows[l] * n2, n = (size_t)A.n1[l] * n2;
+            for (int e = 0; e < 9; ++e)
+                for (int k = threadIdx.x; k < cnt * n2; k += blockDim.x)
+                    stage_async(tx + e * ps + k, A.a9[l] + e * n + (size_t)lo * n2 + k);
+            for (int k = threadIdx.x; k < cnt * n2; k += blockDim.x) stage_async(id + k, A.id[l] + (size_t)lo * n2 + k);
         }
         if (l == 0) {
             T* x = sm + A.off[0][CL_X];
@@ -211,9 +279,10 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
     stage_wait();
     cl.sync();
     // down: levels spread over the cluster
+    const int ncol = A.kind == FACE5 ? 2 : 4;
     for (int l = 0; l < A.nd; ++l) {
-        for (int s = 0; s < 2 * A.pre; ++s) {
-            cl_sweep(cl, sm, rank, A, l, s & 1, A.rb_skip && s == 0 && l > 0);
+        for (int s = 0; s < ncol * A.pre; ++s) {
+            cl_colour(cl, sm, rank, A, l, s, false, A.rb_skip && s == 0 && l > 0);
             cl.sync();
         }
         cl_restrict(cl, sm, rank, A, l);
@@ -222,8 +291,8 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
     // the small levels and the dense solve on CTA 0
     if (rank == 0) {
         for (int l = A.nd; l < A.nl - 1; ++l) {
-            for (int s = 0; s < 2 * A.pre; ++s) {
-                cl_sweep(cl, sm, 0, A, l, s & 1, A.rb_skip && s == 0 && l > 0);
+            for (int s = 0; s < ncol * A.pre; ++s) {
+                cl_colour(cl, sm, 0, A, l, s, false, A.rb_skip && s == 0 && l > 0);
                 __syncthreads();
             }
             cl_restrict(cl, sm, 0, A, l);
@@ -235,8 +304,8 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
         for (int l = A.nl - 2; l >= A.nd; --l) {
             cl_prolong(cl, sm, 0, A, l);
             __syncthreads();
-            for (int s = 0; s < 2 * A.post; ++s) {
-                cl_sweep(cl, sm, 0, A, l, 1 - (s & 1));
+            for (int s = 0; s < ncol * A.post; ++s) {
+                cl_colour(cl, sm, 0, A, l, s, true, false);
                 __syncthreads();
             }
         }
@@ -246,8 +315,8 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster_vcycle(const __grid_cons
     for (int l = A.nd - 1; l >= 0; --l) {
         cl_prolong(cl, sm, rank, A, l);
         cl.sync();
-        for (int s = 0; s < 2 * A.post; ++s) {
-            cl_sweep(cl, sm, rank, A, l, 1 - (s & 1));
+        for (int s = 0; s < ncol * A.post; ++s) {
+            cl_colour(cl, sm, rank, A, l, s, true, false);
             cl.sync();
         }
     }

@@ -70,15 +70,15 @@ __device__ void cv_smooth(int n1, int n2, const T* tx, const T* ty, const T* a9,
                     if (j > 0) sm += ty[IX(i, j, n2 + 1)] * x[k - 1];
                     if (j < n2 - 1) sm += ty[IX(i, j + 1, n2 + 1)] * x[k + 1];
                     x[k] = sm * id[k];
-                } else {
+                } else {  // as k_gs4_exp9: s = b - sum_e a_e x_e, x = s * idiag
                     if ((((i & 1) << 1) | (j & 1)) != col) continue;
-                    T sm = b[k];
+                    T o = 0;
                     for (int e = 1; e < 9; ++e) {
                         int ii = i + c_off[e][0], jj = j + c_off[e][1];
                         if (ii < 0 || ii >= n1 || jj < 0 || jj >= n2) continue;
-                        sm -= a9[e * n + k] * x[IX(ii, jj, n2)];
+                        o += a9[e * n + k] * x[IX(ii, jj, n2)];
                     }
-                    x[k] = sm * id[k];
+                    x[k] = (b[k] - o) * id[k];
                 }
             }
             __syncthreads();

@@ -799,7 +799,7 @@ __global__ void k_apply_ref(Level F, const double* __restrict__ x, int pin, int 
 #include "mgcluster.cuh"
 
 constexpr size_t MG_COARSE_SMEM = 160 * 1024;
-constexpr size_t MG_CLUSTER_SMEM = 160 * 1024;
+constexpr size_t MG_CLUSTER_SMEM = 200 * 1024;
 
 // CTAs per cluster for k_cluster_vcycle: 16 where the device can co-schedule such a cluster
 // with the kernel's shared memory, else 8, else 0 (the per-level path is used).
@@ -1208,7 +1208,7 @@ static void launch_coarse(impec_ctx* ctx, size_t lc) {
 
 // Layout of the cluster V-cycle over levels ls .. L-1: which levels are spread over the cluster
 // (a prefix of at least one level above the CTA-0 threshold), each CTA's band height and the
-// shared-memory offsets.  False when the levels do not fit the kernel (nine-point operators,
+// shared-memory offsets.  False when the levels do not fit the kernel (operators of two kinds,
 // too many levels, too much shared memory, a coarsest level above CL_THREADS cells).
 template <class T>
 static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& smem) {
@@ -1217,19 +1217,20 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
     if (CS < 2 || nl < 2 || nl > (size_t)CL_MAXL || ctx->dense_n > CL_THREADS) return false;
     const long cta0 = ctx->tune.cl_cta0;
     A = ClusterArgs<T>{};
+    A.kind = ctx->L[ls].kind;
     A.nl = (int)nl;
     A.singular = ctx->singular;
     A.pre = (int)ctx->tune.pre;
     A.post = (int)ctx->tune.post;
     A.zero_color = restrict_zero_color(ctx, ctx->L[ls]);
-    A.rb_skip = ctx->tune.rb_skip != 0 && ctx->tune.pre >= 1 && ctx->tune.post >= 1 ? 1 : 0;
+    A.rb_skip = A.kind == FACE5 && ctx->tune.rb_skip != 0 && ctx->tune.pre >= 1 && ctx->tune.post >= 1 ? 1 : 0;
     A.dn = ctx->dense_n;
     A.dinv = ctx->dense_inv;
     size_t off = 0;
     int nd = 0;
     for (size_t k = 0; k < nl; ++k) {
         Level& Lv = ctx->L[ls + k];
-        if (Lv.kind != FACE5) return false;
+        if (Lv.kind != A.kind) return false;
         int R = Lv.n1;
         if (k + 1 < nl && nd == (int)k && (long)Lv.n() > cta0) {
             R = (Lv.n1 + CS - 1) / CS;
@@ -1240,7 +1241,9 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
         A.n2[k] = Lv.n2;
         A.rows[k] = R;
         const size_t n2 = (size_t)Lv.n2, r = (size_t)R;
-        const size_t sz[6] = {(r + 1) * n2, r * (n2 + 1), r * n2, r * n2, r * n2, r * n2};
+        const size_t ops = k + 1 < nl ? r * n2 : 0;  // nine-point: the dense level keeps x and b only
+        const size_t sz[6] = {A.kind == FACE5 ? (r + 1) * n2 : 9 * ops, A.kind == FACE5 ? r * (n2 + 1) : 0,
+                              A.kind == FACE5 ? r * n2 : ops, A.kind == FACE5 ? r * n2 : 0, r * n2, r * n2};
         for (int a = 0; a < 6; ++a) {
             A.off[k][a] = (unsigned)off;
             off += sz[a];
@@ -1252,6 +1255,7 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
         A.ty[k] = ty;
         A.id[k] = id;
         A.dg[k] = level_diag<T>(Lv);
+        A.a9[k] = a9;
         if (k == 0) {
             A.x0 = x;
             A.b0 = b;
@@ -1268,6 +1272,10 @@ static bool cluster_plan(impec_ctx* ctx, size_t ls, ClusterArgs<T>& A, size_t& s
 template <class T>
 static size_t cluster_start(impec_ctx* ctx) {
     if (ctx->cl_size < 2 || ctx->tune.cluster == 0) return SIZE_MAX;
+    // FP32 nine-point cycles keep their per-level and single-CTA kernels: each level's four
+    // colours are cheap launches there, and ten cluster-barrier phases per level cost more
+    // (mixed solve at 1024^2, nu = 2/3: 5.10 ms with the cluster against 4.76 ms without)
+    if (sizeof(T) == 4 && ctx->L[0].kind != FACE5) return SIZE_MAX;
     const long cells = ctx->tune.cl_cells;
     ClusterArgs<T> A;
     size_t smem;
