@@ -19,7 +19,8 @@ __constant__ int d_off[9][2] = {{0, 0}, {-1, 0}, {-1, -1}, {0, -1}, {1, -1}, {1,
 
 struct PeaceArgs {
     int n1, n2;
-    double phi, al, at, phiDm;
+    double phi_al, phi_at, phiDm;  // phi * alpha_l, phi * alpha_t (the products the kernel would
+                                   // form first), phi * Dm
     int guard;
 };
 
@@ -38,7 +39,7 @@ __global__ void k_peaceman(PeaceArgs A, const double* __restrict__ u, const doub
                               v[IX(i0, j, n2 + 1)]);
         double u2 = uu * uu, v2 = vv * vv;
         double inv = rsqrt(u2 + v2);  // 1/|u|
-        double fl = A.phi * A.al * inv, ft = A.phi * A.at * inv;
+        double fl = A.phi_al * inv, ft = A.phi_at * inv;
         if (A.guard && u2 + v2 == 0) fl = ft = 0;
         double d11 = fl * u2 + ft * v2;
         double d12 = fl * (uu * vv) + ft * (-uu * vv);
@@ -53,7 +54,7 @@ __global__ void k_peaceman(PeaceArgs A, const double* __restrict__ u, const doub
         double vv = v[IX(i, j, n2 + 1)];
         double u2 = uu * uu, v2 = vv * vv;
         double inv = rsqrt(u2 + v2);
-        double fl = A.phi * A.al * inv, ft = A.phi * A.at * inv;
+        double fl = A.phi_al * inv, ft = A.phi_at * inv;
         if (A.guard && u2 + v2 == 0) fl = ft = 0;
         double d21 = fl * (uu * vv) + ft * (-uu * vv);
         double d22 = fl * v2 + ft * u2;
@@ -261,7 +262,8 @@ impec_status cn_setup(impec_ctx* ctx, const double* u, const double* v, double d
     const int n1 = P.N1, n2 = P.N2;
     const Geo& G = ctx->G;
     const double maxdx = G.dx > G.dy ? G.dx : G.dy;
-    PeaceArgs pa{n1, n2, P.porosity, P.alpha_l * maxdx, P.alpha_t * maxdx, P.porosity * P.Dm, P.peaceman_guard};
+    PeaceArgs pa{n1, n2, P.porosity * (P.alpha_l * maxdx), P.porosity * (P.alpha_t * maxdx), P.porosity * P.Dm,
+                 P.peaceman_guard};
     dim3 b(DBX, DBY);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_peaceman, dim3((n2 + 1 + DBX - 1) / DBX, (n1 + 1 + DBY - 1) / DBY), b, 0, pa, u, v, ctx->dfx,
