@@ -7,6 +7,8 @@ tests/test_oracle_golden.py pin bit for bit to the reference's own code).
     developed, fingered concentration field: velocities of the same pressure 1e-13, the split advection
     1e-13, the CN half step 1e-11, the pressure's relative residual under the oracle's matrix
     <= 2 tol, and c after the whole step (measured errors recorded in the assertions);
+  * the other transport schemes (upwind, WAF split, WAF, CTU) at 1024^2: one advection step of
+    the developed state, both sweep orders, to 1e-13;
   * the reference's CPU case (128^2 diagonal quarter-five-spot, first-order upwind, porosity
     0.2, M = 41) to t = 0.06 (0.3 pore volumes), engine and oracle in lockstep, compared by
     integrated quantities (time steps, produced volume, mass balance);
@@ -132,6 +134,36 @@ def test_developed_state_step_at_1024(engine, oracle_lib, nu):
           f"cycles); one whole step: dt {abs(info.dt - S.dt) / S.dt:.2e}, c {err_c:.2e}, p {err_pp:.2e}")
     assert abs(info.dt - S.dt) <= 1e-8 * S.dt
     assert err_c <= 1e-9 and err_pp <= 1e-8, (err_c, err_pp)
+    ctx.close()
+
+
+@pytest.mark.parametrize("scheme", [0, 1, 2, 3])  # upwind, WAF split, WAF, CTU (MUSCL: the test above)
+@pytest.mark.parametrize("mode", [4, 1])  # symmetric-parallel, x first
+def test_transport_schemes_at_1024(engine, oracle_lib, scheme, mode):
+    """The other transport schemes at the benchmark's size: one advection step of the developed
+    fingered state with the Darcy velocities of a smooth pressure (a consistent field), each
+    sweep order, against the oracle to 1e-13."""
+    E = engine
+    N = 1024
+    P = E.default_params(N, N, stype=E.PARALLEL, x_ub=2 ** 0.5, y_ub=2 ** 0.5, hmtype=scheme, dim_splitting=mode,
+                         porosity=0.7)
+    OP = oparams(P)
+    c0 = fingered(N, 11)
+    cg = cell_ghost(OP, c0)
+    p = 0.05 * grf(N, 48, 12)
+    vg = np.zeros(O.vel_shape(OP))
+    oracle_lib.or_calc_velocities(C.byref(OP), O.ptr(cell_ghost(OP, p)), O.ptr(vg), O.ptr(cg))
+    u, v = vel_split(OP, vg)
+    dt = 0.9 * oracle_lib.or_max_stable_advection_dt(C.byref(OP), O.ptr(vg)) * OP.porosity
+    ctx = E.Context(P)
+    for pfs0 in (0, 1):
+        co = cg.copy()
+        pfs = C.c_int(pfs0)
+        oracle_lib.or_advect_split(C.byref(OP), O.ptr(co), O.ptr(vg), dt, C.byref(pfs))
+        dc = dev(c0)
+        assert ctx.advect_split(dc, dev(u), dev(v), dt, pfs0) == pfs.value
+        err = rel_err(host(dc), O.interior(OP, co))
+        assert err <= 1e-13, (pfs0, err)
     ctx.close()
 
 
