@@ -126,6 +126,9 @@ struct DevScalars {
     double relres, cn_relres, t_clip;
     double pcg_rz, pcg_zq;  // (r, z) and (z, q_old) of the current CG iteration (written as a pair)
     double pcg_pq, pcg_alpha, pcg_rz_old;
+    // the iteration's beta (for the direction) and alpha (for the update), each computed once by
+    // the last block of the reduction that completes its operands instead of in every thread
+    double pcg_beta, pcg_step;
     double relres0;  // relative residual of the initial iterate of the last pressure solve
     int mg_cycles, cn_cycles, cn_cycles_total, flags, go, clipped, steps;
     long long graph_launches;  // kernels executed by step-graph replays

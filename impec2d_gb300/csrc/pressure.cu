@@ -1426,11 +1426,12 @@ __device__ __forceinline__ double cg_z(const double* __restrict__ z, const float
     return z32 ? (double)z32[k] : z[k];
 }
 
-// (r, z) and (z, q) into out[0], out[1].
+// (r, z) and (z, q) into out[0], out[1].  With S (CG, out = &S->pcg_rz), the last block also
+// stores the direction's beta = -alpha_old (z, q) / (z, r)_old (0 on the first iteration).
 __global__ void __launch_bounds__(RED_THREADS) k_cg_dots(int n1, int n2, const double* __restrict__ r,
                                                          const double* __restrict__ z, const float* __restrict__ z32,
                                                          const double* __restrict__ q, double* partials, int mb,
-                                                         unsigned* counter, double* out) {
+                                                         unsigned* counter, double* out, DevScalars* S) {
     pdl_enter();
     double acc[2] = {0.0, 0.0};
     for_cells(n1, n2, [&](int, int, size_t k) {
@@ -1438,7 +1439,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_dots(int n1, int n2, const d
         acc[0] += r[k] * zz;
         acc[1] += zz * q[k];
     });
-    grid_reduce<2>(acc, 0u, partials, mb, counter, out);
+    if (grid_reduce<2>(acc, 0u, partials, mb, counter, out) && threadIdx.x == 0 && S) {
+        const bool first = S->mg_cycles == 0 || S->pcg_rz_old == 0.0;
+        S->pcg_beta = first ? 0.0 : -S->pcg_alpha * S->pcg_zq / S->pcg_rz_old;
+    }
 }
 
 // p = z + beta p (p = z on the first iteration, whatever p held).
@@ -1446,15 +1450,17 @@ __global__ void k_cg_direction(size_t n, const double* __restrict__ z, const flo
                                double* __restrict__ p, const DevScalars* __restrict__ S) {
     pdl_enter();
     const bool first = S->mg_cycles == 0 || S->pcg_rz_old == 0.0;
-    const double beta = first ? 0.0 : -S->pcg_alpha * S->pcg_zq / S->pcg_rz_old;
+    const double beta = S->pcg_beta;  // from k_cg_dots
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
         p[k] = first ? cg_z(z, z32, k) : cg_z(z, z32, k) + beta * p[k];
 }
 
-// q = A p with the integrated operator (diag p - sum t p_nb) and (p, q) into out[0].
+// q = A p with the integrated operator (diag p - sum t p_nb) and (p, q) into out[0].  With S
+// (CG, out = &S->pcg_pq), the last block also stores the update's alpha = (r, z) / (p, Ap)
+// (0 unless (p, Ap) > 0).
 __global__ void __launch_bounds__(RED_THREADS) k_cg_apply(Level F, const double* __restrict__ p,
                                                           double* __restrict__ q, double* partials, int mb,
-                                                          unsigned* counter, double* out) {
+                                                          unsigned* counter, double* out, DevScalars* S) {
     pdl_enter();
     double acc[1] = {0.0};
     for_cells(F.n1, F.n2, [&](int i, int j, size_t k) {
@@ -1476,7 +1482,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_apply(Level F, const double*
         q[k] = s;
         acc[0] += p[k] * s;
     });
-    grid_reduce<1>(acc, 0u, partials, mb, counter, out);
+    if (grid_reduce<1>(acc, 0u, partials, mb, counter, out) && threadIdx.x == 0 && S) {
+        const double pq = S->pcg_pq;
+        S->pcg_step = pq > 0.0 ? S->pcg_rz / pq : 0.0;
+    }
 }
 
 // alpha = (r, z) / (p, Ap); x += alpha p; r -= alpha Ap (and its FP32 copy); ||r||^2 over the
@@ -1489,8 +1498,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_update(int n1, int n2, doubl
                                                            unsigned* counter, double* out, double tol, int max_cycles,
                                                            cudaGraphConditionalHandle h, int use_h) {
     pdl_enter();
-    const double pq = S->pcg_pq;
-    const double alpha = pq > 0.0 ? S->pcg_rz / pq : 0.0;
+    const double alpha = S->pcg_step;  // from k_cg_apply
     double acc[1] = {0.0};
     for_cells(n1, n2, [&](int, int, size_t k) {
         x[k] += alpha * p[k];
@@ -1598,11 +1606,11 @@ static impec_status learned_guess(impec_ctx* ctx, double* x) {
     const int cap = red_cap(ctx->num_sms, ctx->max_blocks), blocks = seg_blocks(F.n1, F.n2, cap);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_cg_apply, blocks, RED_THREADS, 0, F, (const double*)ctx->lrn_d, ctx->lrn_Ad, ctx->partials,
-             ctx->max_blocks, ctx->counter, &S->pcg_pq);
+             ctx->max_blocks, ctx->counter, &S->pcg_pq, (DevScalars*)nullptr);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_cg_dots, blocks, RED_THREADS, 0, F.n1, F.n2, (const double*)ctx->lrn_r0,
              (const double*)ctx->lrn_d, (const float*)nullptr, (const double*)ctx->lrn_Ad, ctx->partials,
-             ctx->max_blocks, ctx->counter, &S->pcg_rz);
+             ctx->max_blocks, ctx->counter, &S->pcg_rz, (DevScalars*)nullptr);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_learn_step, ctx->num_sms * 4, 256, 0, F.n(), x, (const double*)ctx->lrn_d,
              (const DevScalars*)S, ctx->lrn_alpha);
@@ -1700,12 +1708,12 @@ impec_status pressure_iteration(impec_ctx* ctx, double tol, cudaGraphConditional
     const int cap = red_cap(ctx->num_sms, ctx->max_blocks), blocks = seg_blocks(F.n1, F.n2, cap);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_cg_dots, blocks, RED_THREADS, 0, F.n1, F.n2, r, z, z32, ctx->cg_q, ctx->partials,
-             ctx->max_blocks, ctx->counter, &S->pcg_rz);
+             ctx->max_blocks, ctx->counter, &S->pcg_rz, S);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_cg_direction, ctx->num_sms * 4, 256, 0, n, z, z32, ctx->cg_p, S);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_cg_apply, blocks, RED_THREADS, 0, F, ctx->cg_p, ctx->cg_q, ctx->partials,
-             ctx->max_blocks, ctx->counter, &S->pcg_pq);
+             ctx->max_blocks, ctx->counter, &S->pcg_pq, S);
     ++ctx->nlaunch;
     launch_k(ctx->stream, k_cg_update, blocks, RED_THREADS, 0, F.n1, F.n2, ctx->cg_x, r, mixed ? F.b32 : nullptr,
              (const double*)ctx->cg_p, (const double*)ctx->cg_q, pin_index(ctx), S, ctx->partials, ctx->max_blocks,
