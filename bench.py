@@ -793,7 +793,7 @@ def main():
 
     roof_small = E.roofline_probe(ctx, P, args.precision, flush=flush)
     # The dominant kernel's HBM roofline: the fine-level FP64 sweep where its data cannot stay
-    # in L2, at 4096^2 (BASELINE's large grid).  Inside the 1024^2 step the same sweep runs from
+    # in L2, at 4096^2 (the mixed-precision case's grid).  Inside the 1024^2 step the same sweep runs from
     # L2 (the whole hierarchy, ~150 MB, is about L2's size); its cold figure is kept beside it.
     roof_large = None
     if not args.no_large_roofline and args.nu == 1.0:

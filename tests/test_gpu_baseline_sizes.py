@@ -168,7 +168,7 @@ def test_transport_schemes_at_1024(engine, oracle_lib, scheme, mode):
 
 
 def test_reference_cpu_case_128_to_0p3_pore_volumes(engine, oracle_lib):
-    """BASELINE's CPU case: 128^2 diagonal, one-cell wells, upwind, porosity 0.2, M = 41, CFL 0.5,
+    """The small CPU-runnable case: 128^2 diagonal, one-cell wells, upwind, porosity 0.2, M = 41, CFL 0.5,
     pressure to 1e-10, to t = 0.06 = 0.3 phi |Omega| / I.  The reference's time step ignores the
     porosity its flux divides by (unstable at phi = 0.2); the engine scales it by phi
     (gb300.cfl_porosity), and the oracle gets the same step through cfl * phi."""
@@ -214,7 +214,7 @@ def test_reference_cpu_case_128_to_0p3_pore_volumes(engine, oracle_lib):
 
 @pytest.mark.parametrize("prec", [0, 1])
 def test_heterogeneous_4096_solve_against_oracle_multigrid(engine, oracle_lib, prec):
-    """BASELINE's mixed-precision case at full size: the FP64 and the FP32-in-FP64-refinement
+    """The mixed-precision pressure case at full size (4096^2): the FP64 and the FP32-in-FP64-refinement
     solves reach 1e-10 under the oracle's assembled (reference) system, and their solutions
     agree with the oracle's FP64 multigrid solution (warm-started from the GPU solution and run
     to 4e-11, where FP64 round-off floors the residual of the two-well problem at this size)
