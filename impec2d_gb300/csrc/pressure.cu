@@ -1848,16 +1848,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_maxvel(int n1, int n2, const do
                                                         double at, double dx, double* partials, int mb,
                                                         unsigned* counter, double* out) {
     pdl_enter();
-    double acc[2] = {0.0, -1.0e10};  // max velocity, max of -dt_diff
-    const double tiny = 2.2250738585072014e-308;
+    // acc[0]: the largest |u_i + u_i+1| or |v_j + v_j+1| of a cell.  The reference's cell speed is
+    // half of it, floored at the smallest normal double; both are applied once, to the maximum,
+    // by k_finish_dt (halving is exact, and a maximum commutes with both).
+    double acc[2] = {0.0, -1.0e10};  // max |face velocity sum|, max of -dt_diff
     for_cells(n1, n2, [&](int i, int j, size_t) {
-        double uij = 0.5 * (u[IX(i, j, n2)] + u[IX(i + 1, j, n2)]);
-        double vij = 0.5 * (v[IX(i, j, n2 + 1)] + v[IX(i, j + 1, n2 + 1)]);
-        double uc = fabs(uij), vc = fabs(vij);
-        if (uc < tiny) uc = tiny;
-        if (vc < tiny) vc = tiny;
-        acc[0] = fmax(acc[0], fmax(uc, vc));
+        const double su = u[IX(i, j, n2)] + u[IX(i + 1, j, n2)];
+        const double sv = v[IX(i, j, n2 + 1)] + v[IX(i, j + 1, n2 + 1)];
+        acc[0] = fmax(acc[0], fmax(fabs(su), fabs(sv)));
         if (diffusion) {
+            const double uij = 0.5 * su, vij = 0.5 * sv;
             double vij2 = vij * vij, uij2 = uij * uij;
             double absu = sqrt(vij2 + uij2);
             double d11 = dx / absu * (al * uij2 + at * vij2);
@@ -1871,7 +1871,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_maxvel(int n1, int n2, const do
 
 __global__ void k_finish_dt(DevScalars* S, double dx, double dy, double cfl, int use_diff, double limit) {
     pdl_enter();
-    double mv = S->red[0];
+    double mv = fmax(0.5 * S->red[0], 2.2250738585072014e-308);  // see k_maxvel
     S->maxvel = mv;
     double dt = fmin(dx / mv, dy / mv) * cfl;
     if (use_diff) {
